@@ -1,0 +1,110 @@
+"""corr_gb300: GB300-native correlation hot path of Masterluke87/corr.
+
+The Python side of the C ABI (include/corr_gb300.h).  ``Context`` owns one
+library context (device + stream + device workspace); array arguments may be
+numpy arrays (host) or torch tensors (host or CUDA).  The functions below
+mirror the reference's entry points (src/POSTHF/can_mp2.h, motrans.h, ri.h)
+with explicit sizes instead of the reference's structs.
+"""
+from __future__ import annotations
+
+import ctypes
+
+from ._lib import PRECISION, CorrError, MP2Energy, check, load
+
+__all__ = ["Context", "CorrError", "MP2Energy", "PRECISION", "default_context",
+           "run_canonical_mp2_ri"]
+
+
+def _ptr(x):
+    """Raw address of a numpy array or torch tensor (contiguous required)."""
+    if x is None:
+        return None
+    if hasattr(x, "data_ptr"):
+        if not x.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return ctypes.c_void_p(x.data_ptr())
+    if hasattr(x, "ctypes"):
+        if not x.flags["C_CONTIGUOUS"]:
+            raise ValueError("array must be C-contiguous")
+        return ctypes.c_void_p(x.ctypes.data)
+    raise TypeError(f"unsupported array type {type(x)!r}")
+
+
+def _prec(p):
+    if isinstance(p, str):
+        if p not in PRECISION:
+            raise ValueError(f"unknown precision {p!r}; choose from {sorted(PRECISION)}")
+        return PRECISION[p]
+    return int(p)
+
+
+class Context:
+    """One corr_gb300 context on `device`, ordered on `stream` (a
+    torch.cuda.Stream, a raw cudaStream_t integer, or None for the default
+    stream)."""
+
+    def __init__(self, device=0, stream=None):
+        self._L = load()
+        h = ctypes.c_void_p()
+        check(self._L.corr_create(ctypes.byref(h), int(device), self._stream_ptr(stream)))
+        self._h = h
+        self.device = int(device)
+
+    @staticmethod
+    def _stream_ptr(stream):
+        if stream is None:
+            return None
+        if hasattr(stream, "cuda_stream"):
+            return ctypes.c_void_p(stream.cuda_stream)
+        return ctypes.c_void_p(int(stream))
+
+    def set_stream(self, stream):
+        check(self._L.corr_set_stream(self._h, self._stream_ptr(stream)))
+
+    @property
+    def sm_count(self):
+        return self._L.corr_device_sm_count(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.corr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- RI-MP2 energy (src/POSTHF/can_mp2.cc:53) ---------------------------
+    def rimp2_energy(self, bia, eps, nocc, nvir, naux, precision="fp64"):
+        out = MP2Energy()
+        check(self._L.corr_rimp2_energy(self._h, int(nocc), int(nvir), int(naux), _ptr(bia),
+                                        _ptr(eps), _prec(precision), ctypes.byref(out)))
+        return out
+
+
+_DEFAULT = None
+
+
+def default_context():
+    global _DEFAULT
+    if _DEFAULT is None:
+        _DEFAULT = Context(0)
+    return _DEFAULT
+
+
+def run_canonical_mp2_ri(nroe, nroao, naux_2, Bia, FMo_diag, precision="fp64", ctx=None):
+    """Mirror of run_canonical_mp2_ri(systeminfo*, pHF*) (can_mp2.cc:53):
+    nroe electrons, nroao orbitals, naux_2 auxiliary functions, Bia[Q][i][a],
+    FMo_diag[nroao] = orbital energies.  Returns MP2Energy."""
+    nocc = nroe // 2
+    return (ctx or default_context()).rimp2_energy(Bia, FMo_diag, nocc, nroao - nocc, naux_2,
+                                                   precision)

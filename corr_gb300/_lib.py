@@ -1,0 +1,90 @@
+"""ctypes binding of libcorr_gb300.so (the C ABI declared in include/corr_gb300.h).
+
+The library is built in-tree (corr_gb300/build.py).  There is no fallback: if
+the shared library is missing, loading raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+LIB_PATH = os.path.join(PKG, "libcorr_gb300.so")
+HEADER = os.path.join(ROOT, "include", "corr_gb300.h")
+
+CORR_OK = 0
+STATUS = {
+    0: "CORR_OK", 1: "CORR_ERR_BAD_ARG", 2: "CORR_ERR_OOM", 3: "CORR_ERR_NOT_PD",
+    4: "CORR_ERR_DEVICE_TIMEOUT", 5: "CORR_ERR_CUDA", 6: "CORR_ERR_NO_DEVICE",
+    7: "CORR_ERR_NUMERIC",
+}
+PRECISION = {"fp64": 0, "split_fp16": 1, "split_bf16": 2}
+
+
+class CorrError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class MP2Energy(ctypes.Structure):
+    _fields_ = [("e_ss", ctypes.c_double), ("e_os", ctypes.c_double),
+                ("e_total", ctypes.c_double), ("e_scs", ctypes.c_double)]
+
+    def as_tuple(self):
+        return (self.e_ss, self.e_os, self.e_total)
+
+    def __repr__(self):
+        return (f"MP2Energy(e_ss={self.e_ss!r}, e_os={self.e_os!r}, e_total={self.e_total!r}, "
+                f"e_scs={self.e_scs!r})")
+
+
+_vp = ctypes.c_void_p
+_i = ctypes.c_int
+_ll = ctypes.c_longlong
+_d = ctypes.c_double
+
+# name -> argtypes (restype int unless listed in _RESTYPES)
+SIGNATURES = {
+    "corr_version": [],
+    "corr_create": [ctypes.POINTER(_vp), _i, _vp],
+    "corr_destroy": [_vp],
+    "corr_set_stream": [_vp, _vp],
+    "corr_last_error": [],
+    "corr_device_sm_count": [_vp],
+    "corr_rimp2_energy": [_vp, _i, _i, _i, _vp, _vp, _i, ctypes.POINTER(MP2Energy)],
+}
+_RESTYPES = {"corr_version": ctypes.c_char_p, "corr_last_error": ctypes.c_char_p}
+
+_LIB = None
+
+
+def header_symbols():
+    """Every function the public header declares."""
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\*?\s+\**(corr_\w+)\(", text, re.M)))
+
+
+def load():
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"{LIB_PATH} is missing: build it with corr_gb300.build.build() "
+                "(there is no CPU fallback)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, args in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = _RESTYPES.get(name, ctypes.c_int)
+        _LIB = L
+    return _LIB
+
+
+def check(status):
+    if status != CORR_OK:
+        msg = load().corr_last_error()
+        raise CorrError(status, msg.decode() if msg else "")
+    return status

@@ -1,0 +1,300 @@
+// C-ABI layer: context, status/error reporting, host/device argument staging,
+// TMA descriptor encoding and dispatch of the RI-MP2 energy kernels.
+#include <cudaTypedefs.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "abi_internal.h"
+#include "common.cuh"
+#include "kernels.h"
+
+namespace corr {
+
+static thread_local char g_err[1024] = "";
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+EnergyShape make_energy_shape(int nocc, int nvir, int naux, int tile) {
+  EnergyShape s;
+  s.nocc = nocc;
+  s.nvir = nvir;
+  s.naux = naux;
+  s.tile = tile;
+  s.ntiles = (nvir + tile - 1) / tile;
+  s.npairs = nocc * (nocc + 1) / 2;
+  s.ntpairs = s.ntiles * (s.ntiles + 1) / 2;
+  s.nunits = (long long)s.npairs * s.ntpairs;
+  return s;
+}
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// ---------------------------------------------------------------------------
+// workspace: one grow-only device buffer per context, carved per call
+// ---------------------------------------------------------------------------
+int Workspace::reserve(size_t bytes) {
+  if (bytes <= cap) return CORR_OK;
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  cap = 0;
+  size_t want = bytes + bytes / 8;
+  if (cudaMalloc(&ptr, want) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("device allocation of %zu bytes failed", want);
+    return CORR_ERR_OOM;
+  }
+  cap = want;
+  return CORR_OK;
+}
+
+void* Carver::take(size_t bytes) {
+  size_t at = (used + 255) & ~(size_t)255;
+  used = at + bytes;
+  return base ? static_cast<char*>(base) + at : nullptr;
+}
+
+// Stage a caller array on the device: device pointers pass through, host
+// pointers are copied into `slot` on the context stream.
+const void* stage_in(corr_context* c, const void* p, size_t bytes, void* slot) {
+  if (is_device_ptr(p)) return p;
+  if (cudaMemcpyAsync(slot, p, bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
+    return nullptr;
+  return slot;
+}
+
+int stage_out(corr_context* c, void* dst, const void* src, size_t bytes) {
+  if (dst == src) return CORR_OK;
+  CORR_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, c->stream));
+  return CORR_OK;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    cudaGetLastError();
+  });
+  return fn;
+}
+
+int encode_tmap(CUtensorMap* m, CUtensorMapDataType dt, int rank, void* base,
+                const uint64_t* dims, const uint64_t* strides_bytes, const uint32_t* box,
+                CUtensorMapSwizzle swz) {
+  auto enc = tmap_encoder();
+  if (!enc) {
+    set_error("cuTensorMapEncodeTiled unavailable");
+    return CORR_ERR_CUDA;
+  }
+  cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  CUresult r = enc(m, dt, (cuuint32_t)rank, base, (const cuuint64_t*)dims,
+                   (const cuuint64_t*)strides_bytes, (const cuuint32_t*)box, es,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return CORR_ERR_CUDA;
+  }
+  return CORR_OK;
+}
+
+// Finish a call: copy the small result block back, synchronise, check the
+// device status word and the finiteness of the results.
+int finish_results(corr_context* c, int nres) {
+  CORR_CUDA(cudaMemcpyAsync(c->hres, c->dres, sizeof(ResultBlock), cudaMemcpyDeviceToHost,
+                            c->stream));
+  CORR_CUDA(cudaStreamSynchronize(c->stream));
+  if (c->hres->status & CORR_ERR_DEVICE_TIMEOUT) {
+    set_error("a device-side wait exceeded its time limit");
+    return CORR_ERR_DEVICE_TIMEOUT;
+  }
+  for (int k = 0; k < nres; ++k)
+    if (!std::isfinite(c->hres->e[k])) {
+      set_error("non-finite energy (zero denominator or non-finite input)");
+      return CORR_ERR_NUMERIC;
+    }
+  return CORR_OK;
+}
+
+}  // namespace corr
+
+using namespace corr;
+
+extern "C" {
+
+const char* corr_version(void) { return "corr_gb300 0.1.0 (sm_103a)"; }
+
+const char* corr_last_error(void) { return g_err; }
+
+int corr_create(corr_context** out, int device, void* stream) {
+  CORR_CHECK_ARG(out != nullptr, "corr_create: null output pointer");
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    set_error("no CUDA device visible");
+    return CORR_ERR_NO_DEVICE;
+  }
+  CORR_CHECK_ARG(device >= 0 && device < n, "corr_create: device %d out of range", device);
+  cudaDeviceProp prop;
+  CORR_CUDA(cudaGetDeviceProperties(&prop, device));
+  if (prop.major != 10 || prop.minor != 3) {
+    set_error("device %d is sm_%d%d; this library is built for sm_103a", device, prop.major,
+              prop.minor);
+    return CORR_ERR_NO_DEVICE;
+  }
+  CORR_CUDA(cudaSetDevice(device));
+  corr_context* c = new corr_context();
+  c->device = device;
+  c->stream = static_cast<cudaStream_t>(stream);
+  c->sms = prop.multiProcessorCount;
+  if (cudaMalloc(&c->dres, sizeof(ResultBlock)) != cudaSuccess ||
+      cudaMallocHost(&c->hres, sizeof(ResultBlock)) != cudaSuccess) {
+    cudaGetLastError();
+    delete c;
+    set_error("corr_create: allocation failed");
+    return CORR_ERR_OOM;
+  }
+  *out = c;
+  return CORR_OK;
+}
+
+int corr_destroy(corr_context* c) {
+  if (!c) return CORR_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  if (c->ws.ptr) cudaFree(c->ws.ptr);
+  if (c->dres) cudaFree(c->dres);
+  if (c->hres) cudaFreeHost(c->hres);
+  delete c;
+  return CORR_OK;
+}
+
+int corr_set_stream(corr_context* c, void* stream) {
+  CORR_CHECK_ARG(c != nullptr, "null context");
+  c->stream = static_cast<cudaStream_t>(stream);
+  return CORR_OK;
+}
+
+int corr_device_sm_count(const corr_context* c) { return c ? c->sms : 0; }
+
+int corr_rimp2_energy(corr_context* c, int nocc, int nvir, int naux, const double* bia,
+                      const double* eps, int precision, corr_mp2_energy* out) {
+  CORR_CHECK_ARG(c != nullptr, "null context");
+  CORR_CHECK_ARG(out != nullptr && bia != nullptr && eps != nullptr,
+                 "corr_rimp2_energy: null pointer argument");
+  CORR_CHECK_ARG(nocc >= 1 && nvir >= 1 && naux >= 1,
+                 "corr_rimp2_energy: sizes must be positive (nocc=%d nvir=%d naux=%d)", nocc, nvir,
+                 naux);
+  CORR_CHECK_ARG(precision >= CORR_PREC_FP64 && precision <= CORR_PREC_SPLIT_BF16,
+                 "corr_rimp2_energy: unknown precision %d", precision);
+  CORR_CHECK_ARG((long long)nocc * nvir <= (1ll << 31) && nocc <= 46000,
+                 "corr_rimp2_energy: nocc*nvir too large");
+  CORR_CUDA(cudaSetDevice(c->device));
+  int st = rimp2_energy_device(c, nocc, nvir, naux, bia, eps, precision);
+  if (st != CORR_OK) return st;
+  CORR_TRY(finish_results(c, 4));
+  out->e_ss = c->hres->e[0];
+  out->e_os = c->hres->e[1];
+  out->e_total = c->hres->e[2];
+  out->e_scs = c->hres->e[3];
+  return CORR_OK;
+}
+
+}  // extern "C"
+
+namespace corr {
+
+// Enqueue the whole energy evaluation on the context stream; results land in
+// c->dres.  Shared by the public entry point and the batched driver.
+int rimp2_energy_device(corr_context* c, int nocc, int nvir, int naux, const double* bia,
+                        const double* eps, int precision) {
+  const size_t nb = (size_t)naux * nocc * nvir;
+  const size_t ne = (size_t)nocc + nvir;
+  const bool b_dev = is_device_ptr(bia), e_dev = is_device_ptr(eps);
+  const int Qp = ((naux + 31) / 32) * 32;
+  const EnergyShape sh =
+      make_energy_shape(nocc, nvir, naux, precision == CORR_PREC_FP64 ? kF64Tile : kTcTile);
+  int grid = precision == CORR_PREC_FP64 ? c->sms * 2 : c->sms;
+  if ((long long)grid > sh.nunits) grid = (int)sh.nunits;
+
+  // size the workspace
+  Carver cv{nullptr, 0};
+  if (!b_dev) cv.take(nb * 8);
+  if (!e_dev) cv.take(ne * 8);
+  if (precision != CORR_PREC_FP64) {
+    cv.take((size_t)nocc * nvir * Qp * 2);
+    cv.take((size_t)nocc * nvir * Qp * 2);
+  }
+  cv.take((size_t)grid * 16);
+  cv.take(64);
+  CORR_TRY(c->ws.reserve(cv.used));
+  Carver w{c->ws.ptr, 0};
+  void* b_slot = b_dev ? nullptr : w.take(nb * 8);
+  void* e_slot = e_dev ? nullptr : w.take(ne * 8);
+  void* hi = nullptr;
+  void* lo = nullptr;
+  if (precision != CORR_PREC_FP64) {
+    hi = w.take((size_t)nocc * nvir * Qp * 2);
+    lo = w.take((size_t)nocc * nvir * Qp * 2);
+  }
+  double* partials = static_cast<double*>(w.take((size_t)grid * 16));
+  char* misc = static_cast<char*>(w.take(64));
+  unsigned long long* dmax = reinterpret_cast<unsigned long long*>(misc);
+  double* scale = reinterpret_cast<double*>(misc + 8);
+
+  const double* d_b = static_cast<const double*>(stage_in(c, bia, nb * 8, b_slot));
+  const double* d_e = static_cast<const double*>(stage_in(c, eps, ne * 8, e_slot));
+  if (!d_b || !d_e) {
+    set_error("host-to-device copy failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return CORR_ERR_CUDA;
+  }
+  CORR_CUDA(cudaMemsetAsync(c->dres, 0, sizeof(ResultBlock), c->stream));
+
+  if (precision == CORR_PREC_FP64) {
+    CORR_CUDA(launch_energy_fp64(d_b, d_e, sh, partials, grid, c->stream));
+    CORR_CUDA(launch_energy_reduce(partials, grid, nullptr, c->dres->e, c->stream));
+    return CORR_OK;
+  }
+  const int fmt = precision == CORR_PREC_SPLIT_FP16 ? 0 : 1;
+  CORR_CUDA(cudaMemsetAsync(dmax, 0, 8, c->stream));
+  CORR_CUDA(launch_maxabs(d_b, (long long)nb, dmax, c->sms, c->stream));
+  CORR_CUDA(launch_split(d_b, naux, (long long)nocc * nvir, Qp, fmt, dmax, hi, lo, scale,
+                         c->stream));
+  CUtensorMap mh, ml;
+  const uint64_t dims[3] = {(uint64_t)Qp, (uint64_t)nvir, (uint64_t)nocc};
+  const uint64_t strides[2] = {(uint64_t)Qp * 2, (uint64_t)nvir * Qp * 2};
+  const uint32_t box[3] = {32, (uint32_t)kTcTile, 1};
+  const CUtensorMapDataType dt =
+      fmt == 0 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+  CORR_TRY(encode_tmap(&mh, dt, 3, hi, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_64B));
+  CORR_TRY(encode_tmap(&ml, dt, 3, lo, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_64B));
+  CORR_CUDA(launch_energy_tc(mh, ml, d_e, sh, Qp, fmt, partials, grid, &c->dres->status,
+                             c->stream));
+  CORR_CUDA(launch_energy_reduce(partials, grid, scale, c->dres->e, c->stream));
+  return CORR_OK;
+}
+
+}  // namespace corr

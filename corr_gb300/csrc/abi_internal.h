@@ -1,0 +1,54 @@
+// Context internals shared by the C-ABI translation units.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/corr_gb300.h"
+
+namespace corr {
+
+// Small result block the kernels write and one D2H copy brings back.
+struct ResultBlock {
+  double e[8];
+  int status;  // bit flags raised by device code (CORR_ERR_DEVICE_TIMEOUT)
+  int pad;
+};
+
+struct Workspace {
+  void* ptr = nullptr;
+  size_t cap = 0;
+  int reserve(size_t bytes);
+};
+
+// Bump allocator over a workspace (base == nullptr: size pass only).
+struct Carver {
+  void* base;
+  size_t used;
+  void* take(size_t bytes);
+};
+
+bool is_device_ptr(const void* p);
+int encode_tmap(CUtensorMap* m, CUtensorMapDataType dt, int rank, void* base, const uint64_t* dims,
+                const uint64_t* strides_bytes, const uint32_t* box, CUtensorMapSwizzle swz);
+
+}  // namespace corr
+
+struct corr_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int sms = 0;
+  corr::Workspace ws;
+  corr::ResultBlock* dres = nullptr;  // device
+  corr::ResultBlock* hres = nullptr;  // pinned host
+};
+
+namespace corr {
+const void* stage_in(corr_context* c, const void* p, size_t bytes, void* slot);
+int stage_out(corr_context* c, void* dst, const void* src, size_t bytes);
+int finish_results(corr_context* c, int nres);
+int rimp2_energy_device(corr_context* c, int nocc, int nvir, int naux, const double* bia,
+                        const double* eps, int precision);
+}  // namespace corr

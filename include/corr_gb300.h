@@ -1,0 +1,103 @@
+/*
+ * corr_gb300 -- GB300 (sm_103a) implementation of the correlation hot path of
+ * Masterluke87/corr: build_FMo, the AO->MO 4-index transform, canonical MP2,
+ * the RI metric J^-1/2 and B build, the RI transform and the RI-MP2 energy,
+ * plus an RI-MP2 adjoint and a batched RI-MP2 driver.
+ *
+ * Plain C ABI: opaque context handle, int status codes, caller-owned buffers
+ * given as plain pointers with explicit sizes.  Every array argument may live
+ * in host memory (pageable or pinned) or in device memory of the context's
+ * GPU; the library detects which and stages host data through its own device
+ * buffers.  Layouts are row-major and follow the reference's arrays:
+ *   mos[p*N + mu]            MO coefficients, one MO per row (OEints::MOs)
+ *   fmat, fmo [N*N]          Fock matrix in AO / MO basis (OEints::Fmat, pHF::FMo)
+ *   bpq[(P*N + mu)*N + nu]   B^P_mu,nu                     (pHF::BPQ)
+ *   bia[(Q*nocc + i)*nvir+a] B^Q_ia                        (pHF::Bia)
+ *   prec[((i*N+j)*N+k)*N+l]  MO integrals (ij|kl)          (pHF::prec_ints)
+ *   intval[n], intnums[4n], sortcount[4]  packed AO ERIs   (TEints)
+ * Orbital energies eps[p] are the diagonal FMo[p*N+p] the reference reads.
+ *
+ * There is no CPU fallback: every entry point runs on the GPU or returns an
+ * error status (CORR_ERR_NO_DEVICE when no GPU is visible).
+ */
+#ifndef CORR_GB300_H
+#define CORR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum corr_status {
+  CORR_OK = 0,
+  CORR_ERR_BAD_ARG = 1,        /* invalid size, null pointer, bad enum value   */
+  CORR_ERR_OOM = 2,            /* device allocation failed                     */
+  CORR_ERR_NOT_PD = 3,         /* RI metric has no positive eigenvalue         */
+  CORR_ERR_DEVICE_TIMEOUT = 4, /* a bounded device-side wait gave up           */
+  CORR_ERR_CUDA = 5,           /* any other CUDA runtime error                 */
+  CORR_ERR_NO_DEVICE = 6,      /* no usable sm_103 GPU                          */
+  CORR_ERR_NUMERIC = 7         /* non-finite input or zero energy denominator  */
+};
+
+/* Arithmetic of the RI-MP2 contraction (ia|jb) = sum_Q B^Q_ia B^Q_jb. */
+enum corr_precision {
+  CORR_PREC_FP64 = 0,       /* FP64 end to end                                   */
+  CORR_PREC_SPLIT_FP16 = 1, /* B = hi + lo in FP16 (power-of-two pre-scale), three
+                               products hi.hi + hi.lo + lo.hi on tcgen05, FP32
+                               accumulation in TMEM, FP64 pair-energy sum        */
+  CORR_PREC_SPLIT_BF16 = 2  /* the same with BF16 hi/lo                          */
+};
+
+typedef struct corr_context corr_context;
+
+/* Closed-shell MP2 energy pieces, as printed by the reference
+ * (can_mp2.cc:36-46, 114-125): E_SS, E_OS, E = E_SS + E_OS and the
+ * spin-component-scaled E_SCS = E_SS/3 + 6/5 E_OS. */
+typedef struct corr_mp2_energy {
+  double e_ss;
+  double e_os;
+  double e_total;
+  double e_scs;
+} corr_mp2_energy;
+
+/* ---- context ----------------------------------------------------------- */
+
+/* Library version string. */
+const char* corr_version(void);
+
+/* Create a context bound to CUDA device `device`.  `stream` is a
+ * cudaStream_t (NULL = the legacy default stream); all work of the context
+ * is ordered on it.  Returns CORR_ERR_NO_DEVICE without a usable GPU. */
+int corr_create(corr_context** ctx, int device, void* stream);
+
+/* Release the context and every device buffer it owns. */
+int corr_destroy(corr_context* ctx);
+
+/* Re-bind the context to another stream. */
+int corr_set_stream(corr_context* ctx, void* stream);
+
+/* Human-readable description of the last error raised on this thread. */
+const char* corr_last_error(void);
+
+/* Number of SMs of the context's GPU. */
+int corr_device_sm_count(const corr_context* ctx);
+
+/* ---- RI-MP2 energy ----------------------------------------------------- */
+
+/* Replaces run_canonical_mp2_ri (src/POSTHF/can_mp2.cc:53-132, declared at
+ * src/POSTHF/can_mp2.h:5): E_OS = -sum (ia|jb)^2 / D,
+ * E_SS = -sum [(ia|jb)-(ib|ja)](ia|jb) / D, D = e_a + e_b - e_i - e_j, with
+ * (ia|jb) = sum_Q B^Q_ia B^Q_jb.  bia[(Q*nocc+i)*nvir+a] (pHF::Bia),
+ * eps[nocc+nvir] (the diagonal of pHF::FMo).  The (ia|jb) tiles live only in
+ * registers/TMEM; no 4-index tensor is stored.  `precision` is a
+ * corr_precision. */
+int corr_rimp2_energy(corr_context* ctx, int nocc, int nvir, int naux, const double* bia,
+                      const double* eps, int precision, corr_mp2_energy* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CORR_GB300_H */

@@ -1,0 +1,313 @@
+// Test infrastructure: the reference-oracle harness.
+//
+// Compiled together with the reference's own, unmodified sources
+// (src/POSTHF/{motrans,can_mp2,ri}.cc, src/SCF/{ops_rhf,scf}.cc,
+// src/MATH/ops_mat.cc, src/IO/ops_io.cc) into oracle/_ref/libcorr_ref.so by
+// oracle/Makefile.  Each extern "C" entry point fills the reference's structs
+// (src/UTIL/util.h:7-65), calls one reference function, captures what it
+// prints at 17 significant digits and copies its outputs into caller buffers.
+// Only the tests and the golden-fixture script load this library; it is the
+// checker, never the product.
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <iostream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "MATH/ops_mat.h"
+#include "POSTHF/can_mp2.h"
+#include "POSTHF/motrans.h"
+#include "POSTHF/ri.h"
+#include "SCF/ops_rhf.h"
+#include "SCF/scf.h"
+#include "UTIL/util.h"
+
+namespace corr_oracle_tables {
+int N = 0, X = 0;
+const double* S = nullptr;
+const double* T = nullptr;
+const double* V = nullptr;
+const double* eri = nullptr;
+const double* J = nullptr;
+const double* P3 = nullptr;
+}  // namespace corr_oracle_tables
+
+// Fortran LAPACK/BLAS names the reference declares itself (ops_mat.h:14,
+// scf.cc:13-31), forwarded to scipy's prefixed OpenBLAS exports.
+extern "C" {
+void scipy_dsyev_(char*, char*, int*, double*, int*, double*, double*, int*, int*);
+void scipy_dgels_(char*, int*, int*, int*, double*, int*, double*, int*, double*, int*, int*);
+int scipy_dgemm_(char*, char*, int*, int*, int*, double*, double*, int*, double*, int*, double*,
+                 double*, int*);
+int scipy_daxpy_(int*, double*, double*, int*, double*, int*);
+double scipy_ddot_(int*, double*, int*, double*, int*);
+void scipy_dgesv_(int*, int*, double*, int*, int*, double*, int*, int*);
+void scipy_openblas_set_num_threads(int);
+
+void dsyev_(char* a, char* b, int* n, double* A, int* lda, double* w, double* work, int* lwork,
+            int* info) {
+  scipy_dsyev_(a, b, n, A, lda, w, work, lwork, info);
+}
+void dgels_(char* m, int* a, int* b, int* c, double* A, int* lda, double* B, int* ldb, double* w,
+            int* lw, int* info) {
+  scipy_dgels_(m, a, b, c, A, lda, B, ldb, w, lw, info);
+}
+int dgemm_(char* ta, char* tb, int* m, int* n, int* k, double* al, double* A, int* lda, double* B,
+           int* ldb, double* be, double* C, int* ldc) {
+  return scipy_dgemm_(ta, tb, m, n, k, al, A, lda, B, ldb, be, C, ldc);
+}
+int daxpy_(int* n, double* a, double* x, int* ix, double* y, int* iy) {
+  return scipy_daxpy_(n, a, x, ix, y, iy);
+}
+double ddot_(int* n, double* x, int* ix, double* y, int* iy) { return scipy_ddot_(n, x, ix, y, iy); }
+void dgesv_(int* n, int* r, double* a, int* lda, int* p, double* b, int* ldb, int* info) {
+  scipy_dgesv_(n, r, a, lda, p, b, ldb, info);
+}
+}
+
+namespace {
+
+// Redirect std::cout into a buffer for the duration of one reference call.
+struct Capture {
+  std::ostringstream buf;
+  std::streambuf* old;
+  std::ios_base::fmtflags flags;
+  std::streamsize prec;
+  Capture() {
+    old = std::cout.rdbuf(buf.rdbuf());
+    flags = std::cout.flags();
+    prec = std::cout.precision();
+    std::cout.unsetf(std::ios_base::floatfield);
+    std::cout.precision(17);
+  }
+  ~Capture() {
+    std::cout.rdbuf(old);
+    std::cout.flags(flags);
+    std::cout.precision(prec);
+  }
+};
+
+// Value printed after `key` that follows the first occurrence of `block`.
+double grab(const std::string& text, const char* block, const char* key) {
+  size_t p = text.find(block);
+  if (p == std::string::npos) return 0.0;
+  p = text.find(key, p);
+  if (p == std::string::npos) return 0.0;
+  return std::strtod(text.c_str() + p + std::strlen(key), nullptr);
+}
+
+std::string g_last_output;
+
+}  // namespace
+
+extern "C" {
+
+void ref_set_threads(int n) { scipy_openblas_set_num_threads(n); }
+
+const char* ref_last_output() { return g_last_output.c_str(); }
+
+// src/POSTHF/can_mp2.cc:53 run_canonical_mp2_ri.  Bia[Q][i][a]; eps has nroao
+// entries and becomes the diagonal of FMo.  out = {EMP2_SS, EMP2_OS, EMP2}.
+void ref_rimp2_energy(int nocc, int nvir, int naux, const double* Bia, const double* eps,
+                      double* out) {
+  int nroao = nocc + nvir;
+  systeminfo si;
+  si.nroe = 2 * nocc;
+  si.nroao = nroao;
+  si.naux_2 = naux;
+  std::vector<double> fmo((size_t)nroao * nroao, 0.0);
+  for (int p = 0; p < nroao; ++p) fmo[(size_t)p * nroao + p] = eps[p];
+  pHF ph;
+  ph.FMo = fmo.data();
+  ph.Bia = const_cast<double*>(Bia);
+  std::string text;
+  {
+    Capture c;
+    run_canonical_mp2_ri(&si, &ph);
+    text = c.buf.str();
+  }
+  g_last_output = text;
+  out[0] = grab(text, "RI-MP2-Results", "EMP2_SS:");
+  out[1] = grab(text, "RI-MP2-Results", "EMP2_OS:");
+  out[2] = grab(text, "RI-MP2-Results", "EMP2:");
+}
+
+// src/POSTHF/can_mp2.cc:11 run_canonical_mp2 on a full [N][N][N][N] MO tensor.
+void ref_canonical_mp2(int nroe, int nroao, const double* prec_ints, const double* fmo,
+                       double* out) {
+  systeminfo si;
+  si.nroe = nroe;
+  si.nroao = nroao;
+  pHF ph;
+  ph.FMo = const_cast<double*>(fmo);
+  ph.prec_ints = const_cast<double*>(prec_ints);
+  std::string text;
+  {
+    Capture c;
+    run_canonical_mp2(&si, &ph);
+    text = c.buf.str();
+  }
+  g_last_output = text;
+  out[0] = grab(text, "MP2-Results", "EMP2_SS:");
+  out[1] = grab(text, "MP2-Results", "EMP2_OS:");
+  out[2] = grab(text, "MP2-Results", "EMP2:");
+}
+
+// src/POSTHF/motrans.cc:8 build_FMo.
+void ref_build_fmo(int nroao, const double* mos, const double* fmat, double* fmo_out) {
+  systeminfo si;
+  si.nroao = nroao;
+  OEints oe;
+  oe.MOs = const_cast<double*>(mos);
+  oe.Fmat = const_cast<double*>(fmat);
+  pHF ph;
+  build_FMo(&si, &oe, &ph);
+  std::memcpy(fmo_out, ph.FMo, sizeof(double) * nroao * nroao);
+  delete[] ph.FMo;
+}
+
+// src/SCF/ops_rhf.cc:618 calculate_libint_tei (screening, unique selection)
+// followed by its resort_integrals (ops_rhf.cc:750).  Two calls: with
+// intval == nullptr only the count is returned.
+static std::vector<double> g_intval;
+static std::vector<unsigned short> g_intnums;
+static long long g_sortcount[4];
+
+long long ref_pack_eri(int nroao, const double* eri) {
+  corr_oracle_tables::N = nroao;
+  corr_oracle_tables::eri = eri;
+  libint2::BasisSet obs(0, nroao);
+  systeminfo si;
+  si.nroao = nroao;
+  TEints te;
+  {
+    Capture c;
+    calculate_libint_tei(&si, obs, &te);
+  }
+  g_intval.assign(te.intval, te.intval + si.nrofint);
+  g_intnums.assign(te.intnums, te.intnums + 4 * si.nrofint);
+  for (int k = 0; k < 4; ++k) g_sortcount[k] = te.sortcount[k];
+  delete[] te.intval;
+  delete[] te.intnums;
+  return si.nrofint;
+}
+
+void ref_packed_copy(double* intval, unsigned short* intnums, long long* sortcount) {
+  std::memcpy(intval, g_intval.data(), sizeof(double) * g_intval.size());
+  std::memcpy(intnums, g_intnums.data(), sizeof(unsigned short) * g_intnums.size());
+  for (int k = 0; k < 4; ++k) sortcount[k] = g_sortcount[k];
+}
+
+// src/POSTHF/motrans.cc:35 MOtrans.  Its mo2int_op keeps function-static
+// buffers sized by the first nroao seen, so one process may only use one
+// nroao (the golden script runs each case in its own process).
+void ref_motrans(int nroe, int nroao, const double* mos, long long nrofint,
+                 const long long* sortcount, const double* intval, const unsigned short* intnums,
+                 double* prec_out) {
+  systeminfo si;
+  si.nroe = nroe;
+  si.nroao = nroao;
+  si.nrofint = nrofint;
+  OEints oe;
+  oe.MOs = const_cast<double*>(mos);
+  TEints te;
+  te.intval = const_cast<double*>(intval);
+  te.intnums = const_cast<unsigned short*>(intnums);
+  for (int k = 0; k < 4; ++k) te.sortcount[k] = sortcount[k];
+  pHF ph;
+  {
+    Capture c;
+    MOtrans(&si, &oe, &te, &ph);
+  }
+  size_t n4 = (size_t)nroao * nroao * nroao * nroao;
+  std::memcpy(prec_out, ph.prec_ints, sizeof(double) * n4);
+  delete[] ph.prec_ints;
+}
+
+// src/POSTHF/motrans.cc:286 calc_mo2int_bf (single element, brute force).
+double ref_mo2int_bf(int i, int j, int k, int l, int nroao, const double* mos, long long nrofint,
+                     const long long* sortcount, const double* intval,
+                     const unsigned short* intnums) {
+  return calc_mo2int_bf(i, j, k, l, nroao, const_cast<double*>(mos), nrofint,
+                        const_cast<long long*>(sortcount), const_cast<double*>(intval),
+                        const_cast<unsigned short*>(intnums));
+}
+
+// src/POSTHF/ri.cc:7 calculate_ri on registered (P|Q) and (P|mn) tables:
+// dsyev, the 1e-10 relative eigenvalue cutoff, J^-1/2 and BPQ = J^-1/2 (Q|mn).
+void ref_calculate_ri(int naux, int nroao, const double* J, const double* P3, double* bpq_out) {
+  corr_oracle_tables::N = nroao;
+  corr_oracle_tables::X = naux;
+  corr_oracle_tables::J = J;
+  corr_oracle_tables::P3 = P3;
+  libint2::BasisSet obs(0, nroao), dfbs(1, naux);
+  calculate_ri(obs, dfbs, bpq_out);
+}
+
+// src/POSTHF/ri.cc:147 transform_ri.  Bia[Q][i][a].
+void ref_transform_ri(int nroe, int nroao, int naux, const double* mos, const double* bpq,
+                      double* bia_out) {
+  systeminfo si;
+  si.nroe = nroe;
+  si.nroao = nroao;
+  si.naux_2 = naux;
+  OEints oe;
+  oe.MOs = const_cast<double*>(mos);
+  pHF ph;
+  ph.BPQ = const_cast<double*>(bpq);
+  ph.Bia = bia_out;
+  transform_ri(&si, &oe, &ph);
+}
+
+// The reference's RHF (src/main.cc:102-117): calc_S12, core guess
+// (check_initial_guess, ops_rhf.cc:15), run_scf (scf.cc:145) with 100
+// iterations.  Inputs S, T, V (H = T + V) and the packed ERIs; outputs the MO
+// coefficients [p][mu], the final Fock matrix and the MO energies.
+// out_e = {total HF energy}.
+void ref_rhf(int nroe, int nroao, double ion_rep, const double* S, const double* T,
+             const double* V, long long nrofint, const long long* sortcount, const double* intval,
+             const unsigned short* intnums, double* mos_out, double* fmat_out, double* moens_out,
+             double* out_e) {
+  systeminfo si;
+  si.nroe = nroe;
+  si.nroao = nroao;
+  si.nrofint = nrofint;
+  si.ion_rep = ion_rep;
+  si.scfiter = 100;
+  OEints oe;
+  allocate_onemats(&si, &oe);
+  size_t n2 = (size_t)nroao * nroao;
+  for (size_t x = 0; x < n2; ++x) {
+    oe.Smat[x] = S[x];
+    oe.Tmat[x] = T[x];
+    oe.Vmat[x] = V[x];
+    oe.Hmat[x] = T[x] + V[x];
+    oe.MOs[x] = 0.0;
+    oe.Pmat[x] = 0.0;
+    oe.Fmat[x] = 0.0;
+  }
+  TEints te;
+  te.intval = const_cast<double*>(intval);
+  te.intnums = const_cast<unsigned short*>(intnums);
+  for (int k = 0; k < 4; ++k) te.sortcount[k] = sortcount[k];
+  std::string text;
+  {
+    Capture c;
+    calc_S12(&si, &oe);
+    check_initial_guess(&si, &oe);
+    run_scf(&si, &oe, &te);
+    std::cout.unsetf(std::ios_base::floatfield);
+    std::cout.precision(17);
+    text = c.buf.str();
+  }
+  g_last_output = text;
+  std::memcpy(mos_out, oe.MOs, sizeof(double) * n2);
+  std::memcpy(fmat_out, oe.Fmat, sizeof(double) * n2);
+  std::memcpy(moens_out, oe.MOens, sizeof(double) * nroao);
+  out_e[0] = grab(text, "HF-Results", "TOTAL E:");
+  delete[] oe.Hmat;  // allocate_onemats hands out one block starting at Hmat
+}
+
+}  // extern "C"

@@ -1,0 +1,141 @@
+"""ORACLE -- test infrastructure, not product code.
+
+ctypes front end of ``oracle/_ref/libcorr_ref.so``: the reference's own
+src/POSTHF, src/SCF, src/MATH and src/IO sources compiled unmodified against the
+shim headers in ``oracle/ref_shim`` (see ``oracle/Makefile`` and
+``oracle/ref_harness.cc``).  It exists only where the reference checkout does;
+tests that need it skip elsewhere, and the golden fixtures in tests/golden/
+carry its outputs to machines without it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = os.environ.get("CORR_REFERENCE_DIR", "/root/reference")
+SO = os.path.join(HERE, "_ref", "libcorr_ref.so")
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_i64p = ctypes.POINTER(ctypes.c_longlong)
+_u16p = ctypes.POINTER(ctypes.c_ushort)
+_L = None
+
+
+def _p(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+def available():
+    return os.path.exists(SO) or os.path.isdir(os.path.join(REF, "src"))
+
+
+def build():
+    if os.path.isdir(os.path.join(REF, "src")):
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={REF}",
+                               f"PY={sys.executable}"])
+
+
+def lib():
+    global _L
+    if _L is None:
+        if not os.path.exists(SO):
+            build()
+        L = ctypes.CDLL(SO)
+        L.ref_pack_eri.restype = ctypes.c_longlong
+        L.ref_mo2int_bf.restype = ctypes.c_double
+        L.ref_last_output.restype = ctypes.c_char_p
+        _L = L
+    return _L
+
+
+def set_threads(n):
+    lib().ref_set_threads(int(n))
+
+
+def rimp2_energy(B, eps, nocc, nvir):
+    """src/POSTHF/can_mp2.cc:53 -> (E_SS, E_OS, E)."""
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    out = np.zeros(3)
+    lib().ref_rimp2_energy(nocc, nvir, B.shape[0], _p(B),
+                           _p(np.ascontiguousarray(eps, dtype=np.float64)), _p(out))
+    return tuple(out)
+
+
+def canonical_mp2(nroe, prec, fmo):
+    out = np.zeros(3)
+    lib().ref_canonical_mp2(nroe, fmo.shape[0], _p(np.ascontiguousarray(prec)),
+                            _p(np.ascontiguousarray(fmo)), _p(out))
+    return tuple(out)
+
+
+def build_fmo(mos, fmat):
+    N = mos.shape[0]
+    out = np.zeros((N, N))
+    lib().ref_build_fmo(N, _p(np.ascontiguousarray(mos)), _p(np.ascontiguousarray(fmat)), _p(out))
+    return out
+
+
+def pack_eri(eri):
+    from oracle.oracle import Packed
+    eri = np.ascontiguousarray(eri, dtype=np.float64)
+    n = lib().ref_pack_eri(eri.shape[0], _p(eri))
+    val = np.zeros(n)
+    num = np.zeros(4 * n, dtype=np.uint16)
+    sc = np.zeros(4, dtype=np.int64)
+    lib().ref_packed_copy(_p(val), _p(num, _u16p), _p(sc, _i64p))
+    return Packed(val, num, sc)
+
+
+def motrans(nroe, mos, packed):
+    """src/POSTHF/motrans.cc:35.  One nroao per process (function statics)."""
+    N = mos.shape[0]
+    out = np.zeros((N, N, N, N))
+    lib().ref_motrans(nroe, N, _p(np.ascontiguousarray(mos)), ctypes.c_longlong(packed.nrofint),
+                      _p(packed.sortcount, _i64p), _p(packed.intval), _p(packed.intnums, _u16p),
+                      _p(out))
+    return out
+
+
+def mo2int_bf(i, j, k, l, mos, packed):
+    N = mos.shape[0]
+    return lib().ref_mo2int_bf(i, j, k, l, N, _p(np.ascontiguousarray(mos)),
+                               ctypes.c_longlong(packed.nrofint), _p(packed.sortcount, _i64p),
+                               _p(packed.intval), _p(packed.intnums, _u16p))
+
+
+def calculate_ri(J, P3):
+    """src/POSTHF/ri.cc:7 on tabulated (P|Q) and (P|mn) -> BPQ[P][mu][nu]."""
+    X, N, _ = P3.shape
+    out = np.zeros((X, N, N))
+    lib().ref_calculate_ri(X, N, _p(np.ascontiguousarray(J)), _p(np.ascontiguousarray(P3)),
+                           _p(out))
+    return out
+
+
+def transform_ri(nroe, mos, bpq):
+    X, N, _ = bpq.shape
+    o = nroe // 2
+    out = np.zeros((X, o, N - o))
+    lib().ref_transform_ri(nroe, N, X, _p(np.ascontiguousarray(mos)),
+                           _p(np.ascontiguousarray(bpq)), _p(out))
+    return out
+
+
+def rhf(nroe, ion_rep, S, T, V, packed):
+    """src/SCF: calc_S12, core guess, run_scf (100 iterations).
+    Returns (mos[p][mu], Fmat, MOens, E_HF)."""
+    N = S.shape[0]
+    mos = np.zeros((N, N))
+    f = np.zeros((N, N))
+    e = np.zeros(N)
+    eh = np.zeros(1)
+    lib().ref_rhf(nroe, N, ctypes.c_double(ion_rep), _p(np.ascontiguousarray(S)),
+                  _p(np.ascontiguousarray(T)), _p(np.ascontiguousarray(V)),
+                  ctypes.c_longlong(packed.nrofint), _p(packed.sortcount, _i64p),
+                  _p(packed.intval), _p(packed.intnums, _u16p), _p(mos), _p(f), _p(e), _p(eh))
+    return mos, f, e, float(eh[0])

@@ -1,0 +1,47 @@
+"""C-ABI checks that need no GPU: the library loads, exports every symbol the
+public header declares, and reports a missing device as an error status."""
+import ctypes
+
+import pytest
+
+from corr_gb300 import _lib
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return _lib.load()
+
+
+def test_header_symbols_exported(lib):
+    names = _lib.header_symbols()
+    assert "corr_rimp2_energy" in names
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_binding_covers_header():
+    assert set(_lib.header_symbols()) == set(_lib.SIGNATURES)
+
+
+def test_version(lib):
+    assert b"sm_103a" in lib.corr_version()
+
+
+def test_no_device_or_bad_args(lib):
+    h = ctypes.c_void_p()
+    st = lib.corr_create(ctypes.byref(h), 0, None)
+    try:
+        import torch
+
+        have_gpu = torch.cuda.is_available()
+    except Exception:
+        have_gpu = False
+    if not have_gpu:
+        assert st == 6  # CORR_ERR_NO_DEVICE
+        assert b"device" in lib.corr_last_error()
+    else:
+        assert st == 0
+        lib.corr_destroy(h)
+    assert lib.corr_create(None, 0, None) == 1  # CORR_ERR_BAD_ARG
+    out = _lib.MP2Energy()
+    assert lib.corr_rimp2_energy(None, 1, 1, 1, None, None, 0, ctypes.byref(out)) == 1

@@ -1,0 +1,83 @@
+"""RI-MP2 energy (src/POSTHF/can_mp2.cc:53) on the GPU against the oracle.
+
+FP64 form: |dE| <= 1e-10 Eh or 1e-12 relative (the synthetic configs have
+|E| up to ~6e4 Eh, where a different FP64 summation order alone moves the last
+~4 digits).  Split forms: relative error bounds written per test.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+FP64_ABS, FP64_REL = 1e-10, 1e-12
+
+SHAPES = [
+    (1, 1, 1, 11),      # smallest: E = -(ia|ia)^2/D
+    (3, 5, 7, 12),
+    (5, 19, 60, 13),     # config-1 orbital sizes
+    (2, 64, 17, 14),     # exactly one FP64 tile
+    (6, 129, 70, 15),    # crosses the 128 tcgen05 tile by one
+    (7, 33, 95, 16),     # naux not a multiple of the 32-wide K block
+    (4, 257, 40, 17),
+]
+
+
+def _close(e, ref, abs_tol, rel_tol):
+    return abs(e - ref) <= max(abs_tol, rel_tol * abs(ref))
+
+
+@pytest.mark.parametrize("o,v,X,seed", SHAPES)
+def test_fp64_matches_oracle(ctx, o, v, X, seed):
+    B, eps = O.synth_rimp2(o, v, X, seed)
+    ref = O.rimp2_energy(B, eps, o, v)
+    got = ctx.rimp2_energy(B, eps, o, v, X, "fp64")
+    for g, r in zip(got.as_tuple(), ref):
+        assert _close(g, r, FP64_ABS, FP64_REL), (got, ref)
+    assert abs(got.e_scs - (ref[0] / 3 + ref[1] * 6 / 5)) <= 1e-10 + 1e-12 * abs(ref[2])
+
+
+@pytest.mark.parametrize("o,v,X,seed", SHAPES)
+@pytest.mark.parametrize("prec,rel", [("split_fp16", 2e-7), ("split_bf16", 2e-5)])
+def test_split_matches_oracle(ctx, o, v, X, seed, prec, rel):
+    B, eps = O.synth_rimp2(o, v, X, seed)
+    ref = O.rimp2_energy(B, eps, o, v)
+    got = ctx.rimp2_energy(B, eps, o, v, X, prec)
+    assert abs(got.e_total - ref[2]) <= rel * abs(ref[2]), (prec, got, ref)
+    assert abs(got.e_os - ref[1]) <= rel * abs(ref[1]), (prec, got, ref)
+    # E_SS is a difference; bound it relative to the total
+    assert abs(got.e_ss - ref[0]) <= rel * abs(ref[2]), (prec, got, ref)
+
+
+def test_config2_full_size(ctx):
+    """nocc=40, nvir=360, naux=1200 (decaying aux spectrum)."""
+    o, v, X = 40, 360, 1200
+    B, eps = O.synth_rimp2(o, v, X, 2024)
+    ref = O.rimp2_energy(B, eps, o, v)
+    f64 = ctx.rimp2_energy(B, eps, o, v, X, "fp64")
+    assert _close(f64.e_total, ref[2], FP64_ABS, FP64_REL), (f64, ref)
+    assert _close(f64.e_ss, ref[0], FP64_ABS, FP64_REL), (f64, ref)
+    h16 = ctx.rimp2_energy(B, eps, o, v, X, "split_fp16")
+    assert abs(h16.e_total - ref[2]) <= 2e-7 * abs(ref[2]), (h16, ref)
+
+
+def test_device_resident_inputs(ctx):
+    import torch
+
+    o, v, X = 5, 40, 50
+    B, eps = O.synth_rimp2(o, v, X, 99)
+    ref = ctx.rimp2_energy(B, eps, o, v, X, "fp64")
+    Bd = torch.from_numpy(B).cuda()
+    ed = torch.from_numpy(eps).cuda()
+    got = ctx.rimp2_energy(Bd, ed, o, v, X, "fp64")
+    assert got.as_tuple() == ref.as_tuple()
+
+
+def test_repeat_is_deterministic(ctx):
+    o, v, X = 6, 150, 90
+    B, eps = O.synth_rimp2(o, v, X, 5)
+    for prec in ("fp64", "split_fp16"):
+        a = ctx.rimp2_energy(B, eps, o, v, X, prec)
+        b = ctx.rimp2_energy(B, eps, o, v, X, prec)
+        assert a.as_tuple() == b.as_tuple()
