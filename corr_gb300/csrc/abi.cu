@@ -240,30 +240,31 @@ int rimp2_energy_device(corr_context* c, int nocc, int nvir, int naux, const dou
   int grid = precision == CORR_PREC_FP64 ? c->sms * 2 : c->sms;
   if ((long long)grid > sh.nunits) grid = (int)sh.nunits;
 
-  // size the workspace
+  const long long R = (long long)nocc * nvir;
+  const bool tc = precision != CORR_PREC_FP64;
+  // size the workspace (same carving order twice: size pass, then real pass)
+  auto carve = [&](Carver& w, void** b_slot, void** e_slot, SliceWork* sw, double** partials) {
+    *b_slot = b_dev ? nullptr : w.take(nb * 8);
+    *e_slot = e_dev ? nullptr : w.take(ne * 8);
+    if (tc) {
+      sw->S = static_cast<uint16_t*>(w.take((size_t)3 * R * Qp * 2));
+      sw->erow = static_cast<int*>(w.take((size_t)R * 4));
+      sw->diag = static_cast<double*>(w.take((size_t)R * 8));
+      sw->sc = static_cast<float*>(w.take((size_t)R * 4));
+      sw->dg = static_cast<float*>(w.take((size_t)R * 4));
+      sw->eref = static_cast<int*>(w.take(16));
+      sw->scale = static_cast<double*>(w.take(16));
+    }
+    *partials = static_cast<double*>(w.take((size_t)grid * 16));
+  };
+  void *b_slot, *e_slot;
+  SliceWork sw{};
+  double* partials;
   Carver cv{nullptr, 0};
-  if (!b_dev) cv.take(nb * 8);
-  if (!e_dev) cv.take(ne * 8);
-  if (precision != CORR_PREC_FP64) {
-    cv.take((size_t)nocc * nvir * Qp * 2);
-    cv.take((size_t)nocc * nvir * Qp * 2);
-  }
-  cv.take((size_t)grid * 16);
-  cv.take(64);
+  carve(cv, &b_slot, &e_slot, &sw, &partials);
   CORR_TRY(c->ws.reserve(cv.used));
   Carver w{c->ws.ptr, 0};
-  void* b_slot = b_dev ? nullptr : w.take(nb * 8);
-  void* e_slot = e_dev ? nullptr : w.take(ne * 8);
-  void* hi = nullptr;
-  void* lo = nullptr;
-  if (precision != CORR_PREC_FP64) {
-    hi = w.take((size_t)nocc * nvir * Qp * 2);
-    lo = w.take((size_t)nocc * nvir * Qp * 2);
-  }
-  double* partials = static_cast<double*>(w.take((size_t)grid * 16));
-  char* misc = static_cast<char*>(w.take(64));
-  unsigned long long* dmax = reinterpret_cast<unsigned long long*>(misc);
-  double* scale = reinterpret_cast<double*>(misc + 8);
+  carve(w, &b_slot, &e_slot, &sw, &partials);
 
   const double* d_b = static_cast<const double*>(stage_in(c, bia, nb * 8, b_slot));
   const double* d_e = static_cast<const double*>(stage_in(c, eps, ne * 8, e_slot));
@@ -273,27 +274,24 @@ int rimp2_energy_device(corr_context* c, int nocc, int nvir, int naux, const dou
   }
   CORR_CUDA(cudaMemsetAsync(c->dres, 0, sizeof(ResultBlock), c->stream));
 
-  if (precision == CORR_PREC_FP64) {
+  if (!tc) {
     CORR_CUDA(launch_energy_fp64(d_b, d_e, sh, partials, grid, c->stream));
     CORR_CUDA(launch_energy_reduce(partials, grid, nullptr, c->dres->e, c->stream));
     return CORR_OK;
   }
   const int fmt = precision == CORR_PREC_SPLIT_FP16 ? 0 : 1;
-  CORR_CUDA(cudaMemsetAsync(dmax, 0, 8, c->stream));
-  CORR_CUDA(launch_maxabs(d_b, (long long)nb, dmax, c->sms, c->stream));
-  CORR_CUDA(launch_split(d_b, naux, (long long)nocc * nvir, Qp, fmt, dmax, hi, lo, scale,
-                         c->stream));
-  CUtensorMap mh, ml;
-  const uint64_t dims[3] = {(uint64_t)Qp, (uint64_t)nvir, (uint64_t)nocc};
+  const int p = slice_bits_for(Qp);
+  CORR_CUDA(launch_slices(d_b, naux, R, Qp, fmt, p, sw, c->stream));
+  CUtensorMap tm;
+  const uint64_t dims[3] = {(uint64_t)Qp, (uint64_t)nvir, (uint64_t)3 * nocc};
   const uint64_t strides[2] = {(uint64_t)Qp * 2, (uint64_t)nvir * Qp * 2};
   const uint32_t box[3] = {32, (uint32_t)kTcTile, 1};
   const CUtensorMapDataType dt =
       fmt == 0 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
-  CORR_TRY(encode_tmap(&mh, dt, 3, hi, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_64B));
-  CORR_TRY(encode_tmap(&ml, dt, 3, lo, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_64B));
-  CORR_CUDA(launch_energy_tc(mh, ml, d_e, sh, Qp, fmt, partials, grid, &c->dres->status,
-                             c->stream));
-  CORR_CUDA(launch_energy_reduce(partials, grid, scale, c->dres->e, c->stream));
+  CORR_TRY(encode_tmap(&tm, dt, 3, sw.S, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_64B));
+  CORR_CUDA(launch_energy_tc(tm, d_e, sw.sc, sw.dg, sh, Qp, fmt, p, partials, grid,
+                             &c->dres->status, c->stream));
+  CORR_CUDA(launch_energy_reduce(partials, grid, sw.scale, c->dres->e, c->stream));
   return CORR_OK;
 }
 

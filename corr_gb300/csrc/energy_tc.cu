@@ -1,20 +1,27 @@
-// Split-precision fused RI-MP2 energy on the 5th-generation tensor cores.
+// Precision-form fused RI-MP2 energy on the 5th-generation tensor cores.
 //
-// Input: the pre-pass output hi/lo[i][a][Qp] (16-bit, K-major, see split.cu).
+// Input: the three integer slices of B (split.cu), as one 16-bit array
+// S[l][i][a][Qp] read through a 3-D TMA map over [3*nocc][nvir][Qp].
 // Work unit = (occupied pair i<=j, virtual tile pair A<=B), tiles of 128.
-// Per unit two 128x128 FP32 accumulators live in TMEM:
-//   D1 = hi_iA.hi_jB^T + hi_iA.lo_jB^T + lo_iA.hi_jB^T  ~ g^2 (ia|jb)
-//   D2 = hi_jA.hi_iB^T + hi_jA.lo_iB^T + lo_jA.hi_iB^T  ~ g^2 (ib|ja)
-// and the epilogue folds them into E_OS/E_SS exactly as the FP64 kernel does
-// (energy_fp64.cu has the derivation), so no (ia|jb) value reaches HBM.
+//
+// Phase 1 forms D1[a][b] = (ia|jb) for a in A, b in B; phase 2 forms
+// D2[a][b] = (ib|ja).  Each phase accumulates three levels in TMEM,
+//   acc_m = sum_{k+l=m} s_k(row) . s_l(col)^T    (m = 0, 1, 2; six MMAs per K=16),
+// whose partial sums are exact integers (split.cu), then the epilogue forms
+//   d = sc_row sc_col (acc_0 + acc_1/L + acc_2/L^2)   (FP32, round-to-nearest).
+// D1 is parked in TMEM columns 384-511 while D2 accumulates in 0-383.  For
+// i == j, D2 == D1 and phase 2 is skipped.  On the (i==j, A==B) diagonal the
+// element (ia|ia) is replaced by its FP64 value.  The energy epilogue is the
+// one of energy_fp64.cu:
+//   E_OS -= f w (D1^2 + D2^2)/D,  E_SS -= f w (D1 - D2)^2/D,
+// with 1/D as an IEEE-rounded FP32 reciprocal and FP64 sums per unit.
 //
 // CTA = 6 warps, persistent, one CTA per SM:
-//   warp 0     TMA producer (one thread): 8 tiles of 128x32 per stage, 3 stages
+//   warp 0     TMA producer (one thread), 6 tiles of 128x32 per stage, 4 stages
 //   warp 1     TMEM owner + MMA issuer (one thread), tcgen05.mma kind::f16
-//   warps 2-5  epilogue: tcgen05.ld of their 32-lane quarter, FP32 per-element
-//              math (IEEE reciprocal of the denominator), FP64 per-unit sums
-// TMEM holds two accumulator pairs (2 x 256 columns) so the epilogue of one
-// unit overlaps the MMAs of the next.
+//   warps 2-5  epilogue, one TMEM lane quarter each
+// Every wait is bounded (common.cuh); on a timeout the CTA winds down and the
+// host sees CORR_ERR_DEVICE_TIMEOUT.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -24,23 +31,25 @@ namespace {
 
 constexpr int TILE = kTcTile;                 // 128
 constexpr int KB = 32;                        // 16-bit Q elements per stage row (64 B)
-constexpr int STAGES = 3;
-constexpr int NTILES = 8;                     // tiles per stage
+constexpr int STAGES = 4;
+constexpr int NTILES = 6;                     // 3 slices x (row operand, col operand)
 constexpr int TILE_BYTES = TILE * KB * 2;     // 8 KB
 constexpr int STAGE_BYTES = NTILES * TILE_BYTES;
 constexpr int NTHREADS = 192;
 constexpr uint32_t TMEM_COLS = 512;
+constexpr uint32_t COL_STASH = 384;           // parked D1
 constexpr uint32_t SW64 = 4;                  // descriptor layout type: 64B swizzle
 
 struct Ctl {
   uint64_t full[STAGES];
   uint64_t empty[STAGES];
-  uint64_t tfull[2];
-  uint64_t tempty[2];
+  uint64_t afull;
+  uint64_t aempty;
   uint64_t fin;
   uint32_t tmem;
   int abort;
-  float db[2][TILE];
+  float db[TILE];
+  float scb[TILE];
   double red[2][4];
 };
 
@@ -53,10 +62,49 @@ __device__ __forceinline__ void unit_decode(long long u, const EnergyShape& sh, 
   tpair_decode(tp, sh.ntiles, A, B);
 }
 
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const float* v) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+      "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+      "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+      "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+      "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
+      "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+      "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
+      "r"(__float_as_uint(v[15])), "r"(__float_as_uint(v[16])), "r"(__float_as_uint(v[17])),
+      "r"(__float_as_uint(v[18])), "r"(__float_as_uint(v[19])), "r"(__float_as_uint(v[20])),
+      "r"(__float_as_uint(v[21])), "r"(__float_as_uint(v[22])), "r"(__float_as_uint(v[23])),
+      "r"(__float_as_uint(v[24])), "r"(__float_as_uint(v[25])), "r"(__float_as_uint(v[26])),
+      "r"(__float_as_uint(v[27])), "r"(__float_as_uint(v[28])), "r"(__float_as_uint(v[29])),
+      "r"(__float_as_uint(v[30])), "r"(__float_as_uint(v[31]))
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_wait_st() {
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
+// 32 columns [c, c+32) of one phase's result in scaled FP32 units.
+__device__ __forceinline__ void load_level_sum(uint32_t tb, int c, float inv_l, float inv_l2,
+                                               float sca, const float* scb, float* d) {
+  float a0[32], a1[32], a2[32];
+  tmem_ld32(tb + 0u + (uint32_t)c, a0);
+  tmem_ld32(tb + 128u + (uint32_t)c, a1);
+  tmem_ld32(tb + 256u + (uint32_t)c, a2);
+  tc_wait_ld();
+#pragma unroll
+  for (int k = 0; k < 32; ++k) {
+    // acc_0 is an exact integer; the sum is rounded once to nearest
+    const float t = fmaf(a2[k], inv_l2, fmaf(a1[k], inv_l, a0[k]));
+    d[k] = t * (sca * scb[c + k]);
+  }
+}
+
 __global__ void __launch_bounds__(NTHREADS, 1)
-    energy_tc_kernel(const __grid_constant__ CUtensorMap tm_hi,
-                     const __grid_constant__ CUtensorMap tm_lo, const double* __restrict__ eps,
-                     EnergyShape sh, int nkb, uint32_t idesc, double* __restrict__ partials,
+    energy_tc_kernel(const __grid_constant__ CUtensorMap tm, const double* __restrict__ eps,
+                     const float* __restrict__ sc, const float* __restrict__ dg, EnergyShape sh,
+                     int nkb, uint32_t idesc, float inv_l, double* __restrict__ partials,
                      int* status) {
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
@@ -70,10 +118,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       mbar_init(&ctl->full[s], 1);
       mbar_init(&ctl->empty[s], 1);
     }
-    for (int s = 0; s < 2; ++s) {
-      mbar_init(&ctl->tfull[s], 1);
-      mbar_init(&ctl->tempty[s], 4);
-    }
+    mbar_init(&ctl->afull, 1);
+    mbar_init(&ctl->aempty, 4);
     mbar_init(&ctl->fin, 1);
     ctl->abort = 0;
     fence_mbar_init();
@@ -88,8 +134,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == 0) {
     // ------------------------------------------------------------ producer
     if (lane == 0) {
-      prefetch_tmap(&tm_hi);
-      prefetch_tmap(&tm_lo);
+      prefetch_tmap(&tm);
       int st = 0;
       uint32_t ph = 0;
       uint32_t last_ph[STAGES];
@@ -100,28 +145,30 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         int i, j, A, B;
         unit_decode(u, sh, &i, &j, &A, &B);
         const int A0 = A * TILE, B0 = B * TILE;
-        for (int kb = 0; kb < nkb; ++kb) {
-          if (!mbar_wait(&ctl->empty[st], ph ^ 1, abort, status)) {
-            ok = false;
-            break;
-          }
-          uint64_t* bar = &ctl->full[st];
-          mbar_expect_tx(bar, STAGE_BYTES);
-          uint8_t* sb = tiles + (size_t)st * STAGE_BYTES;
-          const int k0 = kb * KB;
-          tma_load_3d(sb + 0 * TILE_BYTES, &tm_hi, bar, k0, A0, i);
-          tma_load_3d(sb + 1 * TILE_BYTES, &tm_hi, bar, k0, B0, j);
-          tma_load_3d(sb + 2 * TILE_BYTES, &tm_hi, bar, k0, A0, j);
-          tma_load_3d(sb + 3 * TILE_BYTES, &tm_hi, bar, k0, B0, i);
-          tma_load_3d(sb + 4 * TILE_BYTES, &tm_lo, bar, k0, A0, i);
-          tma_load_3d(sb + 5 * TILE_BYTES, &tm_lo, bar, k0, B0, j);
-          tma_load_3d(sb + 6 * TILE_BYTES, &tm_lo, bar, k0, A0, j);
-          tma_load_3d(sb + 7 * TILE_BYTES, &tm_lo, bar, k0, B0, i);
-          has[st] = true;
-          last_ph[st] = ph;
-          if (++st == STAGES) {
-            st = 0;
-            ph ^= 1;
+        const int nph = (i == j) ? 1 : 2;
+        for (int phs = 0; phs < nph && ok; ++phs) {
+          const int x = phs == 0 ? i : j;  // row operand slab
+          const int y = phs == 0 ? j : i;  // column operand slab
+          for (int kb = 0; kb < nkb; ++kb) {
+            if (!mbar_wait(&ctl->empty[st], ph ^ 1, abort, status)) {
+              ok = false;
+              break;
+            }
+            uint64_t* bar = &ctl->full[st];
+            mbar_expect_tx(bar, STAGE_BYTES);
+            uint8_t* sb = tiles + (size_t)st * STAGE_BYTES;
+            const int k0 = kb * KB;
+#pragma unroll
+            for (int l = 0; l < 3; ++l) {
+              tma_load_3d(sb + (2 * l) * TILE_BYTES, &tm, bar, k0, A0, l * o + x);
+              tma_load_3d(sb + (2 * l + 1) * TILE_BYTES, &tm, bar, k0, B0, l * o + y);
+            }
+            has[st] = true;
+            last_ph[st] = ph;
+            if (++st == STAGES) {
+              st = 0;
+              ph ^= 1;
+            }
           }
         }
       }
@@ -135,90 +182,143 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     if (lane == 0) {
       int st = 0;
       uint32_t ph = 0;
-      long long t = 0;
+      uint32_t nuse = 0;
       bool ok = true;
-      for (long long u = blockIdx.x; u < sh.nunits && ok; u += gridDim.x, ++t) {
-        const int s = (int)(t & 1);
-        const uint32_t use = (uint32_t)(t >> 1);
-        if (!mbar_wait(&ctl->tempty[s], (use & 1) ^ 1, abort, status)) break;
-        tc_fence_after();
-        const uint32_t d1 = tmem + (uint32_t)s * 256u, d2 = d1 + 128u;
-        for (int kb = 0; kb < nkb; ++kb) {
-          if (!mbar_wait(&ctl->full[st], ph, abort, status)) {
+      for (long long u = blockIdx.x; u < sh.nunits && ok; u += gridDim.x) {
+        int i, j, A, B;
+        unit_decode(u, sh, &i, &j, &A, &B);
+        const int nph = (i == j) ? 1 : 2;
+        for (int phs = 0; phs < nph && ok; ++phs) {
+          if (!mbar_wait(&ctl->aempty, (nuse & 1) ^ 1, abort, status)) {
             ok = false;
             break;
           }
           tc_fence_after();
-          const uint32_t sb = smem_u32(tiles + (size_t)st * STAGE_BYTES);
+          const uint32_t c0 = tmem, c1 = tmem + 128u, c2 = tmem + 256u;
+          for (int kb = 0; kb < nkb; ++kb) {
+            if (!mbar_wait(&ctl->full[st], ph, abort, status)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t sb = smem_u32(tiles + (size_t)st * STAGE_BYTES);
 #pragma unroll
-          for (int kk = 0; kk < KB / 16; ++kk) {
-            const uint32_t off = (uint32_t)kk * 32u;  // 16 elements x 2 B
-            uint64_t dsc[NTILES];
+            for (int kk = 0; kk < KB / 16; ++kk) {
+              const uint32_t off = (uint32_t)kk * 32u;  // 16 elements x 2 B
+              uint64_t r[3], q[3];
 #pragma unroll
-            for (int n = 0; n < NTILES; ++n)
-              dsc[n] = smem_desc(sb + (uint32_t)n * TILE_BYTES + off, 16, 512, SW64);
-            const uint32_t acc = (kb | kk) ? 1u : 0u;
-            tc_mma_f16(d1, dsc[0], dsc[1], idesc, acc);
-            tc_mma_f16(d1, dsc[0], dsc[5], idesc, 1u);
-            tc_mma_f16(d1, dsc[4], dsc[1], idesc, 1u);
-            tc_mma_f16(d2, dsc[2], dsc[3], idesc, acc);
-            tc_mma_f16(d2, dsc[2], dsc[7], idesc, 1u);
-            tc_mma_f16(d2, dsc[6], dsc[3], idesc, 1u);
+              for (int l = 0; l < 3; ++l) {
+                r[l] = smem_desc(sb + (uint32_t)(2 * l) * TILE_BYTES + off, 16, 512, SW64);
+                q[l] = smem_desc(sb + (uint32_t)(2 * l + 1) * TILE_BYTES + off, 16, 512, SW64);
+              }
+              const uint32_t acc = (kb | kk) ? 1u : 0u;
+              tc_mma_f16(c0, r[0], q[0], idesc, acc);
+              tc_mma_f16(c1, r[0], q[1], idesc, acc);
+              tc_mma_f16(c1, r[1], q[0], idesc, 1u);
+              tc_mma_f16(c2, r[0], q[2], idesc, acc);
+              tc_mma_f16(c2, r[1], q[1], idesc, 1u);
+              tc_mma_f16(c2, r[2], q[0], idesc, 1u);
+            }
+            tc_commit(&ctl->empty[st]);  // stage reusable once these MMAs finish
+            if (++st == STAGES) {
+              st = 0;
+              ph ^= 1;
+            }
           }
-          tc_commit(&ctl->empty[st]);  // stage reusable once these MMAs finish
-          if (++st == STAGES) {
-            st = 0;
-            ph ^= 1;
-          }
+          if (ok) tc_commit(&ctl->afull);
+          ++nuse;
         }
-        if (ok) tc_commit(&ctl->tfull[s]);
       }
-      // wait until every MMA this thread issued has retired
-      tc_commit(&ctl->fin);
+      tc_commit(&ctl->fin);  // wait until every MMA this thread issued has retired
       int never = 0;
       mbar_wait(&ctl->fin, 0, &never, status);
     }
   } else {
     // ------------------------------------------------------------ epilogue
-    const int q = warp & 3;               // TMEM lane quarter of this warp
-    const int et = threadIdx.x - 64;      // 0..127
-    const int arow = 32 * q + lane;       // accumulator row = TMEM lane
+    const int q = warp & 3;           // TMEM lane quarter of this warp
+    const int et = threadIdx.x - 64;  // 0..127
+    const int arow = 32 * q + lane;   // accumulator row = TMEM lane
+    const uint32_t tq = tmem + ((uint32_t)(32 * q) << 16);
+    const float inv_l2 = inv_l * inv_l;
     double tot_os = 0.0, tot_ss = 0.0;
     bool dead = false;
-    long long t = 0;
-    for (long long u = blockIdx.x; u < sh.nunits; u += gridDim.x, ++t) {
-      const int s = (int)(t & 1);
-      const uint32_t use = (uint32_t)(t >> 1);
+    uint32_t nuse = 0;
+    for (long long u = blockIdx.x; u < sh.nunits; u += gridDim.x) {
       int i, j, A, B;
       unit_decode(u, sh, &i, &j, &A, &B);
       const int A0 = A * TILE, B0 = B * TILE;
+      const bool same = (i == j);
       {
+        // phase 1: rows from slab i, columns from slab j
         const int b = B0 + et;
-        ctl->db[s][et] = b < v ? (float)(eps[o + b] - eps[j]) : __int_as_float(0x7f800000);
+        ctl->db[et] = b < v ? (float)(eps[o + b] - eps[j]) : __int_as_float(0x7f800000);
+        ctl->scb[et] = b < v ? sc[(size_t)j * v + b] : 0.0f;
       }
       named_bar(1, 128);
+      const int a = A0 + arow;
+      const float da = a < v ? (float)(eps[o + a] - eps[i]) : __int_as_float(0x7f800000);
+      const float sca1 = a < v ? sc[(size_t)i * v + a] : 0.0f;
+      const float sca2 = a < v ? sc[(size_t)j * v + a] : 0.0f;
+      const bool diag_tile = same && (A == B);
+      const float dga = (diag_tile && a < v) ? dg[(size_t)i * v + a] : 0.0f;
+      double uos = 0.0, uss = 0.0;
+
+      // ---- phase 1: D1
+      bool got = !dead && __all_sync(0xffffffffu,
+                                     mbar_wait(&ctl->afull, nuse & 1, abort, status));
+      if (!got) dead = true;
       if (!dead) {
-        const int a = A0 + arow;
-        const float da = a < v ? (float)(eps[o + a] - eps[i]) : __int_as_float(0x7f800000);
-        // warp-uniform outcome: tcgen05.ld below is .sync.aligned
-        const bool got = __all_sync(0xffffffffu, mbar_wait(&ctl->tfull[s], use & 1, abort, status));
-        if (!got) {
-          dead = true;
-        } else {
-          tc_fence_after();
-          const uint32_t tb = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)s * 256u;
-          double uos = 0.0, uss = 0.0;
+        tc_fence_after();
+        if (same) {
+          // D2 == D1: fold straight into the energy
 #pragma unroll 1
           for (int c = 0; c < TILE; c += 32) {
-            float m1[32], m2[32];
-            tmem_ld32(tb + (uint32_t)c, m1);
-            tmem_ld32(tb + 128u + (uint32_t)c, m2);
+            float d1[32];
+            load_level_sum(tq, c, inv_l, inv_l2, sca1, ctl->scb, d1);
+            float fos = 0.f;
+#pragma unroll
+            for (int k = 0; k < 32; ++k) {
+              const float x = (diag_tile && c + k == arow) ? dga : d1[k];
+              const float r = __frcp_rn(da + ctl->db[c + k]);
+              fos = fmaf(2.0f * x * x, r, fos);
+            }
+            uos += (double)fos;
+          }
+        } else {
+#pragma unroll 1
+          for (int c = 0; c < TILE; c += 32) {
+            float d1[32];
+            load_level_sum(tq, c, inv_l, inv_l2, sca1, ctl->scb, d1);
+            tmem_st32(tq + COL_STASH + (uint32_t)c, d1);
+          }
+          tc_wait_st();
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&ctl->aempty);
+      }
+      ++nuse;
+
+      // ---- phase 2: D2 (i != j): rows from slab j, columns from slab i
+      if (!same) {
+        named_bar(1, 128);  // everyone is done with the phase-1 column scales
+        if (B0 + et < v) ctl->scb[et] = sc[(size_t)i * v + B0 + et];
+        named_bar(1, 128);
+        got = !dead && __all_sync(0xffffffffu, mbar_wait(&ctl->afull, nuse & 1, abort, status));
+        if (!got) dead = true;
+        if (!dead) {
+          tc_fence_after();
+#pragma unroll 1
+          for (int c = 0; c < TILE; c += 32) {
+            float d2[32], d1[32];
+            load_level_sum(tq, c, inv_l, inv_l2, sca2, ctl->scb, d2);
+            tmem_ld32(tq + COL_STASH + (uint32_t)c, d1);
             tc_wait_ld();
             float fos = 0.f, fss = 0.f;
 #pragma unroll
             for (int k = 0; k < 32; ++k) {
-              const float r = __frcp_rn(da + ctl->db[s][c + k]);
-              const float x = m1[k], y = m2[k];
+              const float r = __frcp_rn(da + ctl->db[c + k]);
+              const float x = d1[k], y = d2[k];
               fos = fmaf(fmaf(x, x, y * y), r, fos);
               const float df = x - y;
               fss = fmaf(df * df, r, fss);
@@ -228,12 +328,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           }
           tc_fence_before();
           __syncwarp();
-          if (lane == 0) mbar_arrive(&ctl->tempty[s]);
-          const double fw = (A < B ? 2.0 : 1.0) * (i < j ? 1.0 : 0.5);
-          tot_os -= fw * uos;
-          tot_ss -= fw * uss;
+          if (lane == 0) mbar_arrive(&ctl->aempty);
         }
+        ++nuse;
       }
+      const double fw = (A < B ? 2.0 : 1.0) * (same ? 0.5 : 1.0);
+      tot_os -= fw * uos;
+      tot_ss -= fw * uss;
+      named_bar(1, 128);  // smem db/scb are rewritten by the next unit
     }
     tot_os = warp_sum(tot_os);
     tot_ss = warp_sum(tot_ss);
@@ -243,7 +345,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
     named_bar(1, 128);
     if (et == 0) {
-      partials[2 * blockIdx.x] = (ctl->red[0][0] + ctl->red[0][1]) + (ctl->red[0][2] + ctl->red[0][3]);
+      partials[2 * blockIdx.x] =
+          (ctl->red[0][0] + ctl->red[0][1]) + (ctl->red[0][2] + ctl->red[0][3]);
       partials[2 * blockIdx.x + 1] =
           (ctl->red[1][0] + ctl->red[1][1]) + (ctl->red[1][2] + ctl->red[1][3]);
     }
@@ -258,16 +361,17 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
 }  // namespace
 
-cudaError_t launch_energy_tc(const CUtensorMap& tmap_hi, const CUtensorMap& tmap_lo,
-                             const double* eps, const EnergyShape& sh, int Qp, int fmt,
+cudaError_t launch_energy_tc(const CUtensorMap& tmap, const double* eps, const float* sc,
+                             const float* dg, const EnergyShape& sh, int Qp, int fmt, int p,
                              double* partials, int grid, int* status, cudaStream_t s) {
   cudaError_t e = cudaFuncSetAttribute(energy_tc_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)kSmemBytes);
   if (e != cudaSuccess) return e;
   const uint32_t idesc = idesc_f16((uint32_t)fmt, TILE, TILE);
-  energy_tc_kernel<<<grid, NTHREADS, kSmemBytes, s>>>(tmap_hi, tmap_lo, eps, sh, Qp / KB, idesc,
-                                                      partials, status);
+  const float inv_l = ldexpf(1.0f, -(p + 1));
+  energy_tc_kernel<<<grid, NTHREADS, kSmemBytes, s>>>(tmap, eps, sc, dg, sh, Qp / KB, idesc,
+                                                      inv_l, partials, status);
   return cudaGetLastError();
 }
 

@@ -20,25 +20,30 @@ struct EnergyShape {
 
 EnergyShape make_energy_shape(int nocc, int nvir, int naux, int tile);
 
-// ---- split pre-pass (split.cu) ---------------------------------------------
-// maxabs of n doubles -> *dmax (as ordered uint64 bits; *dmax must start at 0).
-cudaError_t launch_maxabs(const double* x, long long n, unsigned long long* dmax, int sms,
-                          cudaStream_t s);
-// B[Q][r] (r = i*nvir + a, R = nocc*nvir) -> hi/lo[r][Qp] (16-bit), scaled by the
-// power of two derived from *dmax; Q >= naux is zero padding.  fmt 0 fp16, 1 bf16.
-cudaError_t launch_split(const double* b, int naux, long long R, int Qp, int fmt,
-                         const unsigned long long* dmax, void* hi, void* lo, double* scale_out,
-                         cudaStream_t s);
+// ---- slice pre-pass (split.cu) ---------------------------------------------
+// Device buffers of the precision form's pre-pass (R = nocc*nvir rows).
+struct SliceWork {
+  uint16_t* S;     // [3][R][Qp] integer slices (fp16 or bf16 encoding)
+  int* erow;       // [R] row exponents
+  double* diag;    // [R] FP64 sum_Q B^2
+  float* sc;       // [R] 2^(e_r - e_ref)
+  float* dg;       // [R] diag in scaled units
+  int* eref;       // [1]
+  double* scale;   // [1] global energy factor 2^(4 e_ref)
+};
+int slice_bits_for(int Qp);
+cudaError_t launch_slices(const double* b, int naux, long long R, int Qp, int fmt, int p,
+                          SliceWork w, cudaStream_t s);
 // Sum per-CTA partial pairs {os, ss} in fixed order, times `scale` (device),
 // into out[4] = {E_SS, E_OS, E, E_SCS}.
 cudaError_t launch_energy_reduce(const double* partials, int n, const double* scale, double* out,
                                  cudaStream_t s);
 
 // ---- fused energy kernels ---------------------------------------------------
-// tcgen05 split form (energy_tc.cu).  tmap_hi/tmap_lo: 3-D maps over
-// [nocc][nvir][Qp] 16-bit arrays, box {32, 128, 1}, 64B swizzle.
-cudaError_t launch_energy_tc(const CUtensorMap& tmap_hi, const CUtensorMap& tmap_lo,
-                             const double* eps, const EnergyShape& sh, int Qp, int fmt,
+// tcgen05 precision form (energy_tc.cu).  tmap: 3-D map over the slice
+// array viewed as [3*nocc][nvir][Qp] (16-bit), box {32, 128, 1}, 64B swizzle.
+cudaError_t launch_energy_tc(const CUtensorMap& tmap, const double* eps, const float* sc,
+                             const float* dg, const EnergyShape& sh, int Qp, int fmt, int p,
                              double* partials, int grid, int* status, cudaStream_t s);
 constexpr int kTcTile = 128;
 

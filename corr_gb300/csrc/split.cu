@@ -1,11 +1,22 @@
-// Split pre-pass of the RI-MP2 precision form and the final energy reduction.
+// Pre-pass of the RI-MP2 precision form and the final energy reduction.
 //
-// B^Q_ia (FP64, the reference's [Q][i][a] layout, ri.cc:147-172) is
-// transposed to the K-major [i][a][Qp] layout the tcgen05 kernel reads with
-// TMA and split into a 16-bit pair hi + lo, after a power-of-two pre-scale g
-// that puts max|B| g in [2^13, 2^14): hi = rn(g B), lo = rn(g B - hi).  Every
-// product hi*hi', hi*lo', lo*hi' is exact in FP32; the energy kernel undoes g
-// with one multiplication by g^-4 of the pair-energy sums (exact).
+// The tensor cores' FP32 accumulator truncates every partial sum toward zero,
+// which biases |(ia|jb)| low by ~1e-5 relative for naux ~ 1e3 when 16-bit
+// hi/lo products are simply accumulated.  The precision form therefore makes
+// every tensor-core partial sum an exact integer below 2^24:
+//
+//   B^Q_r = 2^(e_r) (s0 + s1/L + s2/L^2),   r = (i,a),  L = 2^(p+1),
+//   s_k = integers in [-2^p, 2^p] (exact in FP16 and BF16), p = 6 for naux <= 2048,
+//   e_r = ilogb(max_Q |B^Q_r|) - (p-1)  (one power-of-two scale per row).
+//
+// The energy kernel forms  acc_m = sum_{k+l=m} sum_Q s_k(ia) s_l(jb)  for
+// m = 0, 1, 2 in separate TMEM accumulators; acc_0 and acc_1 stay exact
+// (|acc| <= 2 K 2^(2p) <= 2^24), acc_2 enters at L^-2.  Representation error is
+// ~2^-21 of the row maximum, round-to-nearest and unbiased.
+//
+// The diagonal elements (ia|ia) = sum_Q (B^Q_ia)^2 are all-positive sums that
+// dominate the bias of any truncated scheme; they are formed here in FP64 and
+// substituted by the energy kernel.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -16,39 +27,46 @@ namespace corr {
 
 namespace {
 
-__global__ void maxabs_kernel(const double* __restrict__ x, long long n,
-                              unsigned long long* dmax) {
-  double m = 0.0;
-  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
-       k += (long long)gridDim.x * blockDim.x)
-    m = fmax(m, fabs(x[k]));
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  __shared__ double wm[32];
-  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) wm[w] = m;
+// Row statistics over Q for each r: e_r, the FP64 diagonal sum_Q B^2, and the
+// global maximum exponent (atomicMax).  Block = 32 rows x 8 Q-groups.
+__global__ void rowstat_kernel(const double* __restrict__ b, int naux, long long R, int p,
+                               int* __restrict__ erow, double* __restrict__ diag, int* eref) {
+  __shared__ double smax[8][32], ssum[8][32];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const long long r = (long long)blockIdx.x * 32 + tx;
+  double m = 0.0, s = 0.0;
+  if (r < R)
+    for (int q = ty; q < naux; q += 8) {
+      double x = b[(long long)q * R + r];
+      m = fmax(m, fabs(x));
+      s = fma(x, x, s);
+    }
+  smax[ty][tx] = m;
+  ssum[ty][tx] = s;
   __syncthreads();
-  if (w == 0) {
-    m = l < (int)(blockDim.x >> 5) ? wm[l] : 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    // non-negative doubles order like their bit patterns
-    if (l == 0) atomicMax(dmax, (unsigned long long)__double_as_longlong(m));
+  if (ty == 0 && r < R) {
+    for (int k = 1; k < 8; ++k) {
+      m = fmax(m, smax[k][tx]);
+      s += ssum[k][tx];
+    }
+    int e = (m > 0.0) ? ilogb(m) - (p - 1) : INT_MIN / 4;
+    erow[r] = e;
+    diag[r] = s;
+    if (m > 0.0) atomicMax(eref, e);
   }
 }
 
-__device__ __forceinline__ double prescale(const unsigned long long* dmax) {
-  double m = __longlong_as_double((long long)*dmax);
-  if (!(m > 0.0) || !isfinite(m)) return 1.0;
-  return ldexp(1.0, 13 - ilogb(m));
+template <int FMT>
+__device__ __forceinline__ uint16_t to16(double v) {
+  if (FMT == 0) return __half_as_ushort(__double2half(v));
+  return __bfloat16_as_ushort(__double2bfloat16(v));
 }
 
+// B[Q][r] -> slices S[l][r][Qp], l = 0..2, zero padded for Q >= naux.
 template <int FMT>
-__global__ void split_kernel(const double* __restrict__ b, int naux, long long R, int Qp,
-                             const unsigned long long* dmax, uint16_t* __restrict__ hi,
-                             uint16_t* __restrict__ lo, double* scale_out) {
+__global__ void slice_kernel(const double* __restrict__ b, int naux, long long R, int Qp, int p,
+                             const int* __restrict__ erow, uint16_t* __restrict__ S) {
   __shared__ double tile[32][33];
-  const double g = prescale(dmax);
   const int tx = threadIdx.x, ty = threadIdx.y;
   const long long r0 = (long long)blockIdx.x * 32;
   const int q0 = blockIdx.y * 32;
@@ -59,32 +77,43 @@ __global__ void split_kernel(const double* __restrict__ b, int naux, long long R
     tile[ty + 8 * k][tx] = (q < naux && r < R) ? b[(long long)q * R + r] : 0.0;
   }
   __syncthreads();
+  const double L = ldexp(1.0, p + 1);
+  const size_t plane = (size_t)R * Qp;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     long long r = r0 + ty + 8 * k;
     int q = q0 + tx;
     if (r < R) {
-      double v = tile[tx][ty + 8 * k] * g;
-      uint16_t h, l;
-      if (FMT == 0) {
-        __half hh = __double2half(v);
-        __half ll = __double2half(v - (double)__half2float(hh));
-        h = __half_as_ushort(hh);
-        l = __half_as_ushort(ll);
-      } else {
-        __nv_bfloat16 hh = __double2bfloat16(v);
-        __nv_bfloat16 ll = __double2bfloat16(v - (double)__bfloat162float(hh));
-        h = __bfloat16_as_ushort(hh);
-        l = __bfloat16_as_ushort(ll);
-      }
-      hi[r * Qp + q] = h;
-      lo[r * Qp + q] = l;
+      int e = erow[r];
+      double x = (e > INT_MIN / 8) ? ldexp(tile[tx][ty + 8 * k], -e) : 0.0;
+      double s0 = rint(x);
+      x = (x - s0) * L;
+      double s1 = rint(x);
+      x = (x - s1) * L;
+      double s2 = rint(x);
+      size_t at = (size_t)r * Qp + q;
+      S[at] = to16<FMT>(s0);
+      S[plane + at] = to16<FMT>(s1);
+      S[2 * plane + at] = to16<FMT>(s2);
     }
   }
-  if (blockIdx.x == 0 && blockIdx.y == 0 && tx == 0 && ty == 0) {
-    double ig = 1.0 / g;  // power of two: exact
-    scale_out[0] = ig * ig * ig * ig;
+}
+
+// Per-row FP32 factors for the energy kernel: sc_r = 2^(e_r - e_ref) and the
+// diagonal sum in the same units, dg_r = diag_r 2^(-2 e_ref).  Also writes
+// the global energy factor 2^(4 e_ref) into scale_out[0].
+__global__ void rowfactor_kernel(const int* __restrict__ erow, const double* __restrict__ diag,
+                                 long long R, const int* eref, float* __restrict__ sc,
+                                 float* __restrict__ dg, double* scale_out) {
+  int er = *eref;
+  if (er < -4000) er = 0;  // every row zero
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < R;
+       r += (long long)gridDim.x * blockDim.x) {
+    int e = erow[r];
+    sc[r] = (e > INT_MIN / 8) ? (float)ldexp(1.0, e - er) : 0.0f;
+    dg[r] = (float)ldexp(diag[r], -2 * er);
   }
+  if (blockIdx.x == 0 && threadIdx.x == 0) scale_out[0] = ldexp(1.0, 4 * er);
 }
 
 __global__ void energy_reduce_kernel(const double* __restrict__ part, int n,
@@ -123,25 +152,26 @@ __global__ void energy_reduce_kernel(const double* __restrict__ part, int n,
 
 }  // namespace
 
-cudaError_t launch_maxabs(const double* x, long long n, unsigned long long* dmax, int sms,
-                          cudaStream_t s) {
-  long long want = (n + 255) / 256;
-  int grid = (int)(want < (long long)sms * 8 ? (want > 0 ? want : 1) : (long long)sms * 8);
-  maxabs_kernel<<<grid, 256, 0, s>>>(x, n, dmax);
-  return cudaGetLastError();
+int slice_bits_for(int Qp) {
+  // largest p with 2 * Qp * 2^(2p) <= 2^24 (acc_0 and acc_1 exact), capped at 6
+  int p = 6;
+  while (p > 1 && (double)2 * Qp * (double)(1ll << (2 * p)) > 16777216.0) --p;
+  return p;
 }
 
-cudaError_t launch_split(const double* b, int naux, long long R, int Qp, int fmt,
-                         const unsigned long long* dmax, void* hi, void* lo, double* scale_out,
-                         cudaStream_t s) {
+cudaError_t launch_slices(const double* b, int naux, long long R, int Qp, int fmt, int p,
+                          SliceWork w, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(w.eref, 0x80, sizeof(int), s);  // very negative start
+  if (e != cudaSuccess) return e;
+  rowstat_kernel<<<(unsigned)((R + 31) / 32), dim3(32, 8), 0, s>>>(b, naux, R, p, w.erow, w.diag,
+                                                                   w.eref);
   dim3 grid((unsigned)((R + 31) / 32), (unsigned)(Qp / 32));
-  dim3 block(32, 8);
   if (fmt == 0)
-    split_kernel<0><<<grid, block, 0, s>>>(b, naux, R, Qp, dmax, (uint16_t*)hi, (uint16_t*)lo,
-                                           scale_out);
+    slice_kernel<0><<<grid, dim3(32, 8), 0, s>>>(b, naux, R, Qp, p, w.erow, w.S);
   else
-    split_kernel<1><<<grid, block, 0, s>>>(b, naux, R, Qp, dmax, (uint16_t*)hi, (uint16_t*)lo,
-                                           scale_out);
+    slice_kernel<1><<<grid, dim3(32, 8), 0, s>>>(b, naux, R, Qp, p, w.erow, w.S);
+  rowfactor_kernel<<<(unsigned)((R + 255) / 256 < 1024 ? (R + 255) / 256 : 1024), 256, 0, s>>>(
+      w.erow, w.diag, R, w.eref, w.sc, w.dg, w.scale);
   return cudaGetLastError();
 }
 

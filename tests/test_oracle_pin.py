@@ -1,0 +1,182 @@
+"""Pin the oracle (oracle/oracle.py + oracle/corr_oracle.c) to the reference.
+
+* against the committed golden fixtures (outputs of the reference's own
+  compiled code, tests/golden/make_golden.py) -- runs everywhere;
+* against the live reference build (oracle/_ref) on further seeded cases --
+  only where the reference checkout exists.
+"""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD_DIR = os.path.join(HERE, "golden")
+with open(os.path.join(GOLD_DIR, "golden.json")) as _f:
+    GOLD = json.load(_f)
+
+
+def _digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()[:16]
+
+
+def _checksum_ok(a, ref):
+    a = np.asarray(a, dtype=np.float64)
+    return np.allclose([a.sum(), (a * a).sum()], ref, rtol=1e-12, atol=1e-12)
+
+
+def _eps_for(N, nocc, seed):
+    r = O.rng(seed)
+    return np.concatenate([np.sort(r.uniform(-1.5, -0.3, nocc)),
+                           np.sort(r.uniform(0.05, 3.0, N - nocc))])
+
+
+@pytest.mark.parametrize("case", GOLD["rimp2"], ids=lambda c: f"o{c['nocc']}v{c['nvir']}x{c['naux']}")
+def test_rimp2_energy_vs_golden(case):
+    o, v, X = case["nocc"], case["nvir"], case["naux"]
+    B, eps = O.synth_rimp2(o, v, X, case["seed"])
+    assert _checksum_ok(B, case["B_checksum"]), "input generator drifted"
+    assert _checksum_ok(eps, case["eps_checksum"]), "input generator drifted"
+    got = O.rimp2_energy(B, eps, o, v)
+    for g, r in zip(got, case["energy"]):
+        assert abs(g - r) <= 1e-12 * max(1.0, abs(case["energy"][2])), (got, case["energy"])
+
+
+def test_tiny_closed_form():
+    """o=1, v=1: E = -(ia|ia)^2 / (2 e_a - 2 e_i), E_SS = 0."""
+    B = np.array([[[0.3]], [[-0.2]]])
+    eps = np.array([-0.5, 0.25])
+    iaia = 0.3 ** 2 + 0.2 ** 2
+    ess, eos, e = O.rimp2_energy(B, eps, 1, 1)
+    assert ess == 0.0
+    assert abs(eos - (-iaia ** 2 / 1.5)) < 1e-16
+
+
+@pytest.mark.parametrize("case", GOLD["motrans"], ids=lambda c: f"N{c['N']}")
+def test_packing_and_motrans_vs_golden(case):
+    N, nocc = case["N"], case["nocc"]
+    eri, _ = O.synth_eri(N, case["eri_seed"])
+    assert _checksum_ok(eri, case["eri_checksum"])
+    pk = O.pack_eri(eri)
+    # packing is integer/index work: bit-exact
+    assert pk.nrofint == case["nrofint"]
+    assert [int(x) for x in pk.sortcount] == case["sortcount"]
+    assert _digest(pk.intnums) == case["intnums_sha"]
+    assert _digest(pk.intval) == case["intval_sha"]
+    # dense unpack restores the full tensor
+    assert np.abs(O.unpack_eri(N, pk) - eri).max() < 1e-15
+    mos = O.synth_orbitals(N, case["mos_seed"])
+    prec = O.motrans(mos, pk)
+    ref = np.load(os.path.join(GOLD_DIR, f"motrans_n{N}.npz"))["prec"]
+    assert np.abs(prec - ref).max() <= 1e-13 * max(1.0, np.abs(ref).max())
+    eps = _eps_for(N, nocc, case["eri_seed"] + 1000)
+    e = O.canonical_mp2(2 * nocc, prec, np.diag(eps))
+    for g, r in zip(e, case["mp2"]):
+        assert abs(g - r) <= 1e-13
+    for (idx, r) in zip([(0, 1, 2, 3), (1, 1, 0, 0), (N - 1, 0, N - 2, 1)], case["mo2int_bf"]):
+        assert abs(O.mo2int_bf(*idx, mos, pk) - r) <= 1e-14
+        assert abs(prec[idx] - r) <= 1e-13
+
+
+@pytest.mark.parametrize("case", GOLD["ri"], ids=lambda c: f"X{c['naux']}N{c['N']}")
+def test_ri_build_transform_vs_golden(case):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("mg", os.path.join(GOLD_DIR, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    X, N, nocc, s = case["naux"], case["N"], case["nocc"], case["seed"]
+    J, P3 = mg.synth_metric(X, N, s)
+    assert _checksum_ok(J, case["J_checksum"]) and _checksum_ok(P3, case["P3_checksum"])
+    ref = np.load(os.path.join(GOLD_DIR, f"ri_x{X}_n{N}.npz"))
+    jm, ncut = O.ri_metric_inv_sqrt(J)
+    assert ncut == 0
+    bpq = O.ri_build_bpq(jm, P3)
+    assert np.abs(bpq - ref["bpq"]).max() <= 1e-12 * np.abs(ref["bpq"]).max()
+    mos = O.synth_orbitals(N, s + 7)
+    bia = O.transform_ri(2 * nocc, mos, ref["bpq"])
+    assert np.abs(bia - ref["bia"]).max() <= 1e-14
+    eps = _eps_for(N, nocc, s + 11)
+    e = O.rimp2_energy(bia, eps, nocc, N - nocc)
+    for g, r in zip(e, case["rimp2"]):
+        assert abs(g - r) <= 1e-13
+    F = O.rng(s + 13).standard_normal((N, N))
+    F = F + F.T
+    assert np.abs(O.build_fmo(mos, F) - ref["fmo"]).max() <= 1e-13
+
+
+def test_kat1_low_rank_identity():
+    """Canonical MP2 on (mn|ls) = sum_P L_Pmn L_Pls equals RI-MP2 with J = 1."""
+    k = GOLD["kat1"]
+    assert abs(k["canonical"][2] - k["ri"][2]) <= 1e-13
+    N, nocc, P = k["N"], k["nocc"], k["rank"]
+    eri, L = O.synth_eri(N, k["eri_seed"], rank=P)
+    mos = O.synth_orbitals(N, k["mos_seed"])
+    eps = np.array(k["eps"])
+    can = O.canonical_mp2(2 * nocc, O.motrans(mos, O.pack_eri(eri)), np.diag(eps))
+    bia = O.transform_ri(2 * nocc, mos, O.ri_build_bpq(np.eye(P), L))
+    ri = O.rimp2_energy(bia, eps, nocc, N - nocc)
+    for a, b, r in zip(can, ri, k["canonical"]):
+        assert abs(a - r) <= 1e-13 and abs(b - r) <= 1e-13
+
+
+def test_gradient_restatement_matches_finite_differences():
+    o, v, X = 2, 5, 6
+    B, eps = O.synth_rimp2(o, v, X, 77)
+    E, dB, de = O.rimp2_gradient(B, eps, o, v)
+    assert abs(E - O.rimp2_energy(B, eps, o, v)[2]) < 1e-14
+    h = 1e-6
+    r = O.rng(5)
+    for _ in range(6):
+        idx = tuple(int(r.integers(0, n)) for n in B.shape)
+        Bp, Bm = B.copy(), B.copy()
+        Bp[idx] += h
+        Bm[idx] -= h
+        fd = (O.rimp2_energy(Bp, eps, o, v)[2] - O.rimp2_energy(Bm, eps, o, v)[2]) / (2 * h)
+        assert abs(fd - dB[idx]) <= 1e-7 * max(1.0, abs(fd))
+    for p in range(o + v):
+        ep, em = eps.copy(), eps.copy()
+        ep[p] += h
+        em[p] -= h
+        fd = (O.rimp2_energy(B, ep, o, v)[2] - O.rimp2_energy(B, em, o, v)[2]) / (2 * h)
+        assert abs(fd - de[p]) <= 1e-7 * max(1.0, abs(fd))
+
+
+# ---- live reference (only where the checkout exists) -----------------------
+def _ref():
+    from oracle import refwrap
+    if not refwrap.available():
+        pytest.skip("reference checkout not present")
+    return refwrap
+
+
+@pytest.mark.parametrize("o,v,X,seed", [(3, 40, 33, 1), (9, 70, 130, 2), (1, 200, 10, 3)])
+def test_rimp2_energy_vs_live_reference(o, v, X, seed):
+    R = _ref()
+    B, eps = O.synth_rimp2(o, v, X, seed)
+    ref = R.rimp2_energy(B, eps, o, v)
+    got = O.rimp2_energy(B, eps, o, v)
+    for g, r in zip(got, ref):
+        assert abs(g - r) <= 1e-12 * max(1.0, abs(ref[2]))
+
+
+def test_ri_metric_with_cut_eigenvalues_vs_live_reference():
+    """Rank-deficient J: the 1e-10 relative cutoff removes eigenvalues."""
+    R = _ref()
+    X, N = 20, 6
+    r = O.rng(9)
+    V = r.standard_normal((X, 14))
+    J = V @ V.T  # rank 14
+    P3 = r.standard_normal((X, N, N))
+    P3 = P3 + P3.transpose(0, 2, 1)
+    bpq_ref = R.calculate_ri(J, P3)
+    jm, ncut = O.ri_metric_inv_sqrt(J)
+    assert ncut == X - 14
+    bpq = O.ri_build_bpq(jm, P3)
+    # the cut subspace is ill-conditioned; compare the metric-weighted product
+    G_ref = np.einsum("Pmn,Pls->mnls", bpq_ref, bpq_ref)
+    G = np.einsum("Pmn,Pls->mnls", bpq, bpq)
+    assert np.abs(G - G_ref).max() <= 1e-8 * np.abs(G_ref).max()
