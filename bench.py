@@ -1,0 +1,375 @@
+#!/usr/bin/env python3
+"""RI-MP2 energy benchmark (one JSON line on rank 0).
+
+Workload: the synthetic RI-MP2 energy at nocc=40, nvir=360, naux=1200 with
+B^Q_ia = G_Qia 0.05 exp(-Q/400), G ~ N(0,1), eps_occ ~ U[-1.5,-0.3],
+eps_vir ~ U[0.05,3.0] (seeded, numpy PCG64).  A step is one full RI-MP2 energy
+evaluation from the FP64 B tensor: slice pre-pass, fused tcgen05 energy kernel
+and the FP64 reduction.  Throughput is the algorithmic count
+F = 2 nocc^2 nvir^2 naux per step (the reference's full-(i,j) count,
+src/POSTHF/can_mp2.cc:82-88) over the device time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision split_bf16]
+  python bench.py --impl reference ...   # the reference's CPU path on host cores
+
+With N > 1 (torchrun, one rank per GPU) every rank runs an independent replica
+of the workload; value = N * F * K / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = ("RI-MP2 time-to-E_corr & TFLOP/s, split-BF16 vs FP64 GPU at |ΔE|≤1 µEh")
+NOCC, NVIR, NAUX, SEED = 40, 360, 1200, 2024
+FLOPS = 2.0 * NOCC * NOCC * NVIR * NVIR * NAUX
+WORKLOAD = (f"RI-MP2 energy nocc={NOCC} nvir={NVIR} naux={NAUX}; synthetic B = G diag(s_Q), "
+            f"s_Q = 0.05 exp(-Q/400), seed {SEED}")
+FALLBACK_PEAK_BF16 = 1900.0
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="split_bf16",
+                    choices=["split_bf16", "split_fp16", "fp64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+
+    def __init__(self, gpu):
+        self.rows = []
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(gpu)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": len(self.rows)}
+        try:
+            sm = [float(r[1]) for r in self.rows]
+            mx = [float(r[2]) for r in self.rows]
+            if sm:
+                out["sm_mhz"] = statistics.median(sm)
+                out["sm_max_mhz"] = max(mx)
+            reasons = set()
+            for r in self.rows:
+                for k, name in enumerate(self.NAMES):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(name)
+            out["reasons"] = sorted(reasons)
+        except Exception:
+            pass
+        return out
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the reference's algorithm on the host cores
+# ---------------------------------------------------------------------------
+def blas_threads():
+    try:
+        from threadpoolctl import threadpool_info
+
+        n = [i.get("num_threads") for i in threadpool_info() if i.get("user_api") == "blas"]
+        if n:
+            return int(max(n))
+    except Exception:
+        pass
+    return os.cpu_count() or 1
+
+
+def cpu_sample(B, eps, nocc_s, min_seconds=10.0, max_reps=50):
+    """Time the reference's RI-MP2 loop on the first nocc_s occupied orbitals
+    (nocc_s^2 of the workload's nocc^2 pair GEMMs, same nvir and naux).
+    Uses the reference's own compiled code (oracle/_ref) when it is present
+    on this machine, else the oracle's restatement (same BLAS calls).
+    Returns (tflops, kind, seconds, reps)."""
+    import numpy as np
+
+    from oracle import oracle as O
+
+    kind = "port"
+    fn = None
+    try:
+        from oracle import refwrap
+
+        if os.path.exists(refwrap.SO):
+            refwrap.lib()
+            fn = refwrap.rimp2_energy
+            kind = "reference"
+    except Exception:
+        fn = None
+    Bs = np.ascontiguousarray(B[:, :nocc_s, :])
+    es = np.concatenate([eps[:nocc_s], eps[NOCC:]])
+    if fn is None:
+        fn = O.rimp2_energy
+    fn(Bs, es, nocc_s, NVIR)  # warm
+    t0 = time.perf_counter()
+    reps = 0
+    while reps < max_reps:
+        fn(Bs, es, nocc_s, NVIR)
+        reps += 1
+        if time.perf_counter() - t0 >= min_seconds:
+            break
+    dt = time.perf_counter() - t0
+    f = 2.0 * nocc_s * nocc_s * NVIR * NVIR * NAUX * reps
+    return f / dt / 1e12, kind, dt, reps
+
+
+def read_traffic():
+    """DRAM bytes per launch of the energy kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "energy_tc_o40v360x1200.md")
+    try:
+        for line in open(path):
+            if line.strip().startswith("dram_bytes_per_launch"):
+                return float(line.split("=")[1].split()[0])
+    except Exception:
+        pass
+    return None
+
+
+def read_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        return FALLBACK_PEAK_BF16, "fallback"
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+
+    B, eps = O.synth_rimp2(NOCC, NVIR, NAUX, SEED)
+    nocc_s = 6  # 36 of the 1600 pair GEMMs per step
+    for _ in range(args.warmup):
+        cpu_sample(B, eps, nocc_s, min_seconds=0.0, max_reps=1)
+    times = []
+    kind = "port"
+    for _ in range(args.steps):
+        tf, kind, dt, reps = cpu_sample(B, eps, nocc_s, min_seconds=0.0, max_reps=1)
+        times.append(dt)
+    f_step = 2.0 * nocc_s * nocc_s * NVIR * NVIR * NAUX
+    tot = sum(times)
+    value = f_step * len(times) / tot / 1e12
+    sample = (f"nocc={nocc_s} of {NOCC} occupied orbitals ({nocc_s * nocc_s} of {NOCC * NOCC} "
+              f"pair GEMMs), nvir={NVIR}, naux={NAUX}, one pass per step")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": tot / len(times) * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "precision": "fp64 (reference CPU path)",
+                   "parallelism": "host cores"},
+        "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": blas_threads(),
+                         "kind": kind, "sample": sample},
+        "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import corr_gb300
+    from oracle import oracle as O
+
+    ws, rank, local = dist_env()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+    stream = torch.cuda.current_stream()
+
+    B, eps = O.synth_rimp2(NOCC, NVIR, NAUX, SEED)
+    Bd = torch.from_numpy(B).to(dev)
+    ed = torch.from_numpy(eps).to(dev)
+    ctx = corr_gb300.Context(dev, stream=stream)
+    ctx.set_timing(True)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    prec = args.precision
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(max(3, args.warmup)):
+        e_split = ctx.rimp2_energy(Bd, ed, NOCC, NVIR, NAUX, prec)
+
+    # ---- timed region: device time per step, L2 flushed between steps
+    launches0 = ctx.timing().launches_total
+    clocks = ClockSampler(dev) if rank == 0 else None
+    barrier()
+    step_ms, kern_ms = [], []
+    for _ in range(args.steps):
+        flush.fill_(1)  # not timed
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        e_split = ctx.rimp2_energy(Bd, ed, NOCC, NVIR, NAUX, prec)
+        t1.record(stream)
+        t1.synchronize()
+        step_ms.append(t0.elapsed_time(t1))
+        kern_ms.append(ctx.timing().kernel_ms)
+    barrier()
+    clk = clocks.stop() if clocks else None
+    launches = ctx.timing().launches_total - launches0
+    total_ms = sum(step_ms)
+    if dist is not None:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = ws * FLOPS * args.steps / (total_ms * 1e-3) / 1e12
+    ms_step = total_ms / args.steps
+
+    # ---- FP64 GPU form of the same job (the comparison form)
+    ctx.rimp2_energy(Bd, ed, NOCC, NVIR, NAUX, "fp64")
+    f64_ms = []
+    for _ in range(2):
+        flush.fill_(1)
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        e64 = ctx.rimp2_energy(Bd, ed, NOCC, NVIR, NAUX, "fp64")
+        t1.record(stream)
+        t1.synchronize()
+        f64_ms.append(t0.elapsed_time(t1))
+    f64 = statistics.median(f64_ms)
+
+    # ---- end to end through the public API with host buffers
+    Bh = torch.from_numpy(B).pin_memory()
+    eh = torch.from_numpy(eps).pin_memory()
+    ctx.rimp2_energy(Bh, eh, NOCC, NVIR, NAUX, prec)
+    n_e2e = max(3, min(args.steps, 10))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(n_e2e):
+        e_host = ctx.rimp2_energy(Bh, eh, NOCC, NVIR, NAUX, prec)
+    e2e_s = (time.perf_counter() - t0) / n_e2e
+    if dist is not None:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = B.nbytes + eps.nbytes
+    d2h = 72  # the library's result block (energies + device status word)
+
+    if rank != 0:
+        dist.destroy_process_group()
+        return
+
+    peak, peak_kind = read_peak()
+    kmean = statistics.mean(kern_ms)
+    achieved = FLOPS / (kmean * 1e-3) / 1e12
+    traffic = read_traffic()
+    cpu = None
+    if ws == 1 and not args.no_cpu_baseline:
+        tf, kind, dt, reps = cpu_sample(B, eps, NOCC, min_seconds=10.0, max_reps=20)
+        cpu = {"value": tf, "unit": "TFLOP/s", "cores": blas_threads(), "kind": kind,
+               "sample": f"{reps} full RI-MP2 energy evaluation(s) of the workload, "
+                         f"{dt:.1f} s"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16" if prec == "split_bf16" else ("f16" if prec == "split_fp16" else "f64"),
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "precision": prec, "global_batch": 1,
+                   "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "l2": "FP64 input 138 MB > L2 (129 MB); 256 MB L2 flush between timed "
+                         "steps, outside the timed region"},
+        "time_to_ecorr_ms": ms_step,
+        "energy": {"split": [e_split.e_ss, e_split.e_os, e_split.e_total],
+                   "fp64": [e64.e_ss, e64.e_os, e64.e_total],
+                   "abs_err_vs_fp64": abs(e_split.e_total - e64.e_total),
+                   "rel_err_vs_fp64": abs(e_split.e_total - e64.e_total) / abs(e64.e_total),
+                   "host_api_matches": e_host.e_total == e_split.e_total},
+        "fp64_form": {"ms_per_step": f64, "tflops": FLOPS / (f64 * 1e-3) / 1e12,
+                      "split_speedup": f64 / ms_step},
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "energy_tc_kernel", "kernel_ms": kmean,
+                     "peak_source": f"{peak_kind} bf16 dense (burst)",
+                     "flops_per_launch": FLOPS},
+        "cpu_baseline": cpu,
+        "e2e": {"value": FLOPS / e2e_s / 1e12 * ws, "unit": "TFLOP/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_s * 1e3},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -10,7 +10,7 @@ from __future__ import annotations
 
 import ctypes
 
-from ._lib import PRECISION, CorrError, MP2Energy, check, load
+from ._lib import PRECISION, CorrError, MP2Energy, Timing, check, load
 
 __all__ = ["Context", "CorrError", "MP2Energy", "PRECISION", "default_context",
            "run_canonical_mp2_ri"]
@@ -65,6 +65,15 @@ class Context:
     @property
     def sm_count(self):
         return self._L.corr_device_sm_count(self._h)
+
+    def set_timing(self, enable=True):
+        check(self._L.corr_set_timing(self._h, 1 if enable else 0))
+
+    def timing(self):
+        """Device timings of the last call (needs set_timing(True))."""
+        t = Timing()
+        check(self._L.corr_get_timing(self._h, ctypes.byref(t)))
+        return t
 
     def close(self):
         if getattr(self, "_h", None):

@@ -41,6 +41,11 @@ class MP2Energy(ctypes.Structure):
                 f"e_scs={self.e_scs!r})")
 
 
+class Timing(ctypes.Structure):
+    _fields_ = [("prepass_ms", ctypes.c_float), ("kernel_ms", ctypes.c_float),
+                ("total_ms", ctypes.c_float), ("launches_total", ctypes.c_longlong)]
+
+
 _vp = ctypes.c_void_p
 _i = ctypes.c_int
 _ll = ctypes.c_longlong
@@ -54,6 +59,8 @@ SIGNATURES = {
     "corr_set_stream": [_vp, _vp],
     "corr_last_error": [],
     "corr_device_sm_count": [_vp],
+    "corr_set_timing": [_vp, _i],
+    "corr_get_timing": [_vp, ctypes.POINTER(Timing)],
     "corr_rimp2_energy": [_vp, _i, _i, _i, _vp, _vp, _i, ctypes.POINTER(MP2Energy)],
 }
 _RESTYPES = {"corr_version": ctypes.c_char_p, "corr_last_error": ctypes.c_char_p}

@@ -122,10 +122,21 @@ int encode_tmap(CUtensorMap* m, CUtensorMapDataType dt, int rank, void* base,
 
 // Finish a call: copy the small result block back, synchronise, check the
 // device status word and the finiteness of the results.
+void mark(corr_context* c, int k) {
+  if (c->timing) cudaEventRecord(c->ev[k], c->stream);
+}
+
 int finish_results(corr_context* c, int nres) {
+  mark(c, 3);
   CORR_CUDA(cudaMemcpyAsync(c->hres, c->dres, sizeof(ResultBlock), cudaMemcpyDeviceToHost,
                             c->stream));
   CORR_CUDA(cudaStreamSynchronize(c->stream));
+  if (c->timing) {
+    cudaEventElapsedTime(&c->t_prepass, c->ev[0], c->ev[1]);
+    cudaEventElapsedTime(&c->t_kernel, c->ev[1], c->ev[2]);
+    cudaEventElapsedTime(&c->t_total, c->ev[0], c->ev[3]);
+    cudaGetLastError();
+  }
   if (c->hres->status & CORR_ERR_DEVICE_TIMEOUT) {
     set_error("a device-side wait exceeded its time limit");
     return CORR_ERR_DEVICE_TIMEOUT;
@@ -188,6 +199,8 @@ int corr_destroy(corr_context* c) {
   if (c->ws.ptr) cudaFree(c->ws.ptr);
   if (c->dres) cudaFree(c->dres);
   if (c->hres) cudaFreeHost(c->hres);
+  for (int k = 0; k < 4; ++k)
+    if (c->ev[k]) cudaEventDestroy(c->ev[k]);
   delete c;
   return CORR_OK;
 }
@@ -199,6 +212,23 @@ int corr_set_stream(corr_context* c, void* stream) {
 }
 
 int corr_device_sm_count(const corr_context* c) { return c ? c->sms : 0; }
+
+int corr_set_timing(corr_context* c, int enable) {
+  CORR_CHECK_ARG(c != nullptr, "null context");
+  if (enable && !c->ev[0])
+    for (int k = 0; k < 4; ++k) CORR_CUDA(cudaEventCreate(&c->ev[k]));
+  c->timing = enable != 0;
+  return CORR_OK;
+}
+
+int corr_get_timing(const corr_context* c, corr_timing* out) {
+  CORR_CHECK_ARG(c != nullptr && out != nullptr, "null argument");
+  out->prepass_ms = c->t_prepass;
+  out->kernel_ms = c->t_kernel;
+  out->total_ms = c->t_total;
+  out->launches_total = c->launches;
+  return CORR_OK;
+}
 
 int corr_rimp2_energy(corr_context* c, int nocc, int nvir, int naux, const double* bia,
                       const double* eps, int precision, corr_mp2_energy* out) {
@@ -266,6 +296,7 @@ int rimp2_energy_device(corr_context* c, int nocc, int nvir, int naux, const dou
   Carver w{c->ws.ptr, 0};
   carve(w, &b_slot, &e_slot, &sw, &partials);
 
+  mark(c, 0);
   const double* d_b = static_cast<const double*>(stage_in(c, bia, nb * 8, b_slot));
   const double* d_e = static_cast<const double*>(stage_in(c, eps, ne * 8, e_slot));
   if (!d_b || !d_e) {
@@ -275,8 +306,11 @@ int rimp2_energy_device(corr_context* c, int nocc, int nvir, int naux, const dou
   CORR_CUDA(cudaMemsetAsync(c->dres, 0, sizeof(ResultBlock), c->stream));
 
   if (!tc) {
+    mark(c, 1);
     CORR_CUDA(launch_energy_fp64(d_b, d_e, sh, partials, grid, c->stream));
+    mark(c, 2);
     CORR_CUDA(launch_energy_reduce(partials, grid, nullptr, c->dres->e, c->stream));
+    c->launches += 2;
     return CORR_OK;
   }
   const int fmt = precision == CORR_PREC_SPLIT_FP16 ? 0 : 1;
@@ -289,9 +323,12 @@ int rimp2_energy_device(corr_context* c, int nocc, int nvir, int naux, const dou
   const CUtensorMapDataType dt =
       fmt == 0 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
   CORR_TRY(encode_tmap(&tm, dt, 3, sw.S, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_64B));
+  mark(c, 1);
   CORR_CUDA(launch_energy_tc(tm, d_e, sw.sc, sw.dg, sh, Qp, fmt, p, partials, grid,
                              &c->dres->status, c->stream));
+  mark(c, 2);
   CORR_CUDA(launch_energy_reduce(partials, grid, sw.scale, c->dres->e, c->stream));
+  c->launches += 5;  // rowstat, slice, rowfactor, energy, reduce
   return CORR_OK;
 }
 

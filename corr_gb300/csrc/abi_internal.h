@@ -43,12 +43,18 @@ struct corr_context {
   corr::Workspace ws;
   corr::ResultBlock* dres = nullptr;  // device
   corr::ResultBlock* hres = nullptr;  // pinned host
+  bool timing = false;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  float t_prepass = 0.f, t_kernel = 0.f, t_total = 0.f;
+  long long launches = 0;
 };
 
 namespace corr {
 const void* stage_in(corr_context* c, const void* p, size_t bytes, void* slot);
 int stage_out(corr_context* c, void* dst, const void* src, size_t bytes);
 int finish_results(corr_context* c, int nres);
+// Record timing event k (0 start, 1 before the main kernel, 2 after it, 3 end).
+void mark(corr_context* c, int k);
 int rimp2_energy_device(corr_context* c, int nocc, int nvir, int naux, const double* bia,
                         const double* eps, int precision);
 }  // namespace corr

@@ -44,11 +44,14 @@ enum corr_status {
 
 /* Arithmetic of the RI-MP2 contraction (ia|jb) = sum_Q B^Q_ia B^Q_jb. */
 enum corr_precision {
-  CORR_PREC_FP64 = 0,       /* FP64 end to end                                   */
-  CORR_PREC_SPLIT_FP16 = 1, /* B = hi + lo in FP16 (power-of-two pre-scale), three
-                               products hi.hi + hi.lo + lo.hi on tcgen05, FP32
-                               accumulation in TMEM, FP64 pair-energy sum        */
-  CORR_PREC_SPLIT_BF16 = 2  /* the same with BF16 hi/lo                          */
+  CORR_PREC_FP64 = 0,       /* FP64 end to end (FP64 mma.sync)                   */
+  CORR_PREC_SPLIT_FP16 = 1, /* each row (i,a) of B scaled by a power of two and
+                               split into three 7-bit integer slices stored as
+                               FP16; the six slice products of orders 0-2 run on
+                               tcgen05 with exact FP32 integer accumulation in
+                               TMEM; (ia|ia) in FP64; FP64 pair-energy sums     */
+  CORR_PREC_SPLIT_BF16 = 2  /* the same slices stored as BF16 (bit-identical
+                               results: the slices are small integers)          */
 };
 
 typedef struct corr_context corr_context;
@@ -84,6 +87,19 @@ const char* corr_last_error(void);
 
 /* Number of SMs of the context's GPU. */
 int corr_device_sm_count(const corr_context* ctx);
+
+/* Per-call device timings (no reference counterpart; the reference only
+ * prints wall-clock totals, src/main.cc:212-214).  With timing enabled every
+ * call records CUDA events on the context stream around its stages. */
+typedef struct corr_timing {
+  float prepass_ms; /* input staging + slice pre-pass                          */
+  float kernel_ms;  /* the dominant kernel of the call                         */
+  float total_ms;   /* whole call on the device                                */
+  long long launches_total; /* kernels this context has launched so far     */
+} corr_timing;
+
+int corr_set_timing(corr_context* ctx, int enable);
+int corr_get_timing(const corr_context* ctx, corr_timing* out);
 
 /* ---- RI-MP2 energy ----------------------------------------------------- */
 
