@@ -100,6 +100,103 @@ class Context:
         return out
 
 
+    def rimp2_energy_async(self, bia, eps, nocc, nvir, naux, precision, out):
+        """Enqueue only (device tensors; out = device float64[4] receiving
+        E_SS, E_OS, E, E_SCS).  Capturable in a CUDA graph after a first call."""
+        check(self._L.corr_rimp2_energy_async(self._h, int(nocc), int(nvir), int(naux),
+                                              _ptr(bia), _ptr(eps), _prec(precision),
+                                              _ptr(out)))
+
+    def sync(self):
+        check(self._L.corr_sync(self._h))
+
+    # -- FP64 transforms (src/POSTHF/motrans.cc, ri.cc) and canonical MP2 ----
+    @staticmethod
+    def _out(like, shape, out):
+        if out is not None:
+            return out
+        if hasattr(like, "device") and getattr(like, "is_cuda", False):
+            import torch
+
+            return torch.empty(shape, dtype=torch.float64, device=like.device)
+        import numpy as np
+
+        return np.zeros(shape)
+
+    def build_fmo(self, mos, fmat, out=None):
+        """build_FMo (motrans.cc:8): FMo = C F C^T with mos[p][mu]."""
+        N = mos.shape[0]
+        out = self._out(mos, (N, N), out)
+        check(self._L.corr_build_fmo(self._h, N, _ptr(mos), _ptr(fmat), _ptr(out)))
+        return out
+
+    def motrans(self, nroe, mos, packed, out=None):
+        """MOtrans (motrans.cc:35): full (ij|kl) from the packed AO list."""
+        N = mos.shape[0]
+        out = self._out(mos, (N, N, N, N), out)
+        check(self._L.corr_motrans(self._h, nroe, N, _ptr(mos), packed.nrofint,
+                                   _ptr(packed.sortcount), _ptr(packed.intval),
+                                   _ptr(packed.intnums), _ptr(out)))
+        return out
+
+    def motrans_ovov(self, nroe, mos, packed, out=None):
+        """(ia|jb) block [i][a][j][b] from the packed AO list."""
+        N = mos.shape[0]
+        o = nroe // 2
+        v = N - o
+        out = self._out(mos, (o, v, o, v), out)
+        check(self._L.corr_motrans_ovov(self._h, nroe, N, _ptr(mos), packed.nrofint,
+                                        _ptr(packed.sortcount), _ptr(packed.intval),
+                                        _ptr(packed.intnums), _ptr(out)))
+        return out
+
+    def canonical_mp2(self, nroe, prec, eps):
+        """run_canonical_mp2 (can_mp2.cc:11) on the full MO tensor."""
+        out = MP2Energy()
+        check(self._L.corr_canonical_mp2(self._h, nroe, prec.shape[0], _ptr(prec), _ptr(eps),
+                                         ctypes.byref(out)))
+        return out
+
+    def canonical_mp2_ovov(self, ovov, eps):
+        out = MP2Energy()
+        o, v = ovov.shape[0], ovov.shape[1]
+        check(self._L.corr_canonical_mp2_ovov(self._h, o, v, _ptr(ovov), _ptr(eps),
+                                              ctypes.byref(out)))
+        return out
+
+    def transform_ri(self, nroe, mos, bpq, out=None):
+        """transform_ri (ri.cc:147): Bia[Q][i][a] from BPQ[Q][mu][nu]."""
+        X, N = bpq.shape[0], bpq.shape[1]
+        o = nroe // 2
+        out = self._out(bpq, (X, o, N - o), out)
+        check(self._L.corr_transform_ri(self._h, nroe, N, X, _ptr(mos), _ptr(bpq), _ptr(out)))
+        return out
+
+    def ri_build_bpq(self, jm12, pmn, out=None):
+        """BPQ = J^-1/2 (Q|mn) (ri.cc:102-103)."""
+        X, N = pmn.shape[0], pmn.shape[1]
+        out = self._out(pmn, (X, N, N), out)
+        check(self._L.corr_ri_build_bpq(self._h, X, N, _ptr(jm12), _ptr(pmn), _ptr(out)))
+        return out
+
+    def ri_metric_inv_sqrt(self, J, tol=1e-10, out=None):
+        """J^-1/2 with the reference's eigenvalue cutoff (ri.cc:50-69).
+        Returns (jm12, ncut)."""
+        X = J.shape[0]
+        out = self._out(J, (X, X), out)
+        ncut = ctypes.c_int(0)
+        check(self._L.corr_ri_metric_inv_sqrt(self._h, X, _ptr(J), float(tol), _ptr(out),
+                                              ctypes.byref(ncut)))
+        return out, ncut.value
+
+    def calculate_ri(self, J, pmn, out=None):
+        """calculate_ri (ri.cc:7) downstream of the integrals: BPQ = J^-1/2 (Q|mn)."""
+        X, N = pmn.shape[0], pmn.shape[1]
+        out = self._out(pmn, (X, N, N), out)
+        check(self._L.corr_calculate_ri(self._h, X, N, _ptr(J), _ptr(pmn), _ptr(out)))
+        return out
+
+
 _DEFAULT = None
 
 

@@ -62,6 +62,17 @@ SIGNATURES = {
     "corr_set_timing": [_vp, _i],
     "corr_get_timing": [_vp, ctypes.POINTER(Timing)],
     "corr_rimp2_energy": [_vp, _i, _i, _i, _vp, _vp, _i, ctypes.POINTER(MP2Energy)],
+    "corr_rimp2_energy_async": [_vp, _i, _i, _i, _vp, _vp, _i, _vp],
+    "corr_sync": [_vp],
+    "corr_build_fmo": [_vp, _i, _vp, _vp, _vp],
+    "corr_motrans": [_vp, _i, _i, _vp, _ll, _vp, _vp, _vp, _vp],
+    "corr_motrans_ovov": [_vp, _i, _i, _vp, _ll, _vp, _vp, _vp, _vp],
+    "corr_canonical_mp2": [_vp, _i, _i, _vp, _vp, ctypes.POINTER(MP2Energy)],
+    "corr_canonical_mp2_ovov": [_vp, _i, _i, _vp, _vp, ctypes.POINTER(MP2Energy)],
+    "corr_transform_ri": [_vp, _i, _i, _i, _vp, _vp, _vp],
+    "corr_ri_build_bpq": [_vp, _i, _i, _vp, _vp, _vp],
+    "corr_ri_metric_inv_sqrt": [_vp, _i, _vp, _d, _vp, ctypes.POINTER(_i)],
+    "corr_calculate_ri": [_vp, _i, _i, _vp, _vp, _vp],
 }
 _RESTYPES = {"corr_version": ctypes.c_char_p, "corr_last_error": ctypes.c_char_p}
 

@@ -123,7 +123,10 @@ int encode_tmap(CUtensorMap* m, CUtensorMapDataType dt, int rank, void* base,
 // Finish a call: copy the small result block back, synchronise, check the
 // device status word and the finiteness of the results.
 void mark(corr_context* c, int k) {
-  if (c->timing) cudaEventRecord(c->ev[k], c->stream);
+  if (!c->timing) return;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(c->stream, &cs);
+  if (cs == cudaStreamCaptureStatusNone) cudaEventRecord(c->ev[k], c->stream);
 }
 
 int finish_results(corr_context* c, int nres) {
@@ -213,6 +216,35 @@ int corr_set_stream(corr_context* c, void* stream) {
 
 int corr_device_sm_count(const corr_context* c) { return c ? c->sms : 0; }
 
+int corr_rimp2_energy_async(corr_context* c, int nocc, int nvir, int naux, const double* bia,
+                            const double* eps, int precision, double* energies_dev) {
+  CORR_CHECK_ARG(c != nullptr, "null context");
+  CORR_CHECK_ARG(bia && eps && energies_dev, "corr_rimp2_energy_async: null pointer argument");
+  CORR_CHECK_ARG(nocc >= 1 && nvir >= 1 && naux >= 1, "corr_rimp2_energy_async: bad sizes");
+  CORR_CHECK_ARG(precision >= CORR_PREC_FP64 && precision <= CORR_PREC_SPLIT_BF16,
+                 "corr_rimp2_energy_async: unknown precision %d", precision);
+  CORR_CHECK_ARG(is_device_ptr(bia) && is_device_ptr(eps) && is_device_ptr(energies_dev),
+                 "corr_rimp2_energy_async: bia, eps and energies_dev must be device pointers");
+  CORR_CUDA(cudaSetDevice(c->device));
+  return rimp2_energy_device(c, nocc, nvir, naux, bia, eps, precision, energies_dev);
+}
+
+int corr_sync(corr_context* c) {
+  CORR_CHECK_ARG(c != nullptr, "null context");
+  CORR_CUDA(cudaSetDevice(c->device));
+  int st = 0;
+  CORR_CUDA(cudaMemcpyAsync(&c->hres->status, &c->dres->status, sizeof(int),
+                            cudaMemcpyDeviceToHost, c->stream));
+  CORR_CUDA(cudaStreamSynchronize(c->stream));
+  st = c->hres->status;
+  CORR_CUDA(cudaMemsetAsync(&c->dres->status, 0, sizeof(int), c->stream));
+  if (st & CORR_ERR_DEVICE_TIMEOUT) {
+    set_error("a device-side wait exceeded its time limit");
+    return CORR_ERR_DEVICE_TIMEOUT;
+  }
+  return CORR_OK;
+}
+
 int corr_set_timing(corr_context* c, int enable) {
   CORR_CHECK_ARG(c != nullptr, "null context");
   if (enable && !c->ev[0])
@@ -260,7 +292,8 @@ namespace corr {
 // Enqueue the whole energy evaluation on the context stream; results land in
 // c->dres.  Shared by the public entry point and the batched driver.
 int rimp2_energy_device(corr_context* c, int nocc, int nvir, int naux, const double* bia,
-                        const double* eps, int precision) {
+                        const double* eps, int precision, double* res) {
+  double* out_e = res ? res : c->dres->e;
   const size_t nb = (size_t)naux * nocc * nvir;
   const size_t ne = (size_t)nocc + nvir;
   const bool b_dev = is_device_ptr(bia), e_dev = is_device_ptr(eps);
@@ -303,13 +336,13 @@ int rimp2_energy_device(corr_context* c, int nocc, int nvir, int naux, const dou
     set_error("host-to-device copy failed: %s", cudaGetErrorString(cudaGetLastError()));
     return CORR_ERR_CUDA;
   }
-  CORR_CUDA(cudaMemsetAsync(c->dres, 0, sizeof(ResultBlock), c->stream));
+  if (!res) CORR_CUDA(cudaMemsetAsync(c->dres, 0, sizeof(ResultBlock), c->stream));
 
   if (!tc) {
     mark(c, 1);
     CORR_CUDA(launch_energy_fp64(d_b, d_e, sh, partials, grid, c->stream));
     mark(c, 2);
-    CORR_CUDA(launch_energy_reduce(partials, grid, nullptr, c->dres->e, c->stream));
+    CORR_CUDA(launch_energy_reduce(partials, grid, nullptr, out_e, c->stream));
     c->launches += 2;
     return CORR_OK;
   }
@@ -324,10 +357,14 @@ int rimp2_energy_device(corr_context* c, int nocc, int nvir, int naux, const dou
       fmt == 0 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
   CORR_TRY(encode_tmap(&tm, dt, 3, sw.S, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_64B));
   mark(c, 1);
+  if (!c->attrs_set) {
+    CORR_CUDA(prepare_energy_tc());
+    c->attrs_set = true;
+  }
   CORR_CUDA(launch_energy_tc(tm, d_e, sw.sc, sw.dg, sh, Qp, fmt, p, partials, grid,
                              &c->dres->status, c->stream));
   mark(c, 2);
-  CORR_CUDA(launch_energy_reduce(partials, grid, sw.scale, c->dres->e, c->stream));
+  CORR_CUDA(launch_energy_reduce(partials, grid, sw.scale, out_e, c->stream));
   c->launches += 5;  // rowstat, slice, rowfactor, energy, reduce
   return CORR_OK;
 }

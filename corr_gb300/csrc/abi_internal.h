@@ -47,6 +47,7 @@ struct corr_context {
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   float t_prepass = 0.f, t_kernel = 0.f, t_total = 0.f;
   long long launches = 0;
+  bool attrs_set = false;  // one-time kernel attributes (kept out of graph capture)
 };
 
 namespace corr {
@@ -55,6 +56,8 @@ int stage_out(corr_context* c, void* dst, const void* src, size_t bytes);
 int finish_results(corr_context* c, int nres);
 // Record timing event k (0 start, 1 before the main kernel, 2 after it, 3 end).
 void mark(corr_context* c, int k);
+// Enqueue an RI-MP2 energy; results go to `res` (device, 4 doubles; NULL =
+// the context's result block).
 int rimp2_energy_device(corr_context* c, int nocc, int nvir, int naux, const double* bia,
-                        const double* eps, int precision);
+                        const double* eps, int precision, double* res = nullptr);
 }  // namespace corr

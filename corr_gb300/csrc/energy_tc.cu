@@ -361,13 +361,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
 }  // namespace
 
+cudaError_t prepare_energy_tc() {
+  return cudaFuncSetAttribute(energy_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)kSmemBytes);
+}
+
 cudaError_t launch_energy_tc(const CUtensorMap& tmap, const double* eps, const float* sc,
                              const float* dg, const EnergyShape& sh, int Qp, int fmt, int p,
                              double* partials, int grid, int* status, cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(energy_tc_kernel,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)kSmemBytes);
-  if (e != cudaSuccess) return e;
   const uint32_t idesc = idesc_f16((uint32_t)fmt, TILE, TILE);
   const float inv_l = ldexpf(1.0f, -(p + 1));
   energy_tc_kernel<<<grid, NTHREADS, kSmemBytes, s>>>(tmap, eps, sc, dg, sh, Qp / KB, idesc,

@@ -45,6 +45,7 @@ cudaError_t launch_energy_reduce(const double* partials, int n, const double* sc
 cudaError_t launch_energy_tc(const CUtensorMap& tmap, const double* eps, const float* sc,
                              const float* dg, const EnergyShape& sh, int Qp, int fmt, int p,
                              double* partials, int grid, int* status, cudaStream_t s);
+cudaError_t prepare_energy_tc();  // one-time attributes (dynamic smem size)
 constexpr int kTcTile = 128;
 
 // FP64 form on the FP64 tensor path (energy_fp64.cu).

@@ -63,40 +63,63 @@ __device__ __forceinline__ uint16_t to16(double v) {
 }
 
 // B[Q][r] -> slices S[l][r][Qp], l = 0..2, zero padded for Q >= naux.
+// Block = 256 threads on a 64 (Q) x 64 (r) tile: reads are coalesced along r
+// (the reference layout), each thread then converts 16 consecutive Q of one r
+// and writes 32 contiguous bytes per slice plane.
 template <int FMT>
-__global__ void slice_kernel(const double* __restrict__ b, int naux, long long R, int Qp, int p,
-                             const int* __restrict__ erow, uint16_t* __restrict__ S) {
-  __shared__ double tile[32][33];
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const long long r0 = (long long)blockIdx.x * 32;
-  const int q0 = blockIdx.y * 32;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    int q = q0 + ty + 8 * k;
-    long long r = r0 + tx;
-    tile[ty + 8 * k][tx] = (q < naux && r < R) ? b[(long long)q * R + r] : 0.0;
-  }
-  __syncthreads();
-  const double L = ldexp(1.0, p + 1);
-  const size_t plane = (size_t)R * Qp;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    long long r = r0 + ty + 8 * k;
-    int q = q0 + tx;
-    if (r < R) {
-      int e = erow[r];
-      double x = (e > INT_MIN / 8) ? ldexp(tile[tx][ty + 8 * k], -e) : 0.0;
-      double s0 = rint(x);
-      x = (x - s0) * L;
-      double s1 = rint(x);
-      x = (x - s1) * L;
-      double s2 = rint(x);
-      size_t at = (size_t)r * Qp + q;
-      S[at] = to16<FMT>(s0);
-      S[plane + at] = to16<FMT>(s1);
-      S[2 * plane + at] = to16<FMT>(s2);
+__global__ void __launch_bounds__(256) slice_kernel(const double* __restrict__ b, int naux,
+                                                    long long R, int Qp, int p,
+                                                    const int* __restrict__ erow,
+                                                    uint16_t* __restrict__ S) {
+  __shared__ double tile[64][65];
+  const int t = threadIdx.x;
+  const long long r0 = (long long)blockIdx.x * 64;
+  const int q0 = blockIdx.y * 64;
+  {
+    const int c = t & 63;
+#pragma unroll 4
+    for (int k = t >> 6; k < 64; k += 4) {
+      const int q = q0 + k;
+      const long long r = r0 + c;
+      tile[k][c] = (q < naux && r < R) ? b[(long long)q * R + r] : 0.0;
     }
   }
+  __syncthreads();
+  const int rl = t >> 2, qc = (t & 3) * 16;
+  const long long r = r0 + rl;
+  if (r >= R || q0 + qc >= Qp) return;
+  const int e = erow[r];
+  const bool live = e > INT_MIN / 8;
+  const double L = ldexp(1.0, p + 1);
+  __align__(16) uint16_t h0[16];
+  __align__(16) uint16_t h1[16];
+  __align__(16) uint16_t h2[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    double x = live ? ldexp(tile[qc + k][rl], -e) : 0.0;
+    const double s0 = rint(x);
+    x = (x - s0) * L;
+    const double s1 = rint(x);
+    x = (x - s1) * L;
+    const double s2 = rint(x);
+    h0[k] = to16<FMT>(s0);
+    h1[k] = to16<FMT>(s1);
+    h2[k] = to16<FMT>(s2);
+  }
+  const size_t plane = (size_t)R * Qp;
+  const size_t at = (size_t)r * Qp + q0 + qc;  // 16 x 2 B, 32-byte aligned (Qp % 32 == 0)
+  uint4* d0 = reinterpret_cast<uint4*>(S + at);
+  uint4* d1 = reinterpret_cast<uint4*>(S + plane + at);
+  uint4* d2 = reinterpret_cast<uint4*>(S + 2 * plane + at);
+  const uint4* v0 = reinterpret_cast<const uint4*>(h0);
+  const uint4* v1 = reinterpret_cast<const uint4*>(h1);
+  const uint4* v2 = reinterpret_cast<const uint4*>(h2);
+  d0[0] = v0[0];
+  d0[1] = v0[1];
+  d1[0] = v1[0];
+  d1[1] = v1[1];
+  d2[0] = v2[0];
+  d2[1] = v2[1];
 }
 
 // Per-row FP32 factors for the energy kernel: sc_r = 2^(e_r - e_ref) and the
@@ -165,11 +188,11 @@ cudaError_t launch_slices(const double* b, int naux, long long R, int Qp, int fm
   if (e != cudaSuccess) return e;
   rowstat_kernel<<<(unsigned)((R + 31) / 32), dim3(32, 8), 0, s>>>(b, naux, R, p, w.erow, w.diag,
                                                                    w.eref);
-  dim3 grid((unsigned)((R + 31) / 32), (unsigned)(Qp / 32));
+  dim3 grid((unsigned)((R + 63) / 64), (unsigned)((Qp + 63) / 64));
   if (fmt == 0)
-    slice_kernel<0><<<grid, dim3(32, 8), 0, s>>>(b, naux, R, Qp, p, w.erow, w.S);
+    slice_kernel<0><<<grid, 256, 0, s>>>(b, naux, R, Qp, p, w.erow, w.S);
   else
-    slice_kernel<1><<<grid, dim3(32, 8), 0, s>>>(b, naux, R, Qp, p, w.erow, w.S);
+    slice_kernel<1><<<grid, 256, 0, s>>>(b, naux, R, Qp, p, w.erow, w.S);
   rowfactor_kernel<<<(unsigned)((R + 255) / 256 < 1024 ? (R + 255) / 256 : 1024), 256, 0, s>>>(
       w.erow, w.diag, R, w.eref, w.sc, w.dg, w.scale);
   return cudaGetLastError();

@@ -113,6 +113,85 @@ int corr_get_timing(const corr_context* ctx, corr_timing* out);
 int corr_rimp2_energy(corr_context* ctx, int nocc, int nvir, int naux, const double* bia,
                       const double* eps, int precision, corr_mp2_energy* out);
 
+/* Asynchronous form of corr_rimp2_energy for device-resident data (no
+ * reference counterpart): bia and eps must be device pointers; the call only
+ * enqueues work on the context stream and writes {E_SS, E_OS, E, E_SCS} to
+ * the device buffer energies_dev[4].  It performs no host synchronisation,
+ * so it can be captured into a CUDA graph once a first call with the same
+ * sizes has sized the context workspace.  Device-side failures (a timed-out
+ * wait) are reported by the next corr_sync. */
+int corr_rimp2_energy_async(corr_context* ctx, int nocc, int nvir, int naux, const double* bia,
+                            const double* eps, int precision, double* energies_dev);
+
+/* Synchronise the context stream and return the device status accumulated
+ * by asynchronous calls since the last corr_sync (CORR_OK or
+ * CORR_ERR_DEVICE_TIMEOUT); clears it. */
+int corr_sync(corr_context* ctx);
+
+/* ---- FP64 transforms and canonical MP2 ---------------------------------- */
+
+/* Replaces build_FMo (src/POSTHF/motrans.cc:8-32, declared at
+ * src/POSTHF/motrans.h:22): fmo[i*N+j] = sum_{mu,nu} mos[i*N+mu] fmat[mu*N+nu]
+ * mos[j*N+nu], as two FP64 GEMMs.  The caller owns fmo (N*N). */
+int corr_build_fmo(corr_context* ctx, int nroao, const double* mos, const double* fmat,
+                   double* fmo);
+
+/* Replaces MOtrans (src/POSTHF/motrans.cc:35-211, declared at
+ * src/POSTHF/motrans.h:21): prec[((i*N+j)*N+k)*N+l] = (ij|kl) over all MOs from
+ * the reference's packed AO list (TEints: intval, intnums, sortcount as produced
+ * by resort_integrals, src/SCF/ops_rhf.cc:750-900).  The caller owns prec (N^4
+ * doubles; the reference allocated it inside MOtrans).  N <= 65535. */
+int corr_motrans(corr_context* ctx, int nroe, int nroao, const double* mos, long long nrofint,
+                 const long long* sortcount, const double* intval,
+                 const unsigned short* intnums, double* prec);
+
+/* The (ia|jb) block only, ovov[((i*nvir+a)*nocc+j)*nvir+b], through four
+ * quarter transforms of cost 2oN^4 + 2ovN^3 + 2o^2vN^2 + 2o^2v^2N.  Same sums as
+ * corr_motrans restricted to occupied/virtual index ranges. */
+int corr_motrans_ovov(corr_context* ctx, int nroe, int nroao, const double* mos,
+                      long long nrofint, const long long* sortcount, const double* intval,
+                      const unsigned short* intnums, double* ovov);
+
+/* Replaces run_canonical_mp2 (src/POSTHF/can_mp2.cc:11-49, declared at
+ * src/POSTHF/can_mp2.h:4) on the full MO tensor prec (corr_motrans layout);
+ * eps[nroao] = diagonal of FMo. */
+int corr_canonical_mp2(corr_context* ctx, int nroe, int nroao, const double* prec,
+                       const double* eps, corr_mp2_energy* out);
+
+/* The same energy from an (ia|jb) block in corr_motrans_ovov layout. */
+int corr_canonical_mp2_ovov(corr_context* ctx, int nocc, int nvir, const double* ovov,
+                            const double* eps, corr_mp2_energy* out);
+
+/* Replaces transform_ri (src/POSTHF/ri.cc:147-172, declared at
+ * src/POSTHF/ri.h:9): bia[(Q*o+i)*v+a] = sum_{mu,nu} mos[i*N+mu]
+ * bpq[(Q*N+mu)*N+nu] mos[(o+a)*N+nu], o = nroe/2, v = nroao - o.  naux <= 65535. */
+int corr_transform_ri(corr_context* ctx, int nroe, int nroao, int naux, const double* mos,
+                      const double* bpq, double* bia);
+
+/* The B build of calculate_ri (src/POSTHF/ri.cc:102-103):
+ * bpq[P][mu][nu] = sum_Q jm12[P][Q] pmn[Q][mu][nu]. */
+int corr_ri_build_bpq(corr_context* ctx, int naux, int nroao, const double* jm12,
+                      const double* pmn, double* bpq);
+
+/* ---- RI metric ----------------------------------------------------------- */
+
+/* The J^-1/2 part of calculate_ri (src/POSTHF/ri.cc:50-69): eigen-decompose
+ * J (naux x naux, symmetric), zero every eigenvalue with lambda/lambda_max <
+ * tol or lambda < 0 (the reference uses tol = 1e-10), take lambda^-1/2 of the
+ * rest and return jm12 = V diag V^T.  FP64 throughout (parallel Jacobi
+ * eigensolver).  *ncut (optional) receives the number of eigenvalues cut.
+ * CORR_ERR_NOT_PD when J has no positive eigenvalue. */
+int corr_ri_metric_inv_sqrt(corr_context* ctx, int naux, const double* J, double tol,
+                            double* jm12, int* ncut);
+
+/* Replaces calculate_ri (src/POSTHF/ri.cc:7-106, declared at src/POSTHF/ri.h:8)
+ * downstream of the integral engine: given the 2-index metric J[P][Q] = (P|Q)
+ * and the 3-index integrals pmn[P][mu][nu] = (P|mu nu) (the reference computes
+ * both with libint inside calculate_ri, ri.cc:25-47, 70-100), returns
+ * bpq = J^-1/2 (Q|mu nu) with the reference's eigenvalue cutoff. */
+int corr_calculate_ri(corr_context* ctx, int naux, int nroao, const double* J, const double* pmn,
+                      double* bpq);
+
 #ifdef __cplusplus
 }
 #endif
