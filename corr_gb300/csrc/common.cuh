@@ -222,17 +222,17 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 // Occupied-pair index -> (i, j) with i <= j, pairs ordered row by row:
-// p = i*o - i*(i-1)/2 + (j - i).
+// p = i*o - i*(i-1)/2 + (j - i).  FP32 estimate, then exact integer fix-up.
 __host__ __device__ inline void pair_decode(int p, int o, int* i, int* j) {
-  // invert with a float estimate, then fix up
-  double b = 2.0 * o + 1.0;
-  int ii = (int)((b - sqrt(b * b - 8.0 * p)) * 0.5);
+  const float b = 2.0f * o + 1.0f;
+  long long ii = (long long)((b - sqrtf(fmaxf(b * b - 8.0f * p, 0.0f))) * 0.5f);
   if (ii < 0) ii = 0;
   if (ii > o - 1) ii = o - 1;
-  while (ii > 0 && ii * o - ii * (ii - 1) / 2 > p) --ii;
-  while (ii + 1 < o && (ii + 1) * o - (ii + 1) * ii / 2 <= p) ++ii;
-  *i = ii;
-  *j = ii + (p - (ii * o - ii * (ii - 1) / 2));
+  auto start = [o](long long r) { return r * o - r * (r - 1) / 2; };
+  while (ii > 0 && start(ii) > p) --ii;
+  while (ii + 1 < o && start(ii + 1) <= p) ++ii;
+  *i = (int)ii;
+  *j = (int)(ii + (p - start(ii)));
 }
 
 // Tile pair index -> (A, B) with A <= B, same ordering.

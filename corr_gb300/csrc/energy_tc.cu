@@ -10,7 +10,8 @@
 // whose partial sums are exact integers (split.cu), then the epilogue forms
 //   d = sc_row sc_col (acc_0 + acc_1/L + acc_2/L^2)   (FP32, round-to-nearest).
 // D1 is parked in TMEM columns 384-511 while D2 accumulates in 0-383.  For
-// i == j, D2 == D1 and phase 2 is skipped.  On the (i==j, A==B) diagonal the
+// i == j, D2 == D1 and phase 2 is skipped; for A == B, D2 = D1^T is obtained
+// by a 32x32-block exchange through shared memory instead of a second pass.  On the (i==j, A==B) diagonal the
 // element (ia|ia) is replaced by its FP64 value.  The energy epilogue is the
 // one of energy_fp64.cu:
 //   E_OS -= f w (D1^2 + D2^2)/D,  E_SS -= f w (D1 - D2)^2/D,
@@ -51,6 +52,8 @@ struct Ctl {
   float db[TILE];
   float scb[TILE];
   double red[2][4];
+  float tbuf[4][32][33];  // D1 -> D1^T exchange on diagonal tile pairs
+  int wok[2][4];          // per-warp wait outcome, combined into one decision
 };
 
 constexpr size_t kSmemBytes = (size_t)STAGES * STAGE_BYTES + sizeof(Ctl) + 1024;
@@ -145,7 +148,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         int i, j, A, B;
         unit_decode(u, sh, &i, &j, &A, &B);
         const int A0 = A * TILE, B0 = B * TILE;
-        const int nph = (i == j) ? 1 : 2;
+        const int nph = (i == j || A == B) ? 1 : 2;
         for (int phs = 0; phs < nph && ok; ++phs) {
           const int x = phs == 0 ? i : j;  // row operand slab
           const int y = phs == 0 ? j : i;  // column operand slab
@@ -187,7 +190,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       for (long long u = blockIdx.x; u < sh.nunits && ok; u += gridDim.x) {
         int i, j, A, B;
         unit_decode(u, sh, &i, &j, &A, &B);
-        const int nph = (i == j) ? 1 : 2;
+        const int nph = (i == j || A == B) ? 1 : 2;
         for (int phs = 0; phs < nph && ok; ++phs) {
           if (!mbar_wait(&ctl->aempty, (nuse & 1) ^ 1, abort, status)) {
             ok = false;
@@ -264,8 +267,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       double uos = 0.0, uss = 0.0;
 
       // ---- phase 1: D1
+      // The outcome of the wait is made uniform over the four epilogue warps
+      // (named barriers below must be reached by all of them or none).
       bool got = !dead && __all_sync(0xffffffffu,
                                      mbar_wait(&ctl->afull, nuse & 1, abort, status));
+      if (lane == 0) ctl->wok[nuse & 1][q] = got ? 1 : 0;
+      named_bar(1, 128);
+      got = ctl->wok[nuse & 1][0] & ctl->wok[nuse & 1][1] & ctl->wok[nuse & 1][2] &
+            ctl->wok[nuse & 1][3];
       if (!got) dead = true;
       if (!dead) {
         tc_fence_after();
@@ -284,6 +293,37 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
             uos += (double)fos;
           }
+        } else if (A == B) {
+          // Diagonal tile pair: D2 = D1^T.  Four rounds; in round k warp q
+          // publishes its D1 block of column chunk (q+k)%4 and takes the block
+          // of warp (q-k)%4, which is the D1^T block of column chunk (q-k)%4.
+#pragma unroll 1
+          for (int k = 0; k < 4; ++k) {
+            float d[32];
+            const int cw = 32 * ((q + k) & 3);
+            load_level_sum(tq, cw, inv_l, inv_l2, sca1, ctl->scb, d);
+#pragma unroll
+            for (int x = 0; x < 32; ++x) ctl->tbuf[q][lane][x] = d[x];
+            named_bar(1, 128);
+            const int wr = (q - k) & 3;
+            const int cr = 32 * wr;
+            float d2[32];
+#pragma unroll
+            for (int x = 0; x < 32; ++x) d2[x] = ctl->tbuf[wr][x][lane];
+            load_level_sum(tq, cr, inv_l, inv_l2, sca1, ctl->scb, d);
+            float fos = 0.f, fss = 0.f;
+#pragma unroll
+            for (int x = 0; x < 32; ++x) {
+              const float r = __frcp_rn(da + ctl->db[cr + x]);
+              const float y1 = d[x], y2 = d2[x];
+              fos = fmaf(fmaf(y1, y1, y2 * y2), r, fos);
+              const float df = y1 - y2;
+              fss = fmaf(df * df, r, fss);
+            }
+            uos += (double)fos;
+            uss += (double)fss;
+            named_bar(1, 128);  // tbuf is rewritten in the next round
+          }
         } else {
 #pragma unroll 1
           for (int c = 0; c < TILE; c += 32) {
@@ -299,12 +339,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       }
       ++nuse;
 
-      // ---- phase 2: D2 (i != j): rows from slab j, columns from slab i
-      if (!same) {
+      // ---- phase 2: D2 (i != j, A != B): rows from slab j, columns from slab i
+      if (!same && A != B) {
         named_bar(1, 128);  // everyone is done with the phase-1 column scales
         if (B0 + et < v) ctl->scb[et] = sc[(size_t)i * v + B0 + et];
         named_bar(1, 128);
         got = !dead && __all_sync(0xffffffffu, mbar_wait(&ctl->afull, nuse & 1, abort, status));
+        if (lane == 0) ctl->wok[nuse & 1][q] = got ? 1 : 0;
+        named_bar(1, 128);
+        got = ctl->wok[nuse & 1][0] & ctl->wok[nuse & 1][1] & ctl->wok[nuse & 1][2] &
+              ctl->wok[nuse & 1][3];
         if (!got) dead = true;
         if (!dead) {
           tc_fence_after();

@@ -27,18 +27,44 @@ namespace corr {
 
 namespace {
 
+// |x| as an ordered integer (IEEE bit pattern without the sign).
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+}
+
+// round(b * 2^k) to nearest (ties away from zero) by integer arithmetic on the
+// IEEE-754 fields; exact for every |result| < 2^31.  Zero and subnormal b map
+// to 0 (their contribution lies far below the row scale).
+__device__ __forceinline__ int round_scaled(double b, int k) {
+  const long long bits = __double_as_longlong(b);
+  const int E = (int)((bits >> 52) & 0x7ff);
+  if (E == 0) return 0;
+  const long long m = (bits & 0xfffffffffffffll) | (1ll << 52);
+  const int sh = 1075 - E - k;  // value = m * 2^-sh
+  long long X;
+  if (sh <= 0) X = m << (-sh > 10 ? 10 : -sh);  // not reached for |b| <= row max
+  else if (sh > 62) X = 0;
+  else X = (m + (1ll << (sh - 1))) >> sh;
+  return bits < 0 ? -(int)X : (int)X;
+}
+
 // Row statistics over Q for each r: e_r, the FP64 diagonal sum_Q B^2, and the
-// global maximum exponent (atomicMax).  Block = 32 rows x 8 Q-groups.
+// global maximum exponent (atomicMax).  Block = 32 rows x 8 Q-groups.  The
+// maximum is taken on the integer bit patterns (no FP64 compare); the
+// diagonal needs one FP64 FMA per element.
 __global__ void rowstat_kernel(const double* __restrict__ b, int naux, long long R, int p,
                                int* __restrict__ erow, double* __restrict__ diag, int* eref) {
-  __shared__ double smax[8][32], ssum[8][32];
+  __shared__ unsigned long long smax[8][32];
+  __shared__ double ssum[8][32];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const long long r = (long long)blockIdx.x * 32 + tx;
-  double m = 0.0, s = 0.0;
+  unsigned long long m = 0;
+  double s = 0.0;
   if (r < R)
     for (int q = ty; q < naux; q += 8) {
-      double x = b[(long long)q * R + r];
-      m = fmax(m, fabs(x));
+      const double x = b[(long long)q * R + r];
+      const unsigned long long ax = abs_bits(x);
+      m = ax > m ? ax : m;
       s = fma(x, x, s);
     }
   smax[ty][tx] = m;
@@ -46,26 +72,30 @@ __global__ void rowstat_kernel(const double* __restrict__ b, int naux, long long
   __syncthreads();
   if (ty == 0 && r < R) {
     for (int k = 1; k < 8; ++k) {
-      m = fmax(m, smax[k][tx]);
+      m = smax[k][tx] > m ? smax[k][tx] : m;
       s += ssum[k][tx];
     }
-    int e = (m > 0.0) ? ilogb(m) - (p - 1) : INT_MIN / 4;
+    const int E = (int)(m >> 52);  // biased exponent of the row maximum
+    const bool live = m != 0 && E != 0;
+    const int e = live ? (E - 1023) - (p - 1) : INT_MIN / 4;
     erow[r] = e;
     diag[r] = s;
-    if (m > 0.0) atomicMax(eref, e);
+    if (live) atomicMax(eref, e);
   }
 }
 
 template <int FMT>
-__device__ __forceinline__ uint16_t to16(double v) {
-  if (FMT == 0) return __half_as_ushort(__double2half(v));
-  return __bfloat16_as_ushort(__double2bfloat16(v));
+__device__ __forceinline__ uint16_t to16i(int v) {
+  if (FMT == 0) return __half_as_ushort(__int2half_rn(v));
+  return __bfloat16_as_ushort(__int2bfloat16_rn(v));
 }
 
 // B[Q][r] -> slices S[l][r][Qp], l = 0..2, zero padded for Q >= naux.
 // Block = 256 threads on a 64 (Q) x 64 (r) tile: reads are coalesced along r
 // (the reference layout), each thread then converts 16 consecutive Q of one r
-// and writes 32 contiguous bytes per slice plane.
+// and writes 32 contiguous bytes per slice plane.  Digit extraction is integer
+// arithmetic: X = round(B 2^(2(p+1) - e_r)), s0 = round(X / L^2),
+// s1 = round((X - s0 L^2) / L), s2 = remainder.
 template <int FMT>
 __global__ void __launch_bounds__(256) slice_kernel(const double* __restrict__ b, int naux,
                                                     long long R, int Qp, int p,
@@ -90,21 +120,21 @@ __global__ void __launch_bounds__(256) slice_kernel(const double* __restrict__ b
   if (r >= R || q0 + qc >= Qp) return;
   const int e = erow[r];
   const bool live = e > INT_MIN / 8;
-  const double L = ldexp(1.0, p + 1);
+  const int lb = p + 1;            // bits per level
+  const int k2 = 2 * lb - e;       // X = B 2^k2
   __align__(16) uint16_t h0[16];
   __align__(16) uint16_t h1[16];
   __align__(16) uint16_t h2[16];
 #pragma unroll
   for (int k = 0; k < 16; ++k) {
-    double x = live ? ldexp(tile[qc + k][rl], -e) : 0.0;
-    const double s0 = rint(x);
-    x = (x - s0) * L;
-    const double s1 = rint(x);
-    x = (x - s1) * L;
-    const double s2 = rint(x);
-    h0[k] = to16<FMT>(s0);
-    h1[k] = to16<FMT>(s1);
-    h2[k] = to16<FMT>(s2);
+    const int X = live ? round_scaled(tile[qc + k][rl], k2) : 0;
+    const int s0 = (X + (1 << (2 * lb - 1))) >> (2 * lb);
+    const int rem = X - (s0 << (2 * lb));
+    const int s1 = (rem + (1 << (lb - 1))) >> lb;
+    const int s2 = rem - (s1 << lb);
+    h0[k] = to16i<FMT>(s0);
+    h1[k] = to16i<FMT>(s1);
+    h2[k] = to16i<FMT>(s2);
   }
   const size_t plane = (size_t)R * Qp;
   const size_t at = (size_t)r * Qp + q0 + qc;  // 16 x 2 B, 32-byte aligned (Qp % 32 == 0)
