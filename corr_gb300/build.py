@@ -17,6 +17,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libcorr_gb300.so")
+SHIM_SRC = os.path.join(PKG, "shim", "corr_shim.cc")
+SHIM_LIB = os.path.join(PKG, "libcorr_shim.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -71,7 +73,21 @@ def build(verbose=False, ptxas_info=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
+    build_shim()
     return LIB
+
+
+def build_shim():
+    """The drop-in C++ layer (reference signatures) over libcorr_gb300.so."""
+    deps = [SHIM_SRC, os.path.join(PKG, "shim", "corr_shim.h"), LIB]
+    if not _needs(SHIM_LIB, deps):
+        return SHIM_LIB
+    cmd = ["g++", "-O2", "-std=c++14", "-fPIC", "-shared", "-o", SHIM_LIB, SHIM_SRC,
+           "-L" + PKG, "-lcorr_gb300", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("shim build failed:\n" + r.stdout + r.stderr)
+    return SHIM_LIB
 
 
 if __name__ == "__main__":
