@@ -128,6 +128,25 @@ int corr_rimp2_energy_async(corr_context* ctx, int nocc, int nvir, int naux, con
  * CORR_ERR_DEVICE_TIMEOUT); clears it. */
 int corr_sync(corr_context* ctx);
 
+/* Allocation-free RI-MP2 energy (no counterpart in the reference).  For
+ * callers that cannot call cudaMalloc -- a host program whose device memory is
+ * all handed out by its own pool allocator, or a latency-critical loop where an
+ * allocation and its implicit synchronisation are not allowed.  Same kernels
+ * and results as corr_rimp2_energy, but no context and no allocation: the
+ * scratch is a fixed 32 MiB device array compiled into the library, which every
+ * GPU that loads the library holds until the process exits.  Limit: the
+ * precision forms need about 6*nocc*nvir*naux bytes of scratch and larger
+ * problems are rejected with CORR_ERR_BAD_ARG; the FP64 form needs only a few
+ * KB.  bia and eps must be device pointers of `device`; `stream` is a
+ * cudaStream_t; the call returns after the stream has finished the work and
+ * writes the energies to the host struct `out`.  Its first call on a device
+ * looks up the array's device address and sets kernel attributes there: make
+ * it before any stream capture on that device.  All calls share the array:
+ * calls whose GPU work overlaps race and must be serialised by the caller. */
+int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int nvir, int naux,
+                              const double* bia, const double* eps, int precision,
+                              corr_mp2_energy* out);
+
 /* ---- FP64 transforms and canonical MP2 ---------------------------------- */
 
 /* Replaces build_FMo (src/POSTHF/motrans.cc:8-32, declared at
