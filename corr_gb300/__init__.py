@@ -107,6 +107,15 @@ class Context:
                                               _ptr(bia), _ptr(eps), _prec(precision),
                                               _ptr(out)))
 
+    def rimp2_gradient(self, bia, eps, nocc, nvir, naux, dbia=None, deps=None):
+        """(E, dE/dB, dE/deps) of the RI-MP2 energy, FP64."""
+        dbia = self._out(bia, tuple(bia.shape), dbia)
+        deps = self._out(eps, tuple(eps.shape), deps)
+        e = MP2Energy()
+        check(self._L.corr_rimp2_gradient(self._h, int(nocc), int(nvir), int(naux), _ptr(bia),
+                                          _ptr(eps), _ptr(dbia), _ptr(deps), ctypes.byref(e)))
+        return e.e_total, dbia, deps
+
     def sync(self):
         check(self._L.corr_sync(self._h))
 

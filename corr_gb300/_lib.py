@@ -64,6 +64,7 @@ SIGNATURES = {
     "corr_rimp2_energy": [_vp, _i, _i, _i, _vp, _vp, _i, ctypes.POINTER(MP2Energy)],
     "corr_rimp2_energy_async": [_vp, _i, _i, _i, _vp, _vp, _i, _vp],
     "corr_sync": [_vp],
+    "corr_rimp2_gradient": [_vp, _i, _i, _i, _vp, _vp, _vp, _vp, ctypes.POINTER(MP2Energy)],
     "corr_rimp2_energy_noalloc": [_i, _vp, _i, _i, _i, _vp, _vp, _i, ctypes.POINTER(MP2Energy)],
     "corr_build_fmo": [_vp, _i, _vp, _vp, _vp],
     "corr_motrans": [_vp, _i, _i, _vp, _ll, _vp, _vp, _vp, _vp],

@@ -6,7 +6,7 @@
 // every tensor-core partial sum an exact integer below 2^24:
 //
 //   B^Q_r = 2^(e_r) (s0 + s1/L + s2/L^2),   r = (i,a),  L = 2^(p+1),
-//   s_k = integers in [-2^p, 2^p] (exact in FP16 and BF16), p = 6 for naux <= 2048,
+//   s_k = integers in [-2^p, 2^p] (exact in FP16 and BF16), p = 6..8 chosen from naux,
 //   e_r = ilogb(max_Q |B^Q_r|) - (p-1)  (one power-of-two scale per row).
 //
 // The energy kernel forms  acc_m = sum_{k+l=m} sum_Q s_k(ia) s_l(jb)  for
@@ -206,8 +206,10 @@ __global__ void energy_reduce_kernel(const double* __restrict__ part, int n,
 }  // namespace
 
 int slice_bits_for(int Qp) {
-  // largest p with 2 * Qp * 2^(2p) <= 2^24 (acc_0 and acc_1 exact), capped at 6
-  int p = 6;
+  // Largest p with 2 * Qp * 2^(2p) <= 2^24, so acc_0 and acc_1 stay exact
+  // integers for any data; at most 8, so every digit in [-2^p, 2^p] is an
+  // exact BF16 (and FP16) value.  naux <= 2048 gives p >= 6 (21+ bits).
+  int p = 8;
   while (p > 1 && (double)2 * Qp * (double)(1ll << (2 * p)) > 16777216.0) --p;
   return p;
 }

@@ -128,6 +128,16 @@ int corr_rimp2_energy_async(corr_context* ctx, int nocc, int nvir, int naux, con
  * CORR_ERR_DEVICE_TIMEOUT); clears it. */
 int corr_sync(corr_context* ctx);
 
+/* RI-MP2 adjoint (no counterpart in the reference, which has no gradients):
+ * dbia[(Q*nocc+i)*nvir+a] = dE/dB^Q_ia and deps[p] = dE/d eps_p for
+ * E = E_OS + E_SS of corr_rimp2_energy, in FP64.  The (ia|jb) tiles are
+ * recomputed, never stored: per block of occupied orbitals a transient panel
+ * G^{ij}_ab = -(4 (ia|jb) - 2 (ib|ja)) / D (at most ~1 GiB) feeds one GEMM
+ * dB = 2 B G^T; dE/d eps comes from W = (2(ia|jb) - (ib|ja))(ia|jb)/D^2.
+ * e_out (optional) receives E in e_total. */
+int corr_rimp2_gradient(corr_context* ctx, int nocc, int nvir, int naux, const double* bia,
+                        const double* eps, double* dbia, double* deps, corr_mp2_energy* e_out);
+
 /* Allocation-free RI-MP2 energy (no counterpart in the reference).  For
  * callers that cannot call cudaMalloc -- a host program whose device memory is
  * all handed out by its own pool allocator, or a latency-critical loop where an

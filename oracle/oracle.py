@@ -183,6 +183,29 @@ def rimp2_gradient(B, eps, nocc, nvir):
     return E, dB, deps
 
 
+def rimp2_energy_local(B, eps, nocc, nvir, i, a):
+    """The part of the RI-MP2 energy (can_mp2.cc:82-97 summed over all ordered
+    (i,j)) that contains an integral with orbital pair (i,a): every term of the
+    pairs (i,j) and (j,i) whose (c,d) has c == a or d == a.  It changes with
+    B^Q_ia exactly as the full energy does, at O(nocc nvir naux) cost, so
+    central differences of it equal those of the full energy."""
+    naux = B.shape[0]
+    Bv = np.asarray(B).reshape(naux, nocc, nvir)
+    ev = np.asarray(eps[nocc:nocc + nvir])
+    row = np.einsum("q,qjb->jb", Bv[:, i, a], Bv)        # M^{ij}_{a,b}
+    col = np.einsum("qc,qj->jc", Bv[:, i, :], Bv[:, :, a])  # M^{ij}_{c,a}
+    tot = 0.0
+    for j in range(nocc):
+        w = 1.0 if j == i else 2.0  # (j,i) mirrors (i,j)
+        Dr = ((ev[a] + ev) - eps[i]) - eps[j]
+        r, c = row[j], col[j]
+        t_row = -((2.0 * r - c) * r / Dr).sum()   # (a, d):  M_ad, M_da = col[d]
+        t_col = -((2.0 * c - r) * c / Dr).sum()   # (c, a):  M_ca = col[c], M_ac = row[c]
+        t_aa = -((2.0 * r[a] - c[a]) * r[a] / Dr[a])
+        tot += w * (t_row + t_col - t_aa)
+    return tot
+
+
 # ---------------------------------------------------------------------------
 # RI metric and B build: src/POSTHF/ri.cc:50-69, 102-103
 # ---------------------------------------------------------------------------

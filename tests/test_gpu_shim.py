@@ -19,7 +19,7 @@ def _energies(text, block):
     i = text.index(block)
     vals = {}
     for key in ("EMP2_SS:", "EMP2_OS:", "EMP2:"):
-        m = re.search(re.escape(key) + r"\s+(\S+)", text[i:])
+        m = re.search(re.escape(key) + r"\s*(\S+)", text[i:])
         vals[key] = float(m.group(1))
     return vals["EMP2_SS:"], vals["EMP2_OS:"], vals["EMP2:"]
 
@@ -38,8 +38,12 @@ def test_shim_pipeline(tmp_path, N, nocc, X, precision):
     pk = O.pack_eri(eri)
     mos = O.synth_orbitals(N, 12 + N)
     r = O.rng(13 + N)
-    F = r.standard_normal((N, N))
-    F = F + F.T
+    # Fock matrix whose MO diagonal is ordered (occupied below virtual):
+    # F = C^T diag(e) C + small symmetric noise, with mos = C (orthonormal rows)
+    e = np.concatenate([np.sort(r.uniform(-1.5, -0.3, nocc)),
+                        np.sort(r.uniform(0.05, 3.0, N - nocc))])
+    noise = r.standard_normal((N, N)) * 1e-3
+    F = mos.T @ np.diag(e) @ mos + noise + noise.T
     L = r.standard_normal((X, X)) / np.sqrt(X)
     J = L @ L.T + 0.5 * np.eye(X)
     P3 = r.standard_normal((X, N, N)) * 0.1
