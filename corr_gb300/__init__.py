@@ -10,7 +10,7 @@ from __future__ import annotations
 
 import ctypes
 
-from ._lib import PRECISION, CorrError, MP2Energy, Timing, check, load
+from ._lib import PRECISION, CorrError, MP2Energy, RIMP2Instance, Timing, check, load
 
 __all__ = ["Context", "CorrError", "MP2Energy", "PRECISION", "default_context",
            "run_canonical_mp2_ri"]
@@ -115,6 +115,72 @@ class Context:
         check(self._L.corr_rimp2_gradient(self._h, int(nocc), int(nvir), int(naux), _ptr(bia),
                                           _ptr(eps), _ptr(dbia), _ptr(deps), ctypes.byref(e)))
         return e.e_total, dbia, deps
+
+    # -- batched RI-MP2 ---------------------------------------------------------
+    @staticmethod
+    def _instances(items):
+        """items: iterable of (B[Q][i][a], eps, nocc, nvir) with device tensors."""
+        items = list(items)
+        arr = (RIMP2Instance * len(items))()
+        for k, (B, e, o, v) in enumerate(items):
+            arr[k].nocc, arr[k].nvir, arr[k].naux = int(o), int(v), int(B.shape[0])
+            arr[k].bia = _ptr(B).value
+            arr[k].eps = _ptr(e).value
+        return arr, len(items)
+
+    def rimp2_energy_batched(self, items, precision="split_bf16"):
+        arr, n = self._instances(items)
+        out = (MP2Energy * n)()
+        check(self._L.corr_rimp2_energy_batched(self._h, n, arr, _prec(precision), out))
+        return list(out)
+
+    def rimp2_energy_batched_async(self, items, precision, out):
+        """Enqueue only; out = device float64[4*n]. Capturable after a first call."""
+        arr, n = self._instances(items)
+        self._keep = arr  # the library copies the table during the call; keep for safety
+        check(self._L.corr_rimp2_energy_batched_async(self._h, n, arr, _prec(precision),
+                                                      _ptr(out)))
+
+    def set_batch_policy(self, order, stages):
+        check(self._L.corr_set_batch_policy(self._h, int(order), int(stages)))
+
+    def batch_autotune(self, items, precision="split_bf16", cache=None):
+        """Pick the batched launch variant by timing them on this batch.  With
+        a cache path, results are stored per batch signature (sorted shape
+        list) and reused without timing."""
+        import hashlib
+        import json
+        import os
+
+        items = list(items)
+        sig = hashlib.sha1(json.dumps(sorted((int(B.shape[0]), int(o), int(v))
+                                              for (B, _, o, v) in items)).encode()).hexdigest()
+        key = f"{sig}:{precision}"
+        db = {}
+        if cache and os.path.exists(cache):
+            try:
+                with open(cache) as f:
+                    db = json.load(f)
+            except Exception:
+                db = {}
+        if key in db:
+            order, stages = db[key]["order"], db[key]["stages"]
+            self.set_batch_policy(order, stages)
+            return order, stages, db[key]["ms"]
+        arr, n = self._instances(items)
+        order, stages, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        check(self._L.corr_rimp2_batch_autotune(self._h, n, arr, _prec(precision),
+                                                ctypes.byref(order), ctypes.byref(stages),
+                                                ctypes.byref(ms)))
+        if cache:
+            db[key] = {"order": order.value, "stages": stages.value, "ms": ms.value}
+            d = os.path.dirname(os.path.abspath(cache))
+            os.makedirs(d, exist_ok=True)
+            tmp = cache + ".tmp"
+            with open(tmp, "w") as f:
+                json.dump(db, f, indent=1)
+            os.replace(tmp, cache)
+        return order.value, stages.value, ms.value
 
     def sync(self):
         check(self._L.corr_sync(self._h))

@@ -46,6 +46,11 @@ class Timing(ctypes.Structure):
                 ("total_ms", ctypes.c_float), ("launches_total", ctypes.c_longlong)]
 
 
+class RIMP2Instance(ctypes.Structure):
+    _fields_ = [("nocc", ctypes.c_int), ("nvir", ctypes.c_int), ("naux", ctypes.c_int),
+                ("bia", ctypes.c_void_p), ("eps", ctypes.c_void_p)]
+
+
 _vp = ctypes.c_void_p
 _i = ctypes.c_int
 _ll = ctypes.c_longlong
@@ -66,6 +71,12 @@ SIGNATURES = {
     "corr_sync": [_vp],
     "corr_rimp2_gradient": [_vp, _i, _i, _i, _vp, _vp, _vp, _vp, ctypes.POINTER(MP2Energy)],
     "corr_rimp2_energy_noalloc": [_i, _vp, _i, _i, _i, _vp, _vp, _i, ctypes.POINTER(MP2Energy)],
+    "corr_rimp2_energy_batched": [_vp, _i, ctypes.POINTER(RIMP2Instance), _i,
+                                  ctypes.POINTER(MP2Energy)],
+    "corr_rimp2_energy_batched_async": [_vp, _i, ctypes.POINTER(RIMP2Instance), _i, _vp],
+    "corr_set_batch_policy": [_vp, _i, _i],
+    "corr_rimp2_batch_autotune": [_vp, _i, ctypes.POINTER(RIMP2Instance), _i, ctypes.POINTER(_i),
+                                  ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_float)],
     "corr_build_fmo": [_vp, _i, _vp, _vp, _vp],
     "corr_motrans": [_vp, _i, _i, _vp, _ll, _vp, _vp, _vp, _vp],
     "corr_motrans_ovov": [_vp, _i, _i, _vp, _ll, _vp, _vp, _vp, _vp],

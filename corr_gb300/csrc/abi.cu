@@ -200,6 +200,8 @@ int corr_destroy(corr_context* c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   if (c->ws.ptr) cudaFree(c->ws.ptr);
+  if (c->batch_out.ptr) cudaFree(c->batch_out.ptr);
+  if (c->pinned) cudaFreeHost(c->pinned);
   if (c->dres) cudaFree(c->dres);
   if (c->hres) cudaFreeHost(c->hres);
   for (int k = 0; k < 4; ++k)

@@ -48,6 +48,13 @@ struct corr_context {
   float t_prepass = 0.f, t_kernel = 0.f, t_total = 0.f;
   long long launches = 0;
   bool attrs_set = false;  // one-time kernel attributes (kept out of graph capture)
+  // batched driver
+  bool batch_attrs_set = false;
+  int batch_order = 1;   // 0 input order, 1 cost-descending
+  int batch_stages = 4;
+  corr::Workspace batch_out;
+  void* pinned = nullptr;
+  size_t pinned_cap = 0;
 };
 
 namespace corr {

@@ -1,0 +1,298 @@
+// Host side of the batched RI-MP2 driver: instance table, per-instance slicing,
+// unit-order policies, the synchronous/asynchronous entry points and the
+// autotuner that picks the launch variant (unit order x pipeline depth) by
+// timing them on the caller's batch.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "abi_internal.h"
+#include "batch.h"
+#include "common.cuh"
+#include "kernels.h"
+
+namespace corr {
+
+namespace {
+
+struct Plan {
+  std::vector<int> order;           // table position -> caller index
+  std::vector<BatchInst> table;     // host copy (device pointers filled)
+  std::vector<CUtensorMap> tmaps;
+  long long total = 0;
+};
+
+double instance_cost(const corr_rimp2_instance& x) {
+  return 2.0 * x.nocc * (double)x.nocc * x.nvir * (double)x.nvir * x.naux;
+}
+
+int grow_pinned(corr_context* c, size_t bytes) {
+  if (bytes <= c->pinned_cap) return CORR_OK;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(c->stream, &cs);
+  if (cs != cudaStreamCaptureStatusNone) {
+    set_error("batched call inside stream capture needs a first call outside capture");
+    return CORR_ERR_BAD_ARG;
+  }
+  if (c->pinned) cudaFreeHost(c->pinned);
+  c->pinned = nullptr;
+  c->pinned_cap = 0;
+  if (cudaMallocHost(&c->pinned, bytes * 2) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("pinned host allocation failed");
+    return CORR_ERR_OOM;
+  }
+  c->pinned_cap = bytes * 2;
+  return CORR_OK;
+}
+
+// Enqueue one batched evaluation; energies (4 per caller instance) to `out`.
+int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int precision,
+                  double* out, int order_policy, int stages) {
+  const bool tc = precision != CORR_PREC_FP64;
+  // ---- plan: order and per-instance shapes
+  std::vector<int> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  if (order_policy == 1)
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+      return instance_cost(in[a]) > instance_cost(in[b]);
+    });
+  struct Shape {
+    int Qp, p;
+    long long R;
+    EnergyShape sh;
+  };
+  std::vector<Shape> shp(n);
+  Carver cv{nullptr, 0};
+  long long total = 0;
+  for (int k = 0; k < n; ++k) {
+    const corr_rimp2_instance& x = in[order[k]];
+    Shape& s = shp[k];
+    s.Qp = ((x.naux + 31) / 32) * 32;
+    s.p = slice_bits_for(s.Qp);
+    s.R = (long long)x.nocc * x.nvir;
+    s.sh = make_energy_shape(x.nocc, x.nvir, x.naux, tc ? kTcTile : kF64Tile);
+    total += s.sh.nunits;
+  }
+  // ---- workspace
+  auto carve = [&](Carver& w, std::vector<SliceWork>& sws, double** unit_part, BatchInst** dtab,
+                   CUtensorMap** dmaps, int** dorder, unsigned long long** queue) {
+    sws.resize(n);
+    for (int k = 0; k < n; ++k) {
+      if (!tc) continue;
+      const Shape& s = shp[k];
+      SliceWork& sw = sws[k];
+      sw.S = static_cast<uint16_t*>(w.take((size_t)3 * s.R * s.Qp * 2));
+      sw.erow = static_cast<int*>(w.take((size_t)s.R * 4));
+      sw.diag = static_cast<double*>(w.take((size_t)s.R * 8));
+      sw.sc = static_cast<float*>(w.take((size_t)s.R * 4));
+      sw.dg = static_cast<float*>(w.take((size_t)s.R * 4));
+      sw.eref = static_cast<int*>(w.take(16));
+      sw.scale = static_cast<double*>(w.take(16));
+    }
+    *unit_part = static_cast<double*>(w.take((size_t)(tc ? total : (long long)c->sms * 2 * n) * 16));
+    *dtab = static_cast<BatchInst*>(w.take(sizeof(BatchInst) * n));
+    *dmaps = static_cast<CUtensorMap*>(w.take(sizeof(CUtensorMap) * n));
+    *dorder = static_cast<int*>(w.take(sizeof(int) * n));
+    *queue = static_cast<unsigned long long*>(w.take(16));
+  };
+  std::vector<SliceWork> sws;
+  double* unit_part;
+  BatchInst* dtab;
+  CUtensorMap* dmaps;
+  int* dorder;
+  unsigned long long* queue;
+  carve(cv, sws, &unit_part, &dtab, &dmaps, &dorder, &queue);
+  if (c->ws.cap < cv.used) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(c->stream, &cs);
+    if (cs != cudaStreamCaptureStatusNone) {
+      set_error("batched call inside stream capture needs a first call outside capture");
+      return CORR_ERR_BAD_ARG;
+    }
+  }
+  CORR_TRY(c->ws.reserve(cv.used));
+  Carver w{c->ws.ptr, 0};
+  carve(w, sws, &unit_part, &dtab, &dmaps, &dorder, &queue);
+
+  if (!tc) {
+    // FP64 comparison form: one fused kernel per instance
+    const int grid = c->sms * 2;
+    for (int k = 0; k < n; ++k) {
+      const corr_rimp2_instance& x = in[order[k]];
+      EnergyShape sh = shp[k].sh;
+      int g = grid;
+      if ((long long)g > sh.nunits) g = (int)sh.nunits;
+      double* part = unit_part + (size_t)k * grid * 2;
+      CORR_CUDA(launch_energy_fp64(x.bia, x.eps, sh, part, g, c->stream));
+      CORR_CUDA(launch_energy_reduce(part, g, nullptr, out + 4 * (size_t)order[k], c->stream));
+    }
+    c->launches += 2LL * n;
+    return CORR_OK;
+  }
+
+  // ---- per-instance slicing and the host copy of the table
+  const int fmt = precision == CORR_PREC_SPLIT_FP16 ? 0 : 1;
+  const size_t hbytes = sizeof(BatchInst) * n + sizeof(CUtensorMap) * n + sizeof(int) * n + 256;
+  CORR_TRY(grow_pinned(c, hbytes));
+  char* hp = static_cast<char*>(c->pinned);
+  BatchInst* htab = reinterpret_cast<BatchInst*>(hp);
+  CUtensorMap* hmaps = reinterpret_cast<CUtensorMap*>(
+      hp + ((sizeof(BatchInst) * n + 127) & ~(size_t)127));
+  int* horder = reinterpret_cast<int*>(reinterpret_cast<char*>(hmaps) + sizeof(CUtensorMap) * n);
+  long long ub = 0;
+  for (int k = 0; k < n; ++k) {
+    const corr_rimp2_instance& x = in[order[k]];
+    const Shape& s = shp[k];
+    CORR_CUDA(launch_slices(x.bia, x.naux, s.R, s.Qp, fmt, s.p, sws[k], c->stream));
+    const uint64_t dims[3] = {(uint64_t)s.Qp, (uint64_t)x.nvir, (uint64_t)3 * x.nocc};
+    const uint64_t strides[2] = {(uint64_t)s.Qp * 2, (uint64_t)x.nvir * s.Qp * 2};
+    const uint32_t box[3] = {32, (uint32_t)kTcTile, 1};
+    CORR_TRY(encode_tmap(&hmaps[k],
+                         fmt == 0 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                  : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+                         3, sws[k].S, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_64B));
+    BatchInst& b = htab[k];
+    b.eps = x.eps;
+    b.sc = sws[k].sc;
+    b.dg = sws[k].dg;
+    b.scale = sws[k].scale;
+    b.unit_begin = ub;
+    b.nunits = s.sh.nunits;
+    b.o = x.nocc;
+    b.v = x.nvir;
+    b.ntiles = s.sh.ntiles;
+    b.ntpairs = s.sh.ntpairs;
+    b.nkb = s.Qp / 32;
+    b.inv_l = ldexpf(1.0f, -(s.p + 1));
+    horder[k] = order[k];
+    ub += s.sh.nunits;
+  }
+  c->launches += 3LL * n;
+  CORR_CUDA(cudaMemcpyAsync(dtab, htab, sizeof(BatchInst) * n, cudaMemcpyHostToDevice, c->stream));
+  CORR_CUDA(cudaMemcpyAsync(dmaps, hmaps, sizeof(CUtensorMap) * n, cudaMemcpyHostToDevice,
+                            c->stream));
+  CORR_CUDA(cudaMemcpyAsync(dorder, horder, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
+  CORR_CUDA(cudaMemsetAsync(queue, 0, 8, c->stream));
+  if (!c->batch_attrs_set) {
+    CORR_CUDA(prepare_energy_batch());
+    c->batch_attrs_set = true;
+  }
+  int grid = c->sms;
+  if ((long long)grid > total) grid = (int)total;
+  mark(c, 1);
+  CORR_CUDA(launch_energy_batch(dtab, dmaps, n, total, queue, fmt, stages, grid, unit_part,
+                                &c->dres->status, c->stream));
+  mark(c, 2);
+  CORR_CUDA(launch_batch_reduce(dtab, n, unit_part, dorder, out, c->stream));
+  c->launches += 2;
+  return CORR_OK;
+}
+
+int check_batch(corr_context* c, int n, const corr_rimp2_instance* in, int precision) {
+  CORR_CHECK_ARG(c != nullptr, "null context");
+  CORR_CHECK_ARG(n >= 1 && in != nullptr, "batched RI-MP2: need n >= 1 instances");
+  CORR_CHECK_ARG(precision >= CORR_PREC_FP64 && precision <= CORR_PREC_SPLIT_BF16,
+                 "batched RI-MP2: unknown precision %d", precision);
+  for (int k = 0; k < n; ++k) {
+    const corr_rimp2_instance& x = in[k];
+    CORR_CHECK_ARG(x.nocc >= 1 && x.nvir >= 1 && x.naux >= 1, "instance %d: bad sizes", k);
+    CORR_CHECK_ARG(is_device_ptr(x.bia) && is_device_ptr(x.eps),
+                   "instance %d: bia and eps must be device pointers", k);
+  }
+  return CORR_OK;
+}
+
+}  // namespace
+}  // namespace corr
+
+using namespace corr;
+
+extern "C" {
+
+int corr_set_batch_policy(corr_context* c, int order, int stages) {
+  CORR_CHECK_ARG(c != nullptr, "null context");
+  CORR_CHECK_ARG(order == 0 || order == 1, "order policy must be 0 (input) or 1 (cost-descending)");
+  CORR_CHECK_ARG(stages == 3 || stages == 4, "stages must be 3 or 4");
+  c->batch_order = order;
+  c->batch_stages = stages;
+  return CORR_OK;
+}
+
+int corr_rimp2_energy_batched_async(corr_context* c, int n, const corr_rimp2_instance* inst,
+                                    int precision, double* energies_dev) {
+  CORR_TRY(check_batch(c, n, inst, precision));
+  CORR_CHECK_ARG(is_device_ptr(energies_dev), "energies_dev must be a device pointer");
+  CORR_CUDA(cudaSetDevice(c->device));
+  return batch_enqueue(c, n, inst, precision, energies_dev, c->batch_order, c->batch_stages);
+}
+
+int corr_rimp2_energy_batched(corr_context* c, int n, const corr_rimp2_instance* inst,
+                              int precision, corr_mp2_energy* out) {
+  CORR_TRY(check_batch(c, n, inst, precision));
+  CORR_CHECK_ARG(out != nullptr, "null output");
+  CORR_CUDA(cudaSetDevice(c->device));
+  CORR_TRY(c->batch_out.reserve((size_t)n * 32));
+  double* dout = static_cast<double*>(c->batch_out.ptr);
+  CORR_CUDA(cudaMemsetAsync(c->dres, 0, sizeof(ResultBlock), c->stream));
+  mark(c, 0);
+  CORR_TRY(batch_enqueue(c, n, inst, precision, dout, c->batch_order, c->batch_stages));
+  std::vector<double> h((size_t)n * 4);
+  CORR_CUDA(cudaMemcpyAsync(h.data(), dout, (size_t)n * 32, cudaMemcpyDeviceToHost, c->stream));
+  CORR_TRY(finish_results(c, 0));
+  for (int k = 0; k < n; ++k) {
+    out[k].e_ss = h[4 * k];
+    out[k].e_os = h[4 * k + 1];
+    out[k].e_total = h[4 * k + 2];
+    out[k].e_scs = h[4 * k + 3];
+    if (!std::isfinite(out[k].e_total)) {
+      set_error("instance %d: non-finite energy", k);
+      return CORR_ERR_NUMERIC;
+    }
+  }
+  return CORR_OK;
+}
+
+int corr_rimp2_batch_autotune(corr_context* c, int n, const corr_rimp2_instance* inst,
+                              int precision, int* order_out, int* stages_out, float* ms_out) {
+  CORR_TRY(check_batch(c, n, inst, precision));
+  CORR_CUDA(cudaSetDevice(c->device));
+  CORR_TRY(c->batch_out.reserve((size_t)n * 32));
+  double* dout = static_cast<double*>(c->batch_out.ptr);
+  cudaEvent_t e0, e1;
+  CORR_CUDA(cudaEventCreate(&e0));
+  CORR_CUDA(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int bo = c->batch_order, bs = c->batch_stages;
+  const int orders[2] = {0, 1}, stages[2] = {4, 3};
+  for (int oi = 0; oi < 2; ++oi)
+    for (int si = 0; si < 2; ++si) {
+      // one untimed warm-up, then the median of three timed runs
+      CORR_TRY(batch_enqueue(c, n, inst, precision, dout, orders[oi], stages[si]));
+      float t[3];
+      for (int r = 0; r < 3; ++r) {
+        CORR_CUDA(cudaEventRecord(e0, c->stream));
+        CORR_TRY(batch_enqueue(c, n, inst, precision, dout, orders[oi], stages[si]));
+        CORR_CUDA(cudaEventRecord(e1, c->stream));
+        CORR_CUDA(cudaEventSynchronize(e1));
+        CORR_CUDA(cudaEventElapsedTime(&t[r], e0, e1));
+      }
+      std::sort(t, t + 3);
+      if (t[1] < best) {
+        best = t[1];
+        bo = orders[oi];
+        bs = stages[si];
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->batch_order = bo;
+  c->batch_stages = bs;
+  if (order_out) *order_out = bo;
+  if (stages_out) *stages_out = bs;
+  if (ms_out) *ms_out = best;
+  return CORR_OK;
+}
+
+}  // extern "C"

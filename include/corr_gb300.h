@@ -128,6 +128,38 @@ int corr_rimp2_energy_async(corr_context* ctx, int nocc, int nvir, int naux, con
  * CORR_ERR_DEVICE_TIMEOUT); clears it. */
 int corr_sync(corr_context* ctx);
 
+/* ---- batched RI-MP2 (no counterpart in the reference) ------------------- */
+
+/* One independent RI-MP2 problem of a batch; bia [naux][nocc][nvir] and eps
+ * [nocc+nvir] in device memory. */
+typedef struct corr_rimp2_instance {
+  int nocc, nvir, naux;
+  const double* bia;
+  const double* eps;
+} corr_rimp2_instance;
+
+/* Energies of n independent instances of uneven sizes.  The precision forms
+ * run every instance's units through one persistent tcgen05 launch fed by a
+ * device work queue (run_canonical_mp2_ri, src/POSTHF/can_mp2.cc:53, per
+ * instance); the FP64 form runs the fused FP64 kernel per instance.  out[n]. */
+int corr_rimp2_energy_batched(corr_context* ctx, int n, const corr_rimp2_instance* inst,
+                              int precision, corr_mp2_energy* out);
+
+/* Enqueue-only form, energies_dev[4*k+{0,1,2,3}] = {E_SS, E_OS, E, E_SCS} of
+ * instance k.  After a first call with the same batch (which sizes the
+ * workspaces) it can be captured into a CUDA graph. */
+int corr_rimp2_energy_batched_async(corr_context* ctx, int n, const corr_rimp2_instance* inst,
+                                    int precision, double* energies_dev);
+
+/* Launch variant of the batched kernel: unit order (0 = input order,
+ * 1 = costliest instance first) and shared-memory pipeline depth (3 or 4). */
+int corr_set_batch_policy(corr_context* ctx, int order, int stages);
+
+/* Time every launch variant on this batch (median of three runs after a
+ * warm-up), keep the fastest in the context and report it. */
+int corr_rimp2_batch_autotune(corr_context* ctx, int n, const corr_rimp2_instance* inst,
+                              int precision, int* order, int* stages, float* ms);
+
 /* RI-MP2 adjoint (no counterpart in the reference, which has no gradients):
  * dbia[(Q*nocc+i)*nvir+a] = dE/dB^Q_ia and deps[p] = dE/d eps_p for
  * E = E_OS + E_SS of corr_rimp2_energy, in FP64.  The (ia|jb) tiles are

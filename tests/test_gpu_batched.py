@@ -1,0 +1,80 @@
+"""Batched RI-MP2 (config 5 family): many uneven instances in one persistent
+launch fed by a device work queue; against single-instance calls, the FP64
+form and the oracle."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu_instances(sizes, seed):
+    import torch
+
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    items = []
+    for (o, v, X) in sizes:
+        s = 0.05 * torch.exp(-torch.arange(X, device="cuda", dtype=torch.float64) / 400.0)
+        B = torch.randn((X, o, v), generator=g, device="cuda", dtype=torch.float64) * s[:, None, None]
+        eo = torch.sort(torch.rand(o, generator=g, device="cuda", dtype=torch.float64) * 1.2 - 1.5)[0]
+        ev = torch.sort(torch.rand(v, generator=g, device="cuda", dtype=torch.float64) * 2.95 + 0.05)[0]
+        items.append((B.contiguous(), torch.cat([eo, ev]).contiguous(), o, v))
+    return items
+
+
+def test_batched_matches_single_and_oracle(ctx):
+    sizes = [(1, 1, 1), (3, 20, 40), (5, 130, 70), (2, 257, 33), (7, 64, 200), (4, 40, 1000)]
+    items = _gpu_instances(sizes, 7)
+    for prec in ("split_bf16", "fp64"):
+        got = ctx.rimp2_energy_batched(items, prec)
+        for (B, e, o, v), g in zip(items, got):
+            single = ctx.rimp2_energy(B, e, o, v, B.shape[0], prec)
+            assert abs(g.e_total - single.e_total) <= 1e-12 * max(1.0, abs(single.e_total))
+            ref = O.rimp2_energy(B.cpu().numpy(), e.cpu().numpy(), o, v)
+            tol = 1e-12 if prec == "fp64" else 2e-7
+            assert abs(g.e_total - ref[2]) <= max(1e-10, tol * abs(ref[2])), (o, v, prec, g, ref)
+            assert abs(g.e_ss - ref[0]) <= max(1e-10, tol * abs(ref[2]))
+
+
+def test_batched_policies_agree_and_autotune(ctx, tmp_path):
+    sizes = O.synth_batch_sizes(24, 55)
+    sizes = [(o, v, X) for (o, v, X) in sizes if o <= 25]  # keep the test quick
+    items = _gpu_instances(sizes, 8)
+    base = None
+    for order in (0, 1):
+        for stages in (3, 4):
+            ctx.set_batch_policy(order, stages)
+            got = [g.e_total for g in ctx.rimp2_energy_batched(items, "split_bf16")]
+            if base is None:
+                base = got
+            assert got == base  # per-unit partials are reduced in a fixed order
+    cache = str(tmp_path / "autotune.json")
+    o1, s1, ms1 = ctx.batch_autotune(items, "split_bf16", cache=cache)
+    o2, s2, ms2 = ctx.batch_autotune(items, "split_bf16", cache=cache)  # from the cache
+    assert (o1, s1) == (o2, s2) and ms1 == ms2 and ms1 > 0
+
+
+def test_batched_graph_capture(ctx):
+    import torch
+
+    items = _gpu_instances([(6, 50, 90), (9, 70, 180), (3, 30, 64)], 9)
+    out = torch.zeros(4 * len(items), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream)
+    ctx.rimp2_energy_batched_async(items, "split_bf16", out)
+    torch.cuda.synchronize()
+    ref = out.clone()
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    side.wait_stream(stream)
+    out.zero_()
+    with torch.cuda.graph(graph, stream=side):
+        ctx.set_stream(side)
+        ctx.rimp2_energy_batched_async(items, "split_bf16", out)
+    ctx.set_stream(stream)
+    graph.replay()
+    torch.cuda.synchronize()
+    ctx.sync()
+    assert torch.equal(out, ref)
