@@ -271,6 +271,25 @@ class Context:
         check(self._L.corr_calculate_ri(self._h, X, N, _ptr(J), _ptr(pmn), _ptr(out)))
         return out
 
+    def ri_apply_metric(self, jm12, x, out=None):
+        """out = jm12 @ x for x [naux][...] (the metric applied to (P|ia))."""
+        X = jm12.shape[0]
+        ncols = int(x.size // X) if hasattr(x, "size") and not callable(x.size) else int(x.numel() // X)
+        out = self._out(x, tuple(x.shape), out)
+        check(self._L.corr_ri_apply_metric(self._h, X, ncols, _ptr(jm12), _ptr(x), _ptr(out)))
+        return out
+
+    def rimp2_energy_from_3index(self, nroe, mos, eps, J, pmn, precision="split_bf16"):
+        """RI-MP2 energy from (P|mu nu), J, MO coefficients mos[p][mu] and
+        orbital energies, entirely on the GPU.  Returns (MP2Energy, ncut)."""
+        X, N = pmn.shape[0], pmn.shape[1]
+        out = MP2Energy()
+        ncut = ctypes.c_int(0)
+        check(self._L.corr_rimp2_energy_from_3index(self._h, int(nroe), N, X, _ptr(mos), _ptr(eps),
+                                                    _ptr(J), _ptr(pmn), _prec(precision),
+                                                    ctypes.byref(out), ctypes.byref(ncut)))
+        return out, ncut.value
+
 
 _DEFAULT = None
 

@@ -86,6 +86,9 @@ SIGNATURES = {
     "corr_ri_build_bpq": [_vp, _i, _i, _vp, _vp, _vp],
     "corr_ri_metric_inv_sqrt": [_vp, _i, _vp, _d, _vp, ctypes.POINTER(_i)],
     "corr_calculate_ri": [_vp, _i, _i, _vp, _vp, _vp],
+    "corr_ri_apply_metric": [_vp, _i, _ll, _vp, _vp, _vp],
+    "corr_rimp2_energy_from_3index": [_vp, _i, _i, _i, _vp, _vp, _vp, _vp, _i,
+                                      ctypes.POINTER(MP2Energy), ctypes.POINTER(_i)],
 }
 _RESTYPES = {"corr_version": ctypes.c_char_p, "corr_last_error": ctypes.c_char_p}
 

@@ -291,55 +291,53 @@ int corr_rimp2_energy(corr_context* c, int nocc, int nvir, int naux, const doubl
 
 namespace corr {
 
-// Enqueue the whole energy evaluation on the context stream; results land in
-// c->dres.  Shared by the public entry point and the batched driver.
-int rimp2_energy_device(corr_context* c, int nocc, int nvir, int naux, const double* bia,
-                        const double* eps, int precision, double* res) {
-  double* out_e = res ? res : c->dres->e;
-  const size_t nb = (size_t)naux * nocc * nvir;
-  const size_t ne = (size_t)nocc + nvir;
-  const bool b_dev = is_device_ptr(bia), e_dev = is_device_ptr(eps);
-  const int Qp = ((naux + 31) / 32) * 32;
-  const EnergyShape sh =
-      make_energy_shape(nocc, nvir, naux, precision == CORR_PREC_FP64 ? kF64Tile : kTcTile);
-  int grid = precision == CORR_PREC_FP64 ? c->sms * 2 : c->sms;
-  if ((long long)grid > sh.nunits) grid = (int)sh.nunits;
-
+// Scratch of the energy stage for device-resident B and eps.
+static void energy_carve(Carver& w, int nocc, int nvir, int Qp, bool tc, int grid, SliceWork* sw,
+                         double** partials) {
   const long long R = (long long)nocc * nvir;
+  if (tc) {
+    sw->S = static_cast<uint16_t*>(w.take((size_t)3 * R * Qp * 2));
+    sw->erow = static_cast<int*>(w.take((size_t)R * 4));
+    sw->diag = static_cast<double*>(w.take((size_t)R * 8));
+    sw->sc = static_cast<float*>(w.take((size_t)R * 4));
+    sw->dg = static_cast<float*>(w.take((size_t)R * 4));
+    sw->eref = static_cast<int*>(w.take(16));
+    sw->scale = static_cast<double*>(w.take(16));
+  }
+  *partials = static_cast<double*>(w.take((size_t)grid * 16));
+}
+
+static int energy_grid(corr_context* c, const EnergyShape& sh, bool tc) {
+  int grid = tc ? c->sms : c->sms * 2;
+  if ((long long)grid > sh.nunits) grid = (int)sh.nunits;
+  return grid;
+}
+
+size_t energy_scratch_bytes(corr_context* c, int nocc, int nvir, int naux, int precision) {
   const bool tc = precision != CORR_PREC_FP64;
-  // size the workspace (same carving order twice: size pass, then real pass)
-  auto carve = [&](Carver& w, void** b_slot, void** e_slot, SliceWork* sw, double** partials) {
-    *b_slot = b_dev ? nullptr : w.take(nb * 8);
-    *e_slot = e_dev ? nullptr : w.take(ne * 8);
-    if (tc) {
-      sw->S = static_cast<uint16_t*>(w.take((size_t)3 * R * Qp * 2));
-      sw->erow = static_cast<int*>(w.take((size_t)R * 4));
-      sw->diag = static_cast<double*>(w.take((size_t)R * 8));
-      sw->sc = static_cast<float*>(w.take((size_t)R * 4));
-      sw->dg = static_cast<float*>(w.take((size_t)R * 4));
-      sw->eref = static_cast<int*>(w.take(16));
-      sw->scale = static_cast<double*>(w.take(16));
-    }
-    *partials = static_cast<double*>(w.take((size_t)grid * 16));
-  };
-  void *b_slot, *e_slot;
+  const int Qp = ((naux + 31) / 32) * 32;
+  const EnergyShape sh = make_energy_shape(nocc, nvir, naux, tc ? kTcTile : kF64Tile);
+  SliceWork sw{};
+  double* part;
+  Carver cv{nullptr, 0};
+  energy_carve(cv, nocc, nvir, Qp, tc, energy_grid(c, sh, tc), &sw, &part);
+  return cv.used + 256;
+}
+
+// Enqueue the energy of device-resident B/eps, carving scratch from `w`
+// (which must already be backed by reserved workspace); results to `res`
+// (device, 4 doubles; NULL = the context's result block).
+int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, const double* d_b,
+                      const double* d_e, int precision, double* res) {
+  double* out_e = res ? res : c->dres->e;
+  const bool tc = precision != CORR_PREC_FP64;
+  const int Qp = ((naux + 31) / 32) * 32;
+  const long long R = (long long)nocc * nvir;
+  const EnergyShape sh = make_energy_shape(nocc, nvir, naux, tc ? kTcTile : kF64Tile);
+  const int grid = energy_grid(c, sh, tc);
   SliceWork sw{};
   double* partials;
-  Carver cv{nullptr, 0};
-  carve(cv, &b_slot, &e_slot, &sw, &partials);
-  CORR_TRY(c->ws.reserve(cv.used));
-  Carver w{c->ws.ptr, 0};
-  carve(w, &b_slot, &e_slot, &sw, &partials);
-
-  mark(c, 0);
-  const double* d_b = static_cast<const double*>(stage_in(c, bia, nb * 8, b_slot));
-  const double* d_e = static_cast<const double*>(stage_in(c, eps, ne * 8, e_slot));
-  if (!d_b || !d_e) {
-    set_error("host-to-device copy failed: %s", cudaGetErrorString(cudaGetLastError()));
-    return CORR_ERR_CUDA;
-  }
-  if (!res) CORR_CUDA(cudaMemsetAsync(c->dres, 0, sizeof(ResultBlock), c->stream));
-
+  energy_carve(w, nocc, nvir, Qp, tc, grid, &sw, &partials);
   if (!tc) {
     mark(c, 1);
     CORR_CUDA(launch_energy_fp64(d_b, d_e, sh, partials, grid, c->stream));
@@ -358,17 +356,43 @@ int rimp2_energy_device(corr_context* c, int nocc, int nvir, int naux, const dou
   const CUtensorMapDataType dt =
       fmt == 0 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
   CORR_TRY(encode_tmap(&tm, dt, 3, sw.S, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_64B));
-  mark(c, 1);
   if (!c->attrs_set) {
     CORR_CUDA(prepare_energy_tc());
     c->attrs_set = true;
   }
+  mark(c, 1);
   CORR_CUDA(launch_energy_tc(tm, d_e, sw.sc, sw.dg, sh, Qp, fmt, p, partials, grid,
                              &c->dres->status, c->stream));
   mark(c, 2);
   CORR_CUDA(launch_energy_reduce(partials, grid, sw.scale, out_e, c->stream));
   c->launches += 5;  // rowstat, slice, rowfactor, energy, reduce
   return CORR_OK;
+}
+
+// Enqueue the whole energy evaluation on the context stream (host or device
+// inputs); results land in `res` or the context's result block.
+int rimp2_energy_device(corr_context* c, int nocc, int nvir, int naux, const double* bia,
+                        const double* eps, int precision, double* res) {
+  const size_t nb = (size_t)naux * nocc * nvir;
+  const size_t ne = (size_t)nocc + nvir;
+  const bool b_dev = is_device_ptr(bia), e_dev = is_device_ptr(eps);
+  Carver cv{nullptr, 0};
+  if (!b_dev) cv.take(nb * 8);
+  if (!e_dev) cv.take(ne * 8);
+  const size_t head = cv.used;
+  CORR_TRY(c->ws.reserve(head + energy_scratch_bytes(c, nocc, nvir, naux, precision)));
+  Carver w{c->ws.ptr, 0};
+  void* b_slot = b_dev ? nullptr : w.take(nb * 8);
+  void* e_slot = e_dev ? nullptr : w.take(ne * 8);
+  if (!res) CORR_CUDA(cudaMemsetAsync(c->dres, 0, sizeof(ResultBlock), c->stream));
+  mark(c, 0);
+  const double* d_b = static_cast<const double*>(stage_in(c, bia, nb * 8, b_slot));
+  const double* d_e = static_cast<const double*>(stage_in(c, eps, ne * 8, e_slot));
+  if (!d_b || !d_e) {
+    set_error("host-to-device copy failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return CORR_ERR_CUDA;
+  }
+  return rimp2_energy_core(c, w, nocc, nvir, naux, d_b, d_e, precision, res);
 }
 
 }  // namespace corr

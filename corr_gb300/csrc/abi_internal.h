@@ -67,4 +67,9 @@ void mark(corr_context* c, int k);
 // the context's result block).
 int rimp2_energy_device(corr_context* c, int nocc, int nvir, int naux, const double* bia,
                         const double* eps, int precision, double* res = nullptr);
+// Scratch bytes of the energy stage, and the stage itself on device-resident
+// inputs, carving from `w` (already backed by reserved workspace).
+size_t energy_scratch_bytes(corr_context* c, int nocc, int nvir, int naux, int precision);
+int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, const double* d_b,
+                      const double* d_e, int precision, double* res);
 }  // namespace corr

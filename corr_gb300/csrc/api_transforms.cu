@@ -378,3 +378,105 @@ int corr_calculate_ri(corr_context* c, int naux, int nroao, const double* J, con
 }
 
 }  // extern "C"
+
+extern "C" {
+
+int corr_ri_apply_metric(corr_context* c, int naux, long long ncols, const double* jm12,
+                         const double* in, double* out) {
+  CORR_CHECK_ARG(c && jm12 && in && out, "corr_ri_apply_metric: null argument");
+  CORR_CHECK_ARG(naux >= 1 && ncols >= 1 && ncols <= 0x7fffffffLL,
+                 "corr_ri_apply_metric: bad sizes");
+  CORR_CUDA(cudaSetDevice(c->device));
+  const size_t nj = (size_t)naux * naux, nx = (size_t)naux * ncols;
+  const bool jdev = is_device_ptr(jm12), idev = is_device_ptr(in), odev = is_device_ptr(out);
+  Carver cv{nullptr, 0};
+  if (!jdev) cv.take(nj * 8);
+  if (!idev) cv.take(nx * 8);
+  if (!odev) cv.take(nx * 8);
+  CORR_TRY(c->ws.reserve(cv.used));
+  Carver w{c->ws.ptr, 0};
+  void* s_j = jdev ? nullptr : w.take(nj * 8);
+  void* s_i = idev ? nullptr : w.take(nx * 8);
+  double* o = odev ? out : static_cast<double*>(w.take(nx * 8));
+  CORR_CUDA(cudaMemsetAsync(c->dres, 0, sizeof(ResultBlock), c->stream));
+  mark(c, 0);
+  const double* d_j = static_cast<const double*>(stage_in(c, jm12, nj * 8, s_j));
+  const double* d_i = static_cast<const double*>(stage_in(c, in, nx * 8, s_i));
+  CORR_CHECK_ARG(d_j && d_i, "host-to-device copy failed");
+  mark(c, 1);
+  CORR_TRY(gemm_f64(gemm_args(d_j, d_i, o, naux, (int)ncols, naux, naux, ncols, ncols, 0, 0),
+                    &c->dres->status, c->stream));
+  c->launches += 1;
+  mark(c, 2);
+  CORR_TRY(stage_out(c, out, o, nx * 8));
+  return finish_results(c, 0);
+}
+
+int corr_rimp2_energy_from_3index(corr_context* c, int nroe, int nroao, int naux,
+                                  const double* mos, const double* eps, const double* J,
+                                  const double* pmn, int precision, corr_mp2_energy* out,
+                                  int* ncut) {
+  CORR_CHECK_ARG(c && mos && eps && J && pmn && out, "corr_rimp2_energy_from_3index: null argument");
+  CORR_CHECK_ARG(nroao >= 1 && naux >= 1 && naux <= 32768 && nroe >= 2 && nroe % 2 == 0 &&
+                     nroe / 2 < nroao,
+                 "corr_rimp2_energy_from_3index: bad sizes");
+  CORR_CHECK_ARG(precision >= CORR_PREC_FP64 && precision <= CORR_PREC_SPLIT_BF16,
+                 "corr_rimp2_energy_from_3index: unknown precision %d", precision);
+  CORR_CUDA(cudaSetDevice(c->device));
+  const int N = nroao, o = nroe / 2, v = N - o, X = naux;
+  const size_t np = (size_t)X * N * N, nia = (size_t)X * o * v, nbiq = (size_t)X * o * N,
+               nj = (size_t)X * X;
+  const bool mdev = is_device_ptr(mos), edev = is_device_ptr(eps), jdev = is_device_ptr(J),
+             pdev = is_device_ptr(pmn);
+  // Region 1 (persistent across the stages): staged inputs, (P|ia), B, J^-1/2.
+  auto plan = [&](Carver& w, void** sm, void** se, void** sj, void** sp, double** pia,
+                  double** bia, double** jm, double** biq, void** jws) {
+    *sm = mdev ? nullptr : w.take((size_t)N * N * 8);
+    *se = edev ? nullptr : w.take((size_t)N * 8);
+    *sj = jdev ? nullptr : w.take(nj * 8);
+    *sp = pdev ? nullptr : w.take(np * 8);
+    *pia = static_cast<double*>(w.take(nia * 8));
+    *bia = static_cast<double*>(w.take(nia * 8));
+    *jm = static_cast<double*>(w.take(nj * 8));
+    *biq = static_cast<double*>(w.take(nbiq * 8));
+    *jws = w.take(jacobi_workspace_bytes(X));
+  };
+  void *sm, *se, *sj, *sp, *jws;
+  double *pia, *bia, *jm, *biq;
+  Carver cv{nullptr, 0};
+  plan(cv, &sm, &se, &sj, &sp, &pia, &bia, &jm, &biq, &jws);
+  CORR_TRY(c->ws.reserve(cv.used + energy_scratch_bytes(c, o, v, X, precision)));
+  Carver w{c->ws.ptr, 0};
+  plan(w, &sm, &se, &sj, &sp, &pia, &bia, &jm, &biq, &jws);
+  CORR_CUDA(cudaMemsetAsync(c->dres, 0, sizeof(ResultBlock), c->stream));
+  mark(c, 0);
+  const double* d_m = static_cast<const double*>(stage_in(c, mos, (size_t)N * N * 8, sm));
+  const double* d_e = static_cast<const double*>(stage_in(c, eps, (size_t)N * 8, se));
+  const double* d_j = static_cast<const double*>(stage_in(c, J, nj * 8, sj));
+  const double* d_p = static_cast<const double*>(stage_in(c, pmn, np * 8, sp));
+  CORR_CHECK_ARG(d_m && d_e && d_j && d_p, "host-to-device copy failed");
+  // (P|ia) = C_occ (P|mu nu) C_vir^T  (the transform_ri contractions, ri.cc:147-172)
+  GemmF64 g1 = gemm_args(d_m, d_p, biq, o, N, N, N, N, N, 0, 0);
+  g1.sb = (long long)N * N;
+  g1.sc = (long long)o * N;
+  g1.batch = X;
+  CORR_TRY(gemm_f64(g1, &c->dres->status, c->stream));
+  CORR_TRY(gemm_f64(gemm_args(biq, d_m + (size_t)o * N, pia, X * o, v, N, N, N, v, 0, 1),
+                    &c->dres->status, c->stream));
+  // J^-1/2 (ri.cc:50-69), applied to the (P|ia) matrix: 2 X^2 o v flops instead of 2 X^2 N^2
+  CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, X, 1e-10, jm, ncut));
+  CORR_TRY(gemm_f64(gemm_args(jm, pia, bia, X, o * v, X, X, (long long)o * v, (long long)o * v,
+                              0, 0),
+                    &c->dres->status, c->stream));
+  c->launches += 3;
+  // energy on the device-resident B; its scratch is carved after region 1
+  CORR_TRY(rimp2_energy_core(c, w, o, v, X, bia, d_e, precision, nullptr));
+  CORR_TRY(finish_results(c, 4));
+  out->e_ss = c->hres->e[0];
+  out->e_os = c->hres->e[1];
+  out->e_total = c->hres->e[2];
+  out->e_scs = c->hres->e[3];
+  return CORR_OK;
+}
+
+}  // extern "C"

@@ -253,6 +253,24 @@ int corr_ri_metric_inv_sqrt(corr_context* ctx, int naux, const double* J, double
 int corr_calculate_ri(corr_context* ctx, int naux, int nroao, const double* J, const double* pmn,
                       double* bpq);
 
+/* out[P][k] = sum_Q jm12[P][Q] in[Q][k] for k < ncols: the metric step of
+ * ri.cc:102-103 applied after the MO transform, on (P|ia) (ncols = nocc*nvir)
+ * instead of (P|mu nu) -- 2 naux^2 nocc nvir flops instead of 2 naux^2 N^2.
+ * No reference counterpart (the reference applies J^-1/2 in the AO basis). */
+int corr_ri_apply_metric(corr_context* ctx, int naux, long long ncols, const double* jm12,
+                         const double* in, double* out);
+
+/* The RI-MP2 energy from integrals, all on the GPU: (P|ia) from
+ * pmn[P][mu][nu] = (P|mu nu) and the MO coefficients (the contractions of
+ * transform_ri, ri.cc:147-172), J^-1/2 with the reference's cutoff
+ * (ri.cc:50-69), B = J^-1/2 (P|ia), and the energy of run_canonical_mp2_ri
+ * (can_mp2.cc:53) in `precision`.  Equals calculate_ri + transform_ri +
+ * run_canonical_mp2_ri whenever no eigenvalue is cut. *ncut optional. */
+int corr_rimp2_energy_from_3index(corr_context* ctx, int nroe, int nroao, int naux,
+                                  const double* mos, const double* eps, const double* J,
+                                  const double* pmn, int precision, corr_mp2_energy* out,
+                                  int* ncut);
+
 #ifdef __cplusplus
 }
 #endif

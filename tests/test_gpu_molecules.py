@@ -1,0 +1,85 @@
+"""The molecular workloads on the GPU against the reference's own outputs.
+
+config 1 -- H2O / def2-SVP (N = 24, nocc = 5): MOtrans + canonical MP2 and
+  calculate_ri + transform_ri + RI-MP2 must match the reference's energies on
+  the same orbitals to 1e-10 Eh; the precision form within 1 uEh.
+config 3 -- 20 H2O / def2-SVP / def2-SVP-RI (N = 480, nocc = 100, naux = 1520):
+  the FP64 GPU RI pipeline must match the reference's calculate_ri,
+  transform_ri and run_canonical_mp2_ri to 1e-9 Eh, and the precision form the
+  FP64 form within 1 uEh.
+"""
+import json
+import os
+import time
+
+import numpy as np
+import pytest
+
+from oracle import molecule as M
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+with open(os.path.join(HERE, "golden", "golden_molecules.json")) as _f:
+    GOLD = json.load(_f)
+
+
+def test_config1_h2o(ctx):
+    g = GOLD["config1"]
+    fx = np.load(os.path.join(HERE, "golden", "config1_h2o.npz"))
+    mos, fmat = fx["mos"], fx["fmat"]
+    I = M.Integrals(M.water(), "def2-svp", "def2-svp-ri")
+    pk = O.pack_eri(I.eri())
+    assert pk.nrofint == g["nrofint"] and [int(x) for x in pk.sortcount] == g["sortcount"]
+    fmo = ctx.build_fmo(mos, fmat)
+    eps = np.diag(fmo).copy()
+    prec = ctx.motrans(10, mos, pk)
+    can = ctx.canonical_mp2(10, prec, eps)
+    for a, b in zip(can.as_tuple(), g["canonical_mp2"]):
+        assert abs(a - b) <= 1e-10, (can, g["canonical_mp2"])
+    J, P3 = I.metric(), I.three_center()
+    bia = ctx.transform_ri(10, mos, ctx.calculate_ri(J, P3))
+    ri = ctx.rimp2_energy(bia, eps, 5, 19, 76, "fp64")
+    for a, b in zip(ri.as_tuple(), g["ri_mp2"]):
+        assert abs(a - b) <= 1e-10, (ri, g["ri_mp2"])
+    for prec_form in ("split_bf16", "split_fp16"):
+        sp = ctx.rimp2_energy(bia, eps, 5, 19, 76, prec_form)
+        assert abs(sp.e_total - g["ri_mp2"][2]) <= 1e-6
+    e3, ncut = ctx.rimp2_energy_from_3index(10, mos, eps, J, P3, "fp64")
+    assert ncut == 0
+    assert abs(e3.e_total - g["ri_mp2"][2]) <= 1e-10
+
+
+def test_config3_water_cluster(ctx):
+    g = GOLD.get("config3")
+    if g is None:
+        pytest.skip("config 3 fixture not generated")
+    fx = np.load(os.path.join(HERE, "golden", "config3_cluster.npz"))
+    mos, eps = fx["mos"], fx["eps"]
+    I = M.Integrals(M.water_cluster(20, box=g["box"], min_oo=g["min_oo"], seed=g["seed"]),
+                    "def2-svp", "def2-svp-ri")
+    J, P3 = I.metric(), I.three_center()
+    for name, arr in (("J", J), ("P3", P3)):
+        assert np.allclose([arr.sum(), (arr * arr).sum()], g["checksums"][name], rtol=1e-11), name
+    import torch
+
+    Jd = torch.from_numpy(J).cuda()
+    Pd = torch.from_numpy(P3).cuda()
+    md = torch.from_numpy(mos).cuda()
+    ed = torch.from_numpy(eps).cuda()
+    e64, ncut = ctx.rimp2_energy_from_3index(200, md, ed, Jd, Pd, "fp64")
+    assert ncut == g["ncut"]
+    ref = g["ri_mp2"]
+    assert abs(e64.e_total - ref[2]) <= 1e-9, (e64, ref)
+    assert abs(e64.e_ss - ref[0]) <= 1e-9 and abs(e64.e_os - ref[1]) <= 1e-9
+    esp, _ = ctx.rimp2_energy_from_3index(200, md, ed, Jd, Pd, "split_bf16")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    esp2, _ = ctx.rimp2_energy_from_3index(200, md, ed, Jd, Pd, "split_bf16")
+    t_split = time.perf_counter() - t0
+    assert esp2.e_total == esp.e_total  # fixed-order reductions: reproducible
+    # the spec bar: precision form within 1 uEh of FP64
+    assert abs(esp.e_total - e64.e_total) <= 1e-6, (esp, e64)
+    print(f"config3 time-to-E_corr from integrals (split_bf16): {t_split * 1e3:.1f} ms, "
+          f"|dE| = {abs(esp.e_total - e64.e_total):.3e} Eh")
