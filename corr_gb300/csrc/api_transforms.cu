@@ -304,6 +304,12 @@ int corr_ri_build_bpq(corr_context* c, int naux, int nroao, const double* jm12,
 
 namespace corr {
 size_t jacobi_workspace_bytes(int m);
+size_t chol_workspace_bytes(int m);
+int chol_norm_inf(corr_context* c, void* scratch, const double* J, int m, double* out);
+int chol_factor_device(corr_context* c, void* ws, const double* J, int m, double shift,
+                       double** Lm_out, double** Linv_out, bool* ok);
+int chol_solve_device(corr_context* c, const double* Lm, const double* Linv, int m, double* P,
+                      long long ncols, double* out);
 int ri_inv_sqrt_device(corr_context* c, void* ws, const double* J, int m, double tol,
                        double* out, int* ncut);
 }  // namespace corr
@@ -439,7 +445,8 @@ int corr_rimp2_energy_from_3index(corr_context* c, int nroe, int nroao, int naux
     *bia = static_cast<double*>(w.take(nia * 8));
     *jm = static_cast<double*>(w.take(nj * 8));
     *biq = static_cast<double*>(w.take(nbiq * 8));
-    *jws = w.take(jacobi_workspace_bytes(X));
+    // the eigendecomposition and the Cholesky path run one after the other
+    *jws = w.take(std::max(jacobi_workspace_bytes(X), chol_workspace_bytes(X)));
   };
   void *sm, *se, *sj, *sp, *jws;
   double *pia, *bia, *jm, *biq;
@@ -463,12 +470,31 @@ int corr_rimp2_energy_from_3index(corr_context* c, int nroe, int nroao, int naux
   CORR_TRY(gemm_f64(g1, &c->dres->status, c->stream));
   CORR_TRY(gemm_f64(gemm_args(biq, d_m + (size_t)o * N, pia, X * o, v, N, N, N, v, 0, 1),
                     &c->dres->status, c->stream));
-  // J^-1/2 (ri.cc:50-69), applied to the (P|ia) matrix: 2 X^2 o v flops instead of 2 X^2 N^2
-  CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, X, 1e-10, jm, ncut));
-  CORR_TRY(gemm_f64(gemm_args(jm, pia, bia, X, o * v, X, X, (long long)o * v, (long long)o * v,
-                              0, 0),
-                    &c->dres->status, c->stream));
-  c->launches += 3;
+  // The metric.  The energy sees J only through J^-1 = W^T W: when the
+  // reference's cutoff (ri.cc:56-66, lambda/lambda_max < 1e-10) provably cuts
+  // nothing -- J - 10 tol ||J||_inf I is positive definite -- W = L^-1 from a
+  // Cholesky factorisation (chol.cu); otherwise W = J^-1/2 with the cutoff
+  // (ri.cc:50-69), applied to the (P|ia) matrix (2 X^2 o v flops).
+  const double tol = 1e-10;
+  double jnorm = 0.0;
+  CORR_TRY(chol_norm_inf(c, jm, d_j, X, &jnorm));
+  double *Lm = nullptr, *Linv = nullptr;
+  bool certified = false;
+  if (jnorm > 0.0) CORR_TRY(chol_factor_device(c, jws, d_j, X, 10.0 * tol * jnorm, &Lm, &Linv,
+                                               &certified));
+  bool factored = false;
+  if (certified) CORR_TRY(chol_factor_device(c, jws, d_j, X, 0.0, &Lm, &Linv, &factored));
+  if (factored) {
+    CORR_TRY(chol_solve_device(c, Lm, Linv, X, pia, (long long)o * v, bia));
+    if (ncut) *ncut = 0;
+  } else {
+    CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, X, tol, jm, ncut));
+    CORR_TRY(gemm_f64(gemm_args(jm, pia, bia, X, o * v, X, X, (long long)o * v,
+                                (long long)o * v, 0, 0),
+                      &c->dres->status, c->stream));
+    c->launches += 1;
+  }
+  c->launches += 2;
   // energy on the device-resident B; its scratch is carved after region 1
   CORR_TRY(rimp2_energy_core(c, w, o, v, X, bia, d_e, precision, nullptr));
   CORR_TRY(finish_results(c, 4));

@@ -10,9 +10,11 @@
 //   c = 1/sqrt(1 + t^2),  s = t c,   R = [[c, s], [-s, c]],
 //   A <- R^T A R (one 2x2 block per thread, in place),  V <- V R,
 // and a sweep is n-1 rounds of the circle pairing (index n-1 fixed, index r
-// paired with it, (r+k) mod (n-1) with (r-k) mod (n-1)).  Sweeps repeat until
-// the off-diagonal Frobenius mass falls below (1e-15)^2 of the total.  The
-// cutoff and the assembly V f(Lambda) V^T (gemm_fp64.cu) follow the reference.
+// paired with it, (r+k) mod (n-1) with (r-k) mod (n-1)).  A pair is rotated
+// only while |a_pq| > 1e-15 sqrt(|a_pp a_qq|) (the threshold rule of Demmel &
+// Veselic, "Jacobi's method is more accurate than QR", 1992), and sweeps repeat
+// until one sweep rotates no pair (at most 40).  The cutoff and the assembly
+// V f(Lambda) V^T (gemm_fp64.cu) follow the reference.
 #include <cmath>
 #include <vector>
 
@@ -34,14 +36,18 @@ __device__ __forceinline__ void round_pair(int n, int r, int k, int* p, int* q) 
   }
 }
 
-__global__ void jacobi_params(const double* __restrict__ A, int n, int r, double2* __restrict__ cs) {
+constexpr double kRotTol = 1e-15;
+
+__global__ void jacobi_params(const double* __restrict__ A, int n, int r, double2* __restrict__ cs,
+                              int* __restrict__ rotated) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n / 2) return;
   int p, q;
   round_pair(n, r, k, &p, &q);
   const double app = A[(size_t)p * n + p], aqq = A[(size_t)q * n + q], apq = A[(size_t)p * n + q];
   double c = 1.0, s = 0.0;
-  if (apq != 0.0) {
+  if (fabs(apq) > kRotTol * sqrt(fabs(app * aqq))) {
+    *rotated = 1;
     const double tau = (aqq - app) / (2.0 * apq);
     const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
     c = 1.0 / sqrt(1.0 + t * t);
@@ -171,32 +177,32 @@ int ri_inv_sqrt_device(corr_context* c, void* ws, const double* J, int m, double
   CORR_CUDA(cudaGetLastError());
   c->launches += 1;
   std::vector<double> hp((size_t)fgrid * 2);
+  frob_kernel<<<fgrid, 256, 0, s>>>(A, n, part);
+  CORR_CUDA(cudaMemcpyAsync(hp.data(), part, hp.size() * 8, cudaMemcpyDeviceToHost, s));
+  CORR_CUDA(cudaStreamSynchronize(s));
+  c->launches += 1;
+  double tot = 0;
+  for (int k = 0; k < fgrid; ++k) tot += hp[2 * k + 1];
+  if (!(tot > 0.0)) {
+    set_error("RI metric is zero");
+    return CORR_ERR_NOT_PD;
+  }
+  int* rotated = reinterpret_cast<int*>(part);
   const int h = n / 2;
   const long long napply = (long long)h * h + (long long)n * h;
   const int agrid = (int)((napply + 255) / 256);
-  double off = 0, tot = 0;
-  int sweeps = 0;
-  for (; sweeps < 40; ++sweeps) {
-    frob_kernel<<<fgrid, 256, 0, s>>>(A, n, part);
-    CORR_CUDA(cudaMemcpyAsync(hp.data(), part, hp.size() * 8, cudaMemcpyDeviceToHost, s));
-    CORR_CUDA(cudaStreamSynchronize(s));
-    off = tot = 0;
-    for (int k = 0; k < fgrid; ++k) {
-      off += hp[2 * k];
-      tot += hp[2 * k + 1];
-    }
-    c->launches += 1;
-    if (!(tot > 0.0) || off <= 1e-30 * tot || n < 2) break;
+  for (int sweeps = 0; sweeps < 40 && n >= 2; ++sweeps) {
+    CORR_CUDA(cudaMemsetAsync(rotated, 0, sizeof(int), s));
     for (int r = 0; r < n - 1; ++r) {
-      jacobi_params<<<(h + 127) / 128, 128, 0, s>>>(A, n, r, cs);
+      jacobi_params<<<(h + 127) / 128, 128, 0, s>>>(A, n, r, cs, rotated);
       jacobi_apply<<<agrid, 256, 0, s>>>(A, V, n, r, cs);
     }
     CORR_CUDA(cudaGetLastError());
     c->launches += 2LL * (n - 1);
-  }
-  if (!(tot > 0.0)) {
-    set_error("RI metric is zero");
-    return CORR_ERR_NOT_PD;
+    int hrot = 0;
+    CORR_CUDA(cudaMemcpyAsync(&hrot, rotated, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CORR_CUDA(cudaStreamSynchronize(s));
+    if (!hrot) break;
   }
   // eigenvalues -> reference cutoff (ri.cc:56-66) on the host (m values)
   double* dlam = W;  // reuse W's head as a scratch vector before W is written

@@ -73,3 +73,63 @@ def test_not_positive_definite_is_an_error(ctx):
     with pytest.raises(corr_gb300.CorrError) as ei:
         ctx.ri_metric_inv_sqrt(-np.eye(5))
     assert ei.value.status == 3  # CORR_ERR_NOT_PD
+
+
+def _from_3index_case(X, N, nocc, seed, spectrum=None):
+    r = O.rng(seed)
+    if spectrum is None:
+        L = r.standard_normal((X, X)) / np.sqrt(X)
+        J = L @ L.T + 0.5 * np.eye(X)
+    else:
+        Q, _ = np.linalg.qr(r.standard_normal((X, X)))
+        J = (Q * spectrum) @ Q.T
+        J = 0.5 * (J + J.T)
+    P3 = r.standard_normal((X, N, N)) * 0.1
+    P3 = 0.5 * (P3 + P3.transpose(0, 2, 1))
+    mos = O.synth_orbitals(N, seed + 1)
+    eps = np.concatenate([np.sort(r.uniform(-1.5, -0.3, nocc)),
+                          np.sort(r.uniform(0.05, 3.0, N - nocc))])
+    return J, P3, mos, eps
+
+
+def _oracle_from_3index(J, P3, mos, eps, nocc):
+    N = mos.shape[0]
+    jm, ncut = O.ri_metric_inv_sqrt(J)
+    pia = np.einsum("im,Qmn,an->Qia", mos[:nocc], P3, mos[nocc:], optimize=True)
+    B = (jm @ pia.reshape(J.shape[0], -1)).reshape(J.shape[0], nocc, N - nocc)
+    return O.rimp2_energy(B, eps, nocc, N - nocc), ncut
+
+
+@pytest.mark.parametrize("kind", ["certified", "rank_deficient", "near_cutoff"])
+def test_from_3index_metric_paths(ctx, kind):
+    """Energy from (P|mn) and J: a certified metric takes the Cholesky path
+    (chol.cu), a metric with eigenvalues at or below 10 tol lambda_max takes
+    the eigendecomposition with the reference's cutoff.  Both must give the
+    reference energy."""
+    X, N, nocc = 96, 22, 5
+    spec = None
+    if kind == "rank_deficient":
+        spec = np.concatenate([np.geomspace(1.0, 1e-3, 80), np.zeros(16)])
+    elif kind == "near_cutoff":
+        # smallest eigenvalue 5e-10 lambda_max: kept by the reference's cutoff,
+        # below the certificate's 10 tol ||J||_inf
+        spec = np.concatenate([np.geomspace(1.0, 1e-4, 95), [5e-10]])
+    J, P3, mos, eps = _from_3index_case(X, N, nocc, 71, spec)
+    (ess, eos, et), ncut_ref = _oracle_from_3index(J, P3, mos, eps, nocc)
+    e, ncut = ctx.rimp2_energy_from_3index(2 * nocc, mos, eps, J, P3, "fp64")
+    assert ncut == ncut_ref
+    if kind == "rank_deficient":
+        assert ncut == 16
+    tol = {"certified": 1e-10, "rank_deficient": 1e-8, "near_cutoff": 1e-6}[kind]
+    assert abs(e.e_total - et) <= tol * abs(et), (e, et)
+    assert abs(e.e_os - eos) <= tol * abs(eos)
+
+
+@pytest.mark.parametrize("X,N,nocc", [(64, 16, 3), (200, 30, 7), (650, 40, 9)])
+def test_from_3index_cholesky_sizes(ctx, X, N, nocc):
+    """Certified metrics of sizes around the 64-row block edges."""
+    J, P3, mos, eps = _from_3index_case(X, N, nocc, X + N)
+    (ess, eos, et), ncut_ref = _oracle_from_3index(J, P3, mos, eps, nocc)
+    e, ncut = ctx.rimp2_energy_from_3index(2 * nocc, mos, eps, J, P3, "fp64")
+    assert ncut == ncut_ref == 0
+    assert abs(e.e_total - et) <= 1e-10 * abs(et)
