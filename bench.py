@@ -9,7 +9,7 @@ and the FP64 reduction.  Throughput is the algorithmic count
 F = 2 nocc^2 nvir^2 naux per step (the reference's full-(i,j) count,
 src/POSTHF/can_mp2.cc:82-88) over the device time.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision split_bf16]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision split_fp16]
   python bench.py --impl reference ...   # the reference's CPU path on host cores
 
 With N > 1 (torchrun, one rank per GPU) every rank runs an independent replica
@@ -45,8 +45,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="split_bf16",
-                    choices=["split_bf16", "split_fp16", "fp64"])
+    ap.add_argument("--precision", default="split_fp16",
+                    choices=["split_fp16", "split_bf16", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="rimp2", choices=["rimp2", "batch256"],
                     help="batch256: 256 uneven RI-MP2 instances in one batched launch")
@@ -326,6 +326,15 @@ def run_ours(args):
         e_split = ctx.rimp2_energy(Bd, ed, NOCC, NVIR, NAUX, prec)
         kern_ms.append(ctx.timing().kernel_ms)
 
+    # ---- the other precision form (same job, library device timing)
+    alt = "split_bf16" if prec != "split_bf16" else "split_fp16"
+    e_alt = ctx.rimp2_energy(Bd, ed, NOCC, NVIR, NAUX, alt)
+    alt_ms = []
+    for _ in range(5):
+        flush.fill_(1)
+        e_alt = ctx.rimp2_energy(Bd, ed, NOCC, NVIR, NAUX, alt)
+        alt_ms.append(ctx.timing().total_ms)
+
     # ---- FP64 GPU form of the same job (the comparison form)
     ctx.rimp2_energy(Bd, ed, NOCC, NVIR, NAUX, "fp64")
     f64_ms = []
@@ -390,6 +399,10 @@ def run_ours(args):
                    "host_api_matches": e_host.e_total == e_split.e_total},
         "fp64_form": {"ms_per_step": f64, "tflops": FLOPS / (f64 * 1e-3) / 1e12,
                       "split_speedup": f64 / ms_step},
+        "other_split_form": {"precision": alt, "device_ms": statistics.median(alt_ms),
+                             "tflops": FLOPS / (statistics.median(alt_ms) * 1e-3) / 1e12,
+                             "rel_err_vs_fp64": abs(e_alt.e_total - e64.e_total)
+                             / abs(e64.e_total)},
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "kernel": "energy_tc_kernel", "kernel_ms": kmean,
@@ -435,7 +448,7 @@ def run_batch(args):
         items.append((B, torch.cat([eo, ev]).contiguous(), o, v))
         flops += 2.0 * o * o * v * v * X
     ctx = corr_gb300.Context(0, stream=stream)
-    prec = args.precision if args.precision != "fp64" else "split_bf16"
+    prec = args.precision if args.precision != "fp64" else "split_fp16"
     order, stages, tune_ms = ctx.batch_autotune(items, prec)
     out = torch.zeros(4 * len(items), dtype=torch.float64, device="cuda")
     ctx.rimp2_energy_batched_async(items, prec, out)

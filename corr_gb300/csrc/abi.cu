@@ -346,9 +346,10 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
     c->launches += 2;
     return CORR_OK;
   }
-  const int fmt = precision == CORR_PREC_SPLIT_FP16 ? 0 : 1;
+  const int scheme = scheme_for_precision(precision);
+  const int fmt = format_for_scheme(scheme);
   const int p = slice_bits_for(Qp);
-  CORR_CUDA(launch_slices(d_b, naux, R, Qp, fmt, p, sw, c->stream));
+  CORR_CUDA(launch_slices(d_b, naux, R, Qp, scheme, fmt, p, sw, c->stream));
   CUtensorMap tm;
   const uint64_t dims[3] = {(uint64_t)Qp, (uint64_t)nvir, (uint64_t)3 * nocc};
   const uint64_t strides[2] = {(uint64_t)Qp * 2, (uint64_t)nvir * Qp * 2};
@@ -361,8 +362,8 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
     c->attrs_set = true;
   }
   mark(c, 1);
-  CORR_CUDA(launch_energy_tc(tm, d_e, sw.sc, sw.dg, sh, Qp, fmt, p, partials, grid,
-                             &c->dres->status, c->stream));
+  CORR_CUDA(launch_energy_tc(tm, d_e, sw.sc, sw.dg, sw.scale, sh, Qp, fmt, scheme, partials,
+                             grid, &c->dres->status, c->stream));
   mark(c, 2);
   CORR_CUDA(launch_energy_reduce(partials, grid, sw.scale, out_e, c->stream));
   c->launches += 5;  // rowstat, slice, rowfactor, energy, reduce

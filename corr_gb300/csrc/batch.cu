@@ -133,7 +133,8 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
   }
 
   // ---- per-instance slicing and the host copy of the table
-  const int fmt = precision == CORR_PREC_SPLIT_FP16 ? 0 : 1;
+  const int scheme = scheme_for_precision(precision);
+  const int fmt = format_for_scheme(scheme);
   const size_t hbytes = sizeof(BatchInst) * n + sizeof(CUtensorMap) * n + sizeof(int) * n + 256;
   CORR_TRY(grow_pinned(c, hbytes));
   char* hp = static_cast<char*>(c->pinned);
@@ -145,7 +146,7 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
   for (int k = 0; k < n; ++k) {
     const corr_rimp2_instance& x = in[order[k]];
     const Shape& s = shp[k];
-    CORR_CUDA(launch_slices(x.bia, x.naux, s.R, s.Qp, fmt, s.p, sws[k], c->stream));
+    CORR_CUDA(launch_slices(x.bia, x.naux, s.R, s.Qp, scheme, fmt, s.p, sws[k], c->stream));
     const uint64_t dims[3] = {(uint64_t)s.Qp, (uint64_t)x.nvir, (uint64_t)3 * x.nocc};
     const uint64_t strides[2] = {(uint64_t)s.Qp * 2, (uint64_t)x.nvir * s.Qp * 2};
     const uint32_t box[3] = {32, (uint32_t)kTcTile, 1};
@@ -165,7 +166,6 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
     b.ntiles = s.sh.ntiles;
     b.ntpairs = s.sh.ntpairs;
     b.nkb = s.Qp / 32;
-    b.inv_l = ldexpf(1.0f, -(s.p + 1));
     horder[k] = order[k];
     ub += s.sh.nunits;
   }
@@ -182,8 +182,8 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
   int grid = c->sms;
   if ((long long)grid > total) grid = (int)total;
   mark(c, 1);
-  CORR_CUDA(launch_energy_batch(dtab, dmaps, n, total, queue, fmt, stages, grid, unit_part,
-                                &c->dres->status, c->stream));
+  CORR_CUDA(launch_energy_batch(dtab, dmaps, n, total, queue, fmt, scheme, stages, grid,
+                                unit_part, &c->dres->status, c->stream));
   mark(c, 2);
   CORR_CUDA(launch_batch_reduce(dtab, n, unit_part, dorder, out, c->stream));
   c->launches += 2;

@@ -12,18 +12,18 @@ struct BatchInst {
   const double* eps;    // [o+v]
   const float* sc;      // [o*v] row factors 2^(e_r - e_ref)
   const float* dg;      // [o*v] FP64 diagonal in scaled units
-  const double* scale;  // [1] energy factor 2^(4 e_ref)
+  const double* scale;  // [2] {energy factor 2^(4 e_ref), 1/L of the digits}
   long long unit_begin; // first global unit of this instance
   long long nunits;
   int o, v, ntiles, ntpairs, nkb;
-  float inv_l;          // 2^-(p+1) of this instance's digits
 };
 
 size_t batch_kernel_smem(int stages);
 cudaError_t prepare_energy_batch();
 cudaError_t launch_energy_batch(const BatchInst* insts, const CUtensorMap* tmaps, int ninst,
-                                long long total, unsigned long long* queue, int fmt, int stages,
-                                int grid, double* unit_part, int* status, cudaStream_t s);
+                                long long total, unsigned long long* queue, int fmt, int scheme,
+                                int stages, int grid, double* unit_part, int* status,
+                                cudaStream_t s);
 cudaError_t launch_batch_reduce(const BatchInst* insts, int ninst, const double* unit_part,
                                 const int* out_index, double* out, cudaStream_t s);
 

@@ -85,7 +85,7 @@ __device__ __forceinline__ UnitInfo unit_info(const BatchInst* __restrict__ in, 
   return r;
 }
 
-template <int STAGES>
+template <int STAGES, int SCHEME>
 __global__ void __launch_bounds__(NTHREADS, 1)
     energy_batch_kernel(const BatchInst* __restrict__ insts, const CUtensorMap* __restrict__ tmaps,
                         int ninst, long long total, unsigned long long* __restrict__ queue,
@@ -213,12 +213,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 q[l] = smem_desc(sb + (uint32_t)(2 * l + 1) * TILE_BYTES + off, 16, 512, SW64);
               }
               const uint32_t acc = (kb | kk) ? 1u : 0u;
-              tc_mma_f16(c0, r[0], q[0], idesc, acc);
-              tc_mma_f16(c1, r[0], q[1], idesc, acc);
-              tc_mma_f16(c1, r[1], q[0], idesc, 1u);
-              tc_mma_f16(c2, r[0], q[2], idesc, acc);
-              tc_mma_f16(c2, r[1], q[1], idesc, 1u);
-              tc_mma_f16(c2, r[2], q[0], idesc, 1u);
+              issue_digit_mmas<SCHEME>(c0, c1, c2, r, q, idesc, acc);
             }
             tc_commit(&ctl->empty[st]);
             if (++st == STAGES) {
@@ -260,7 +255,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const int o = bi.o, v = bi.v, i = ui.i, j = ui.j, A = ui.A, B = ui.B;
       const double* eps = bi.eps;
       const float* sc = bi.sc;
-      const float inv_l = bi.inv_l, inv_l2 = inv_l * inv_l;
+      const float inv_l = (float)bi.scale[1], inv_l2 = inv_l * inv_l;
       const int A0 = A * TILE, B0 = B * TILE;
       const bool same = (i == j);
       {
@@ -289,7 +284,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll 1
           for (int c = 0; c < TILE; c += 32) {
             float d1[32];
-            load_level_sum(tq, c, inv_l, inv_l2, sca1, ctl->scb, d1);
+            load_level_sum<SCHEME>(tq, c, inv_l, inv_l2, sca1, ctl->scb, d1);
             float fos = 0.f;
 #pragma unroll
             for (int k = 0; k < 32; ++k) {
@@ -304,7 +299,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           for (int k = 0; k < 4; ++k) {
             float d[32];
             const int cw = 32 * ((q + k) & 3);
-            load_level_sum(tq, cw, inv_l, inv_l2, sca1, ctl->scb, d);
+            load_level_sum<SCHEME>(tq, cw, inv_l, inv_l2, sca1, ctl->scb, d);
 #pragma unroll
             for (int x = 0; x < 32; ++x) ctl->tbuf[q][lane][x] = d[x];
             named_bar(1, 128);
@@ -313,7 +308,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             float d2[32];
 #pragma unroll
             for (int x = 0; x < 32; ++x) d2[x] = ctl->tbuf[wr][x][lane];
-            load_level_sum(tq, cr, inv_l, inv_l2, sca1, ctl->scb, d);
+            load_level_sum<SCHEME>(tq, cr, inv_l, inv_l2, sca1, ctl->scb, d);
             float fos = 0.f, fss = 0.f;
 #pragma unroll
             for (int x = 0; x < 32; ++x) {
@@ -331,7 +326,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll 1
           for (int c = 0; c < TILE; c += 32) {
             float d1[32];
-            load_level_sum(tq, c, inv_l, inv_l2, sca1, ctl->scb, d1);
+            load_level_sum<SCHEME>(tq, c, inv_l, inv_l2, sca1, ctl->scb, d1);
             tmem_st32(tq + COL_STASH + (uint32_t)c, d1);
           }
           tc_wait_st();
@@ -357,7 +352,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll 1
           for (int c = 0; c < TILE; c += 32) {
             float d2[32], d1[32];
-            load_level_sum(tq, c, inv_l, inv_l2, sca2, ctl->scb, d2);
+            load_level_sum<SCHEME>(tq, c, inv_l, inv_l2, sca2, ctl->scb, d2);
             tmem_ld32(tq + COL_STASH + (uint32_t)c, d1);
             tc_wait_ld();
             float fos = 0.f, fss = 0.f;
@@ -448,25 +443,50 @@ size_t batch_kernel_smem(int stages) {
   return stages == 3 ? batch_smem_bytes<3>() : batch_smem_bytes<4>();
 }
 
+template <int STAGES, int SCHEME>
+static cudaError_t set_batch_attr() {
+  return cudaFuncSetAttribute(energy_batch_kernel<STAGES, SCHEME>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)batch_smem_bytes<STAGES>());
+}
+
 cudaError_t prepare_energy_batch() {
-  cudaError_t e = cudaFuncSetAttribute(energy_batch_kernel<3>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)batch_smem_bytes<3>());
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(energy_batch_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)batch_smem_bytes<4>());
+  cudaError_t e = set_batch_attr<3, kSchemeDigits3>();
+  if (e == cudaSuccess) e = set_batch_attr<4, kSchemeDigits3>();
+  if (e == cudaSuccess) e = set_batch_attr<3, kSchemeKara>();
+  if (e == cudaSuccess) e = set_batch_attr<4, kSchemeKara>();
+  return e;
+}
+
+template <int STAGES, int SCHEME>
+static void launch_batch_variant(const BatchInst* insts, const CUtensorMap* tmaps, int ninst,
+                                 long long total, unsigned long long* queue, uint32_t idesc,
+                                 int grid, double* unit_part, int* status, cudaStream_t s) {
+  energy_batch_kernel<STAGES, SCHEME><<<grid, NTHREADS, batch_smem_bytes<STAGES>(), s>>>(
+      insts, tmaps, ninst, total, queue, idesc, unit_part, status);
 }
 
 cudaError_t launch_energy_batch(const BatchInst* insts, const CUtensorMap* tmaps, int ninst,
-                                long long total, unsigned long long* queue, int fmt, int stages,
-                                int grid, double* unit_part, int* status, cudaStream_t s) {
+                                long long total, unsigned long long* queue, int fmt, int scheme,
+                                int stages, int grid, double* unit_part, int* status,
+                                cudaStream_t s) {
   const uint32_t idesc = idesc_f16((uint32_t)fmt, TILE, TILE);
-  if (stages == 3)
-    energy_batch_kernel<3><<<grid, NTHREADS, batch_smem_bytes<3>(), s>>>(
-        insts, tmaps, ninst, total, queue, idesc, unit_part, status);
-  else
-    energy_batch_kernel<4><<<grid, NTHREADS, batch_smem_bytes<4>(), s>>>(
-        insts, tmaps, ninst, total, queue, idesc, unit_part, status);
+  const bool kara = scheme == kSchemeKara;
+  if (stages == 3) {
+    if (kara)
+      launch_batch_variant<3, kSchemeKara>(insts, tmaps, ninst, total, queue, idesc, grid,
+                                           unit_part, status, s);
+    else
+      launch_batch_variant<3, kSchemeDigits3>(insts, tmaps, ninst, total, queue, idesc, grid,
+                                              unit_part, status, s);
+  } else {
+    if (kara)
+      launch_batch_variant<4, kSchemeKara>(insts, tmaps, ninst, total, queue, idesc, grid,
+                                           unit_part, status, s);
+    else
+      launch_batch_variant<4, kSchemeDigits3>(insts, tmaps, ninst, total, queue, idesc, grid,
+                                              unit_part, status, s);
+  }
   return cudaGetLastError();
 }
 

@@ -1,14 +1,16 @@
 // Precision-form fused RI-MP2 energy on the 5th-generation tensor cores.
 //
-// Input: the three integer slices of B (split.cu), as one 16-bit array
+// Input: the three 16-bit integer planes of B (split.cu), as one array
 // S[l][i][a][Qp] read through a 3-D TMA map over [3*nocc][nvir][Qp].
 // Work unit = (occupied pair i<=j, virtual tile pair A<=B), tiles of 128.
 //
 // Phase 1 forms D1[a][b] = (ia|jb) for a in A, b in B; phase 2 forms
-// D2[a][b] = (ib|ja).  Each phase accumulates three levels in TMEM,
-//   acc_m = sum_{k+l=m} s_k(row) . s_l(col)^T    (m = 0, 1, 2; six MMAs per K=16),
-// whose partial sums are exact integers (split.cu), then the epilogue forms
-//   d = sc_row sc_col (acc_0 + acc_1/L + acc_2/L^2)   (FP32, round-to-nearest).
+// D2[a][b] = (ib|ja).  Each phase accumulates three exact integer sums in
+// TMEM (split.cu), by scheme:
+//   0: acc_m = sum_{k+l=m} s_k(row) . s_l(col)^T   (m = 0..2, six MMAs per K=16)
+//   1: P0 = s0.s0', Pm = u.u', P2 = s1.s1'        (three MMAs per K=16)
+// and the epilogue forms d = sc_row sc_col (value of the digits) in FP32 with
+// round-to-nearest (tc_common.cuh).
 // D1 is parked in TMEM columns 384-511 while D2 accumulates in 0-383.  For
 // i == j, D2 == D1 and phase 2 is skipped; for A == B, D2 = D1^T is obtained
 // by a 32x32-block exchange through shared memory instead of a second pass.  On the (i==j, A==B) diagonal the
@@ -66,11 +68,12 @@ __device__ __forceinline__ void unit_decode(long long u, const EnergyShape& sh, 
   tpair_decode(tp, sh.ntiles, A, B);
 }
 
+template <int SCHEME>
 __global__ void __launch_bounds__(NTHREADS, 1)
     energy_tc_kernel(const __grid_constant__ CUtensorMap tm, const double* __restrict__ eps,
-                     const float* __restrict__ sc, const float* __restrict__ dg, EnergyShape sh,
-                     int nkb, uint32_t idesc, float inv_l, double* __restrict__ partials,
-                     int* status) {
+                     const float* __restrict__ sc, const float* __restrict__ dg,
+                     const double* __restrict__ scale, EnergyShape sh, int nkb, uint32_t idesc,
+                     double* __restrict__ partials, int* status) {
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   uint8_t* tiles = smem_raw + (((raw + 1023u) & ~1023u) - raw);
@@ -177,12 +180,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 q[l] = smem_desc(sb + (uint32_t)(2 * l + 1) * TILE_BYTES + off, 16, 512, SW64);
               }
               const uint32_t acc = (kb | kk) ? 1u : 0u;
-              tc_mma_f16(c0, r[0], q[0], idesc, acc);
-              tc_mma_f16(c1, r[0], q[1], idesc, acc);
-              tc_mma_f16(c1, r[1], q[0], idesc, 1u);
-              tc_mma_f16(c2, r[0], q[2], idesc, acc);
-              tc_mma_f16(c2, r[1], q[1], idesc, 1u);
-              tc_mma_f16(c2, r[2], q[0], idesc, 1u);
+              issue_digit_mmas<SCHEME>(c0, c1, c2, r, q, idesc, acc);
             }
             tc_commit(&ctl->empty[st]);  // stage reusable once these MMAs finish
             if (++st == STAGES) {
@@ -204,6 +202,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const int et = threadIdx.x - 64;  // 0..127
     const int arow = 32 * q + lane;   // accumulator row = TMEM lane
     const uint32_t tq = tmem + ((uint32_t)(32 * q) << 16);
+    const float inv_l = (float)scale[1];
     const float inv_l2 = inv_l * inv_l;
     double tot_os = 0.0, tot_ss = 0.0;
     bool dead = false;
@@ -245,7 +244,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll 1
           for (int c = 0; c < TILE; c += 32) {
             float d1[32];
-            load_level_sum(tq, c, inv_l, inv_l2, sca1, ctl->scb, d1);
+            load_level_sum<SCHEME>(tq, c, inv_l, inv_l2, sca1, ctl->scb, d1);
             float fos = 0.f;
 #pragma unroll
             for (int k = 0; k < 32; ++k) {
@@ -263,7 +262,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           for (int k = 0; k < 4; ++k) {
             float d[32];
             const int cw = 32 * ((q + k) & 3);
-            load_level_sum(tq, cw, inv_l, inv_l2, sca1, ctl->scb, d);
+            load_level_sum<SCHEME>(tq, cw, inv_l, inv_l2, sca1, ctl->scb, d);
 #pragma unroll
             for (int x = 0; x < 32; ++x) ctl->tbuf[q][lane][x] = d[x];
             named_bar(1, 128);
@@ -272,7 +271,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             float d2[32];
 #pragma unroll
             for (int x = 0; x < 32; ++x) d2[x] = ctl->tbuf[wr][x][lane];
-            load_level_sum(tq, cr, inv_l, inv_l2, sca1, ctl->scb, d);
+            load_level_sum<SCHEME>(tq, cr, inv_l, inv_l2, sca1, ctl->scb, d);
             float fos = 0.f, fss = 0.f;
 #pragma unroll
             for (int x = 0; x < 32; ++x) {
@@ -290,7 +289,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll 1
           for (int c = 0; c < TILE; c += 32) {
             float d1[32];
-            load_level_sum(tq, c, inv_l, inv_l2, sca1, ctl->scb, d1);
+            load_level_sum<SCHEME>(tq, c, inv_l, inv_l2, sca1, ctl->scb, d1);
             tmem_st32(tq + COL_STASH + (uint32_t)c, d1);
           }
           tc_wait_st();
@@ -317,7 +316,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll 1
           for (int c = 0; c < TILE; c += 32) {
             float d2[32], d1[32];
-            load_level_sum(tq, c, inv_l, inv_l2, sca2, ctl->scb, d2);
+            load_level_sum<SCHEME>(tq, c, inv_l, inv_l2, sca2, ctl->scb, d2);
             tmem_ld32(tq + COL_STASH + (uint32_t)c, d1);
             tc_wait_ld();
             float fos = 0.f, fss = 0.f;
@@ -368,17 +367,25 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 }  // namespace
 
 cudaError_t prepare_energy_tc() {
-  return cudaFuncSetAttribute(energy_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)kSmemBytes);
+  cudaError_t e = cudaFuncSetAttribute(energy_tc_kernel<kSchemeDigits3>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kSmemBytes);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(energy_tc_kernel<kSchemeKara>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
 }
 
 cudaError_t launch_energy_tc(const CUtensorMap& tmap, const double* eps, const float* sc,
-                             const float* dg, const EnergyShape& sh, int Qp, int fmt, int p,
-                             double* partials, int grid, int* status, cudaStream_t s) {
+                             const float* dg, const double* scale, const EnergyShape& sh, int Qp,
+                             int fmt, int scheme, double* partials, int grid, int* status,
+                             cudaStream_t s) {
   const uint32_t idesc = idesc_f16((uint32_t)fmt, TILE, TILE);
-  const float inv_l = ldexpf(1.0f, -(p + 1));
-  energy_tc_kernel<<<grid, NTHREADS, kSmemBytes, s>>>(tmap, eps, sc, dg, sh, Qp / KB, idesc,
-                                                      inv_l, partials, status);
+  if (scheme == kSchemeKara)
+    energy_tc_kernel<kSchemeKara><<<grid, NTHREADS, kSmemBytes, s>>>(
+        tmap, eps, sc, dg, scale, sh, Qp / KB, idesc, partials, status);
+  else
+    energy_tc_kernel<kSchemeDigits3><<<grid, NTHREADS, kSmemBytes, s>>>(
+        tmap, eps, sc, dg, scale, sh, Qp / KB, idesc, partials, status);
   return cudaGetLastError();
 }
 

@@ -28,12 +28,20 @@ struct SliceWork {
   double* diag;    // [R] FP64 sum_Q B^2
   float* sc;       // [R] 2^(e_r - e_ref)
   float* dg;       // [R] diag in scaled units
-  int* eref;       // [1]
-  double* scale;   // [1] global energy factor 2^(4 e_ref)
+  int* eref;       // [2] {e_ref, level exponent k (scheme 1)}
+  double* scale;   // [2] {global energy factor 2^(4 e_ref), 1/L}
 };
+// Slice schemes (split.cu).  0: three BF16 digits, six products per K step
+// (levels 0..2).  1: two FP16 digits, three Karatsuba products.
+constexpr int kSchemeDigits3 = 0;
+constexpr int kSchemeKara = 1;
+inline int scheme_for_precision(int precision) {
+  return precision == 1 /* CORR_PREC_SPLIT_FP16 */ ? kSchemeKara : kSchemeDigits3;
+}
+inline int format_for_scheme(int scheme) { return scheme == kSchemeKara ? 0 : 1; }  // 0 FP16
 int slice_bits_for(int Qp);
-cudaError_t launch_slices(const double* b, int naux, long long R, int Qp, int fmt, int p,
-                          SliceWork w, cudaStream_t s);
+cudaError_t launch_slices(const double* b, int naux, long long R, int Qp, int scheme, int fmt,
+                          int p, SliceWork w, cudaStream_t s);
 // Sum per-CTA partial pairs {os, ss} in fixed order, times `scale` (device),
 // into out[4] = {E_SS, E_OS, E, E_SCS}.
 cudaError_t launch_energy_reduce(const double* partials, int n, const double* scale, double* out,
@@ -42,9 +50,11 @@ cudaError_t launch_energy_reduce(const double* partials, int n, const double* sc
 // ---- fused energy kernels ---------------------------------------------------
 // tcgen05 precision form (energy_tc.cu).  tmap: 3-D map over the slice
 // array viewed as [3*nocc][nvir][Qp] (16-bit), box {32, 128, 1}, 64B swizzle.
+// scale: the SliceWork scale pair (the kernel reads 1/L from scale[1]).
 cudaError_t launch_energy_tc(const CUtensorMap& tmap, const double* eps, const float* sc,
-                             const float* dg, const EnergyShape& sh, int Qp, int fmt, int p,
-                             double* partials, int grid, int* status, cudaStream_t s);
+                             const float* dg, const double* scale, const EnergyShape& sh, int Qp,
+                             int fmt, int scheme, double* partials, int grid, int* status,
+                             cudaStream_t s);
 cudaError_t prepare_energy_tc();  // one-time attributes (dynamic smem size)
 constexpr int kTcTile = 128;
 

@@ -154,9 +154,10 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
     CORR_CUDA(launch_energy_fp64(bia, eps, sh, partials, grid, s));
     CORR_CUDA(launch_energy_reduce(partials, grid, nullptr, hdr->e, s));
   } else {
-    const int fmt = precision == CORR_PREC_SPLIT_FP16 ? 0 : 1;
+    const int scheme = scheme_for_precision(precision);
+    const int fmt = format_for_scheme(scheme);
     const int p = slice_bits_for(Qp);
-    CORR_CUDA(launch_slices(bia, naux, R, Qp, fmt, p, sw, s));
+    CORR_CUDA(launch_slices(bia, naux, R, Qp, scheme, fmt, p, sw, s));
     CUtensorMap tm;
     const uint64_t dims[3] = {(uint64_t)Qp, (uint64_t)nvir, (uint64_t)3 * nocc};
     const uint64_t strides[2] = {(uint64_t)Qp * 2, (uint64_t)nvir * Qp * 2};
@@ -165,8 +166,8 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
                          fmt == 0 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
                                   : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
                          3, sw.S, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_64B));
-    CORR_CUDA(launch_energy_tc(tm, eps, sw.sc, sw.dg, sh, Qp, fmt, p, partials, grid,
-                               &hdr->status, s));
+    CORR_CUDA(launch_energy_tc(tm, eps, sw.sc, sw.dg, sw.scale, sh, Qp, fmt, scheme, partials,
+                               grid, &hdr->status, s));
     CORR_CUDA(launch_energy_reduce(partials, grid, sw.scale, hdr->e, s));
   }
   Header h;

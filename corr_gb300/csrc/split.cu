@@ -17,6 +17,30 @@
 // The diagonal elements (ia|ia) = sum_Q (B^Q_ia)^2 are all-positive sums that
 // dominate the bias of any truncated scheme; they are formed here in FP64 and
 // substituted by the energy kernel.
+//
+// Scheme 1 (FP16 slices, Karatsuba): two digits per element,
+//
+//   B^Q_r = 2^(e_r) (s0 + s1/L),   s0 = round(x), s1 = round(L (x - s0)),
+//   x = B^Q_r 2^(-e_r),  u = s0 + s1,
+//
+// and three products per pair of rows (Karatsuba's identity for the cross term),
+//
+//   P0 = s0.s0',  Pm = u.u',  P2 = s1.s1',
+//   x.x' = P0 + (Pm - P0 - P2)/L + P2/L^2   (exact for the two-digit values).
+//
+// Dropping the s1.s1' product (plain two-term hi/lo splitting) loses every
+// product of two sub-digit elements and biases molecular energies; the
+// Karatsuba form keeps it at the cost of three products, not four.  Each of
+// P0, Pm, P2 is a tensor-core sum of integer products, exact in FP32 when
+// every partial sum stays below 2^24; by Cauchy-Schwarz that holds when
+// ||s0||, ||u||, ||s1|| <= 2^12 for every row, which the pre-pass enforces:
+//   e_r: ||x|| <= 2^11.5 - sqrt(naux)/2 - 1 and max|x| <= 2^11 - 2^9 - 1;
+//   L = 2^k, the largest k <= 10 such that for every row
+//     ||s0 + L r|| + (1/2 + 2^-10) sqrt(naux) <= 2^12   (bounds ||u||),
+//     L ||r|| + (1/2 + 2^-10) sqrt(naux) <= 2^12        (bounds ||s1||),
+//     max|s0| + L/2 <= 2^11                            (u exact in FP16),
+//   with r = x - s0 and the row sums a = ||s0||^2, b = s0.r, c = ||r||^2 taken
+//   in a second pass over the row (a exact, b and c with a 2^-10 margin).
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -46,6 +70,134 @@ __device__ __forceinline__ int round_scaled(double b, int k) {
   else if (sh > 62) X = 0;
   else X = (m + (1ll << (sh - 1))) >> sh;
   return bits < 0 ? -(int)X : (int)X;
+}
+
+// round(b * 2^k) as a 64-bit integer (same rounding as round_scaled); exact
+// for |result| < 2^62.
+__device__ __forceinline__ long long round_scaled64(double b, int k) {
+  const long long bits = __double_as_longlong(b);
+  const int E = (int)((bits >> 52) & 0x7ff);
+  if (E == 0) return 0;
+  const long long m = (bits & 0xfffffffffffffll) | (1ll << 52);
+  const int sh = 1075 - E - k;
+  long long X;
+  if (sh <= 0) X = m << (-sh > 9 ? 9 : -sh);  // not reached for |x| < 2^11
+  else if (sh > 62) X = 0;
+  else X = (m + (1ll << (sh - 1))) >> sh;
+  return bits < 0 ? -X : X;
+}
+
+// Scheme-1 digits of one element from its 24-bit fixed-point value
+// X24 = round(x 2^24): s0 = round(x) (ties up), r24 = X24 - s0 2^24.
+__device__ __forceinline__ void kara_digits(long long X24, int k, int* s0, int* s1) {
+  const long long h = (X24 + (1ll << 23)) >> 24;
+  const int r24 = (int)(X24 - (h << 24));
+  *s0 = (int)h;
+  *s1 = (r24 + (1 << (23 - k))) >> (24 - k);
+}
+
+// smallest e with y 2^-e <= 1 (y > 0)
+__device__ __forceinline__ int ceil_log2(double y) {
+  int k;
+  const double f = frexp(y, &k);  // y = f 2^k, f in [0.5, 1)
+  return f == 0.5 ? k - 1 : k;
+}
+
+constexpr int kKaraMaxK = 10;
+
+// Scheme 1: per row r, e_r and the FP64 diagonal (first pass), then the
+// digit statistics of the second pass and the largest admissible level
+// exponent k_r (global minimum by atomicMin into kglob).  Block = 32 rows x
+// 8 Q-groups.
+__global__ void rowstat_kara_kernel(const double* __restrict__ b, int naux, long long R,
+                                    int* __restrict__ erow, double* __restrict__ diag, int* eref,
+                                    int* kglob) {
+  __shared__ unsigned long long smax[8][32];
+  __shared__ double ssum[8][32];
+  __shared__ double sb[8][32], scc[8][32];
+  __shared__ int sa[8][32], sm0[8][32];
+  __shared__ int se[32];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const long long r = (long long)blockIdx.x * 32 + tx;
+  unsigned long long m = 0;
+  double s = 0.0;
+  if (r < R)
+    for (int q = ty; q < naux; q += 8) {
+      const double x = b[(long long)q * R + r];
+      const unsigned long long ax = abs_bits(x);
+      m = ax > m ? ax : m;
+      s = fma(x, x, s);
+    }
+  smax[ty][tx] = m;
+  ssum[ty][tx] = s;
+  __syncthreads();
+  const double hs = 0.5 * sqrt((double)naux);
+  if (ty == 0) {
+    int e = INT_MIN / 4;
+    if (r < R) {
+      for (int k = 1; k < 8; ++k) {
+        m = smax[k][tx] > m ? smax[k][tx] : m;
+        s += ssum[k][tx];
+      }
+      const bool live = m != 0 && (m >> 52) != 0;
+      if (live) {
+        const double mx = __longlong_as_double((long long)m);
+        const double t0 = 2896.309375740099 - hs - 1.0;  // 2^11.5 - sqrt(naux)/2 - 1
+        const int en = ceil_log2(sqrt(s) / t0);
+        const int ec = ceil_log2(mx / (2048.0 - 512.0 - 1.0));
+        e = en > ec ? en : ec;
+        atomicMax(eref, e);
+      }
+      erow[r] = e;
+      diag[r] = s;
+    }
+    se[tx] = e;
+  }
+  __syncthreads();
+  const int e = se[tx];
+  const bool live = r < R && e > INT_MIN / 8;
+  int a = 0, m0 = 0;
+  float bb = 0.f, cc = 0.f;
+  if (live)
+    for (int q = ty; q < naux; q += 8) {
+      const long long X24 = round_scaled64(b[(long long)q * R + r], 24 - e);
+      const long long h = (X24 + (1ll << 23)) >> 24;
+      const float rf = (float)(int)(X24 - (h << 24));
+      const int s0 = (int)h;
+      a += s0 * s0;
+      m0 = max(m0, abs(s0));
+      bb = fmaf((float)s0, rf, bb);
+      cc = fmaf(rf, rf, cc);
+    }
+  sa[ty][tx] = a;
+  sm0[ty][tx] = m0;
+  sb[ty][tx] = (double)bb;
+  scc[ty][tx] = (double)cc;
+  __syncthreads();
+  if (ty == 0 && live) {
+    double bsum = 0.0, csum = 0.0;
+    for (int k = 0; k < 8; ++k) {
+      if (k) {
+        a += sa[k][tx];
+        m0 = max(m0, sm0[k][tx]);
+      }
+      bsum += sb[k][tx];
+      csum += scc[k][tx];
+    }
+    const double A = (double)a, Bx = bsum * 0x1p-24, C = csum * 0x1p-48;
+    const double marg = 1.0 + 0x1p-10;
+    const double slack = (0.5 + 0x1p-10) * sqrt((double)naux);
+    const double bpos = Bx + 0x1p-10 * sqrt(A * C * marg);  // upper bound on s0.r
+    int k = kKaraMaxK;
+    for (; k > 0; --k) {
+      const double L = (double)(1 << k);
+      const double nu2 = A + 2.0 * L * bpos + L * L * C * marg;
+      const bool ok = sqrt(nu2 > 0.0 ? nu2 : 0.0) + slack <= 4096.0 &&
+                      L * sqrt(C * marg) + slack <= 4096.0 && m0 + (1 << (k - 1)) <= 2048;
+      if (ok) break;
+    }
+    atomicMin(kglob, k);
+  }
 }
 
 // Row statistics over Q for each r: e_r, the FP64 diagonal sum_Q B^2, and the
@@ -152,12 +304,68 @@ __global__ void __launch_bounds__(256) slice_kernel(const double* __restrict__ b
   d2[1] = v2[1];
 }
 
+// Scheme 1 slices: planes S[0] = s0, S[1] = u = s0 + s1, S[2] = s1 (FP16),
+// same tiling and store pattern as slice_kernel.
+__global__ void __launch_bounds__(256) slice_kara_kernel(const double* __restrict__ b, int naux,
+                                                         long long R, int Qp,
+                                                         const int* __restrict__ erow,
+                                                         const int* __restrict__ kglob,
+                                                         uint16_t* __restrict__ S) {
+  __shared__ double tile[64][65];
+  const int t = threadIdx.x;
+  const long long r0 = (long long)blockIdx.x * 64;
+  const int q0 = blockIdx.y * 64;
+  {
+    const int c = t & 63;
+#pragma unroll 4
+    for (int k = t >> 6; k < 64; k += 4) {
+      const int q = q0 + k;
+      const long long r = r0 + c;
+      tile[k][c] = (q < naux && r < R) ? b[(long long)q * R + r] : 0.0;
+    }
+  }
+  __syncthreads();
+  const int rl = t >> 2, qc = (t & 3) * 16;
+  const long long r = r0 + rl;
+  if (r >= R || q0 + qc >= Qp) return;
+  const int e = erow[r];
+  const bool live = e > INT_MIN / 8;
+  const int k = *kglob;
+  __align__(16) uint16_t h0[16];
+  __align__(16) uint16_t h1[16];
+  __align__(16) uint16_t h2[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    int s0 = 0, s1 = 0;
+    if (live) kara_digits(round_scaled64(tile[qc + j][rl], 24 - e), k, &s0, &s1);
+    h0[j] = to16i<0>(s0);
+    h1[j] = to16i<0>(s0 + s1);
+    h2[j] = to16i<0>(s1);
+  }
+  const size_t plane = (size_t)R * Qp;
+  const size_t at = (size_t)r * Qp + q0 + qc;
+  uint4* d0 = reinterpret_cast<uint4*>(S + at);
+  uint4* d1 = reinterpret_cast<uint4*>(S + plane + at);
+  uint4* d2 = reinterpret_cast<uint4*>(S + 2 * plane + at);
+  const uint4* v0 = reinterpret_cast<const uint4*>(h0);
+  const uint4* v1 = reinterpret_cast<const uint4*>(h1);
+  const uint4* v2 = reinterpret_cast<const uint4*>(h2);
+  d0[0] = v0[0];
+  d0[1] = v0[1];
+  d1[0] = v1[0];
+  d1[1] = v1[1];
+  d2[0] = v2[0];
+  d2[1] = v2[1];
+}
+
 // Per-row FP32 factors for the energy kernel: sc_r = 2^(e_r - e_ref) and the
 // diagonal sum in the same units, dg_r = diag_r 2^(-2 e_ref).  Also writes
-// the global energy factor 2^(4 e_ref) into scale_out[0].
+// the global energy factor 2^(4 e_ref) into scale_out[0] and the level
+// factor 1/L into scale_out[1] (scheme 1: L = 2^eref[1]; scheme 0: L = 2^(p+1)).
 __global__ void rowfactor_kernel(const int* __restrict__ erow, const double* __restrict__ diag,
-                                 long long R, const int* eref, float* __restrict__ sc,
-                                 float* __restrict__ dg, double* scale_out) {
+                                 long long R, const int* eref, int level_log2,
+                                 float* __restrict__ sc, float* __restrict__ dg,
+                                 double* scale_out) {
   int er = *eref;
   if (er < -4000) er = 0;  // every row zero
   for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < R;
@@ -166,7 +374,10 @@ __global__ void rowfactor_kernel(const int* __restrict__ erow, const double* __r
     sc[r] = (e > INT_MIN / 8) ? (float)ldexp(1.0, e - er) : 0.0f;
     dg[r] = (float)ldexp(diag[r], -2 * er);
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) scale_out[0] = ldexp(1.0, 4 * er);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    scale_out[0] = ldexp(1.0, 4 * er);
+    scale_out[1] = ldexp(1.0, -(level_log2 >= 0 ? level_log2 : eref[1]));
+  }
 }
 
 __global__ void energy_reduce_kernel(const double* __restrict__ part, int n,
@@ -214,19 +425,28 @@ int slice_bits_for(int Qp) {
   return p;
 }
 
-cudaError_t launch_slices(const double* b, int naux, long long R, int Qp, int fmt, int p,
-                          SliceWork w, cudaStream_t s) {
+cudaError_t launch_slices(const double* b, int naux, long long R, int Qp, int scheme, int fmt,
+                          int p, SliceWork w, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(w.eref, 0x80, sizeof(int), s);  // very negative start
   if (e != cudaSuccess) return e;
-  rowstat_kernel<<<(unsigned)((R + 31) / 32), dim3(32, 8), 0, s>>>(b, naux, R, p, w.erow, w.diag,
-                                                                   w.eref);
+  e = cudaMemsetAsync(w.eref + 1, 0x7f, sizeof(int), s);  // level exponent: min-reduced
+  if (e != cudaSuccess) return e;
   dim3 grid((unsigned)((R + 63) / 64), (unsigned)((Qp + 63) / 64));
-  if (fmt == 0)
-    slice_kernel<0><<<grid, 256, 0, s>>>(b, naux, R, Qp, p, w.erow, w.S);
-  else
-    slice_kernel<1><<<grid, 256, 0, s>>>(b, naux, R, Qp, p, w.erow, w.S);
+  if (scheme == kSchemeKara) {
+    rowstat_kara_kernel<<<(unsigned)((R + 31) / 32), dim3(32, 8), 0, s>>>(b, naux, R, w.erow,
+                                                                          w.diag, w.eref,
+                                                                          w.eref + 1);
+    slice_kara_kernel<<<grid, 256, 0, s>>>(b, naux, R, Qp, w.erow, w.eref + 1, w.S);
+  } else {
+    rowstat_kernel<<<(unsigned)((R + 31) / 32), dim3(32, 8), 0, s>>>(b, naux, R, p, w.erow,
+                                                                     w.diag, w.eref);
+    if (fmt == 0)
+      slice_kernel<0><<<grid, 256, 0, s>>>(b, naux, R, Qp, p, w.erow, w.S);
+    else
+      slice_kernel<1><<<grid, 256, 0, s>>>(b, naux, R, Qp, p, w.erow, w.S);
+  }
   rowfactor_kernel<<<(unsigned)((R + 255) / 256 < 1024 ? (R + 255) / 256 : 1024), 256, 0, s>>>(
-      w.erow, w.diag, R, w.eref, w.sc, w.dg, w.scale);
+      w.erow, w.diag, R, w.eref, scheme == kSchemeKara ? -1 : p + 1, w.sc, w.dg, w.scale);
   return cudaGetLastError();
 }
 

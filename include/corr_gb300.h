@@ -46,12 +46,14 @@ enum corr_status {
 enum corr_precision {
   CORR_PREC_FP64 = 0,       /* FP64 end to end (FP64 mma.sync)                   */
   CORR_PREC_SPLIT_FP16 = 1, /* each row (i,a) of B scaled by a power of two and
-                               split into three 7-bit integer slices stored as
-                               FP16; the six slice products of orders 0-2 run on
-                               tcgen05 with exact FP32 integer accumulation in
-                               TMEM; (ia|ia) in FP64; FP64 pair-energy sums     */
-  CORR_PREC_SPLIT_BF16 = 2  /* the same slices stored as BF16 (bit-identical
-                               results: the slices are small integers)          */
+                               split into two integer digits s0 + s1/L stored as
+                               FP16 (|digit| <= 2048); three Karatsuba products
+                               s0.s0', (s0+s1).(s0'+s1'), s1.s1' on tcgen05 with
+                               exact FP32 integer accumulation in TMEM; (ia|ia)
+                               in FP64; FP64 pair-energy sums.  The fast form.  */
+  CORR_PREC_SPLIT_BF16 = 2  /* three 7-bit integer digits per element stored as
+                               BF16; the six digit products of orders 0-2 on
+                               tcgen05, exact accumulation, (ia|ia) in FP64     */
 };
 
 typedef struct corr_context corr_context;

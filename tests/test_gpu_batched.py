@@ -27,7 +27,7 @@ def _gpu_instances(sizes, seed):
 def test_batched_matches_single_and_oracle(ctx):
     sizes = [(1, 1, 1), (3, 20, 40), (5, 130, 70), (2, 257, 33), (7, 64, 200), (4, 40, 1000)]
     items = _gpu_instances(sizes, 7)
-    for prec in ("split_bf16", "fp64"):
+    for prec in ("split_fp16", "split_bf16", "fp64"):
         got = ctx.rimp2_energy_batched(items, prec)
         for (B, e, o, v), g in zip(items, got):
             single = ctx.rimp2_energy(B, e, o, v, B.shape[0], prec)
@@ -42,17 +42,18 @@ def test_batched_policies_agree_and_autotune(ctx, tmp_path):
     sizes = O.synth_batch_sizes(24, 55)
     sizes = [(o, v, X) for (o, v, X) in sizes if o <= 25]  # keep the test quick
     items = _gpu_instances(sizes, 8)
-    base = None
-    for order in (0, 1):
-        for stages in (3, 4):
-            ctx.set_batch_policy(order, stages)
-            got = [g.e_total for g in ctx.rimp2_energy_batched(items, "split_bf16")]
-            if base is None:
-                base = got
-            assert got == base  # per-unit partials are reduced in a fixed order
+    for prec in ("split_fp16", "split_bf16"):
+        base = None
+        for order in (0, 1):
+            for stages in (3, 4):
+                ctx.set_batch_policy(order, stages)
+                got = [g.e_total for g in ctx.rimp2_energy_batched(items, prec)]
+                if base is None:
+                    base = got
+                assert got == base  # per-unit partials are reduced in a fixed order
     cache = str(tmp_path / "autotune.json")
-    o1, s1, ms1 = ctx.batch_autotune(items, "split_bf16", cache=cache)
-    o2, s2, ms2 = ctx.batch_autotune(items, "split_bf16", cache=cache)  # from the cache
+    o1, s1, ms1 = ctx.batch_autotune(items, "split_fp16", cache=cache)
+    o2, s2, ms2 = ctx.batch_autotune(items, "split_fp16", cache=cache)  # from the cache
     assert (o1, s1) == (o2, s2) and ms1 == ms2 and ms1 > 0
 
 
@@ -63,7 +64,7 @@ def test_batched_graph_capture(ctx):
     out = torch.zeros(4 * len(items), dtype=torch.float64, device="cuda")
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream)
-    ctx.rimp2_energy_batched_async(items, "split_bf16", out)
+    ctx.rimp2_energy_batched_async(items, "split_fp16", out)
     torch.cuda.synchronize()
     ref = out.clone()
     graph = torch.cuda.CUDAGraph()
@@ -72,7 +73,7 @@ def test_batched_graph_capture(ctx):
     out.zero_()
     with torch.cuda.graph(graph, stream=side):
         ctx.set_stream(side)
-        ctx.rimp2_energy_batched_async(items, "split_bf16", out)
+        ctx.rimp2_energy_batched_async(items, "split_fp16", out)
     ctx.set_stream(stream)
     graph.replay()
     torch.cuda.synchronize()

@@ -73,13 +73,14 @@ def test_config3_water_cluster(ctx):
     ref = g["ri_mp2"]
     assert abs(e64.e_total - ref[2]) <= 1e-9, (e64, ref)
     assert abs(e64.e_ss - ref[0]) <= 1e-9 and abs(e64.e_os - ref[1]) <= 1e-9
-    esp, _ = ctx.rimp2_energy_from_3index(200, md, ed, Jd, Pd, "split_bf16")
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    esp2, _ = ctx.rimp2_energy_from_3index(200, md, ed, Jd, Pd, "split_bf16")
-    t_split = time.perf_counter() - t0
-    assert esp2.e_total == esp.e_total  # fixed-order reductions: reproducible
-    # the spec bar: precision form within 1 uEh of FP64
-    assert abs(esp.e_total - e64.e_total) <= 1e-6, (esp, e64)
-    print(f"config3 time-to-E_corr from integrals (split_bf16): {t_split * 1e3:.1f} ms, "
-          f"|dE| = {abs(esp.e_total - e64.e_total):.3e} Eh")
+    for prec in ("split_fp16", "split_bf16"):
+        esp, _ = ctx.rimp2_energy_from_3index(200, md, ed, Jd, Pd, prec)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        esp2, _ = ctx.rimp2_energy_from_3index(200, md, ed, Jd, Pd, prec)
+        t_split = time.perf_counter() - t0
+        assert esp2.e_total == esp.e_total  # fixed-order reductions: reproducible
+        # precision form within 1 uEh of the FP64 form
+        assert abs(esp.e_total - e64.e_total) <= 1e-6, (prec, esp, e64)
+        print(f"config3 time-to-E_corr from integrals ({prec}): {t_split * 1e3:.1f} ms, "
+              f"dE = {esp.e_total - e64.e_total:+.3e} Eh")

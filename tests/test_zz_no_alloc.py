@@ -19,7 +19,7 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 FP64_ABS, FP64_REL = 1e-10, 1e-12  # the FP64-form tolerance of the other tests
-PREC = {"fp64": 0, "split_bf16": 2}
+PREC = {"fp64": 0, "split_fp16": 1, "split_bf16": 2}
 
 
 def _regular(L, B, eps, o, v, X, prec):
@@ -35,7 +35,7 @@ def _regular(L, B, eps, o, v, X, prec):
         L.corr_destroy(h)
 
 
-@pytest.mark.parametrize("prec", ["fp64", "split_bf16"])
+@pytest.mark.parametrize("prec", ["fp64", "split_fp16", "split_bf16"])
 def test_noalloc_matches_regular_entry_point_twice(prec):
     import torch
 
