@@ -296,7 +296,7 @@ static void energy_carve(Carver& w, int nocc, int nvir, int Qp, bool tc, int gri
                          double** partials) {
   const long long R = (long long)nocc * nvir;
   if (tc) {
-    sw->S = static_cast<uint16_t*>(w.take((size_t)3 * R * Qp * 2));
+    sw->S = static_cast<uint16_t*>(w.take(slice_bytes(nocc, nvir, Qp)));
     sw->erow = static_cast<int*>(w.take((size_t)R * 4));
     sw->diag = static_cast<double*>(w.take((size_t)R * 8));
     sw->sc = static_cast<float*>(w.take((size_t)R * 4));
@@ -349,20 +349,13 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
   const int scheme = scheme_for_precision(precision);
   const int fmt = format_for_scheme(scheme);
   const int p = slice_bits_for(Qp);
-  CORR_CUDA(launch_slices(d_b, naux, R, Qp, scheme, fmt, p, sw, c->stream));
-  CUtensorMap tm;
-  const uint64_t dims[3] = {(uint64_t)Qp, (uint64_t)nvir, (uint64_t)3 * nocc};
-  const uint64_t strides[2] = {(uint64_t)Qp * 2, (uint64_t)nvir * Qp * 2};
-  const uint32_t box[3] = {32, (uint32_t)kTcTile, 1};
-  const CUtensorMapDataType dt =
-      fmt == 0 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
-  CORR_TRY(encode_tmap(&tm, dt, 3, sw.S, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_64B));
+  CORR_CUDA(launch_slices(d_b, naux, nocc, nvir, Qp, scheme, fmt, p, sw, c->stream));
   if (!c->attrs_set) {
     CORR_CUDA(prepare_energy_tc());
     c->attrs_set = true;
   }
   mark(c, 1);
-  CORR_CUDA(launch_energy_tc(tm, d_e, sw.sc, sw.dg, sw.scale, sh, Qp, fmt, scheme, partials,
+  CORR_CUDA(launch_energy_tc(sw.S, d_e, sw.sc, sw.dg, sw.scale, sh, Qp, fmt, scheme, partials,
                              grid, &c->dres->status, c->stream));
   mark(c, 2);
   CORR_CUDA(launch_energy_reduce(partials, grid, sw.scale, out_e, c->stream));

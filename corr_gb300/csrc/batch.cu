@@ -19,7 +19,6 @@ namespace {
 struct Plan {
   std::vector<int> order;           // table position -> caller index
   std::vector<BatchInst> table;     // host copy (device pointers filled)
-  std::vector<CUtensorMap> tmaps;
   long long total = 0;
 };
 
@@ -77,13 +76,13 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
   }
   // ---- workspace
   auto carve = [&](Carver& w, std::vector<SliceWork>& sws, double** unit_part, BatchInst** dtab,
-                   CUtensorMap** dmaps, int** dorder, unsigned long long** queue) {
+                   int** dorder, unsigned long long** queue) {
     sws.resize(n);
     for (int k = 0; k < n; ++k) {
       if (!tc) continue;
       const Shape& s = shp[k];
       SliceWork& sw = sws[k];
-      sw.S = static_cast<uint16_t*>(w.take((size_t)3 * s.R * s.Qp * 2));
+      sw.S = static_cast<uint16_t*>(w.take(slice_bytes(in[order[k]].nocc, in[order[k]].nvir, s.Qp)));
       sw.erow = static_cast<int*>(w.take((size_t)s.R * 4));
       sw.diag = static_cast<double*>(w.take((size_t)s.R * 8));
       sw.sc = static_cast<float*>(w.take((size_t)s.R * 4));
@@ -93,17 +92,15 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
     }
     *unit_part = static_cast<double*>(w.take((size_t)(tc ? total : (long long)c->sms * 2 * n) * 16));
     *dtab = static_cast<BatchInst*>(w.take(sizeof(BatchInst) * n));
-    *dmaps = static_cast<CUtensorMap*>(w.take(sizeof(CUtensorMap) * n));
     *dorder = static_cast<int*>(w.take(sizeof(int) * n));
     *queue = static_cast<unsigned long long*>(w.take(16));
   };
   std::vector<SliceWork> sws;
   double* unit_part;
   BatchInst* dtab;
-  CUtensorMap* dmaps;
   int* dorder;
   unsigned long long* queue;
-  carve(cv, sws, &unit_part, &dtab, &dmaps, &dorder, &queue);
+  carve(cv, sws, &unit_part, &dtab, &dorder, &queue);
   if (c->ws.cap < cv.used) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     cudaStreamIsCapturing(c->stream, &cs);
@@ -114,7 +111,7 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
   }
   CORR_TRY(c->ws.reserve(cv.used));
   Carver w{c->ws.ptr, 0};
-  carve(w, sws, &unit_part, &dtab, &dmaps, &dorder, &queue);
+  carve(w, sws, &unit_part, &dtab, &dorder, &queue);
 
   if (!tc) {
     // FP64 comparison form: one fused kernel per instance
@@ -135,26 +132,19 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
   // ---- per-instance slicing and the host copy of the table
   const int scheme = scheme_for_precision(precision);
   const int fmt = format_for_scheme(scheme);
-  const size_t hbytes = sizeof(BatchInst) * n + sizeof(CUtensorMap) * n + sizeof(int) * n + 256;
+  const size_t hbytes = sizeof(BatchInst) * n + sizeof(int) * n + 256;
   CORR_TRY(grow_pinned(c, hbytes));
   char* hp = static_cast<char*>(c->pinned);
   BatchInst* htab = reinterpret_cast<BatchInst*>(hp);
-  CUtensorMap* hmaps = reinterpret_cast<CUtensorMap*>(
-      hp + ((sizeof(BatchInst) * n + 127) & ~(size_t)127));
-  int* horder = reinterpret_cast<int*>(reinterpret_cast<char*>(hmaps) + sizeof(CUtensorMap) * n);
+  int* horder = reinterpret_cast<int*>(hp + ((sizeof(BatchInst) * n + 127) & ~(size_t)127));
   long long ub = 0;
   for (int k = 0; k < n; ++k) {
     const corr_rimp2_instance& x = in[order[k]];
     const Shape& s = shp[k];
-    CORR_CUDA(launch_slices(x.bia, x.naux, s.R, s.Qp, scheme, fmt, s.p, sws[k], c->stream));
-    const uint64_t dims[3] = {(uint64_t)s.Qp, (uint64_t)x.nvir, (uint64_t)3 * x.nocc};
-    const uint64_t strides[2] = {(uint64_t)s.Qp * 2, (uint64_t)x.nvir * s.Qp * 2};
-    const uint32_t box[3] = {32, (uint32_t)kTcTile, 1};
-    CORR_TRY(encode_tmap(&hmaps[k],
-                         fmt == 0 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
-                                  : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
-                         3, sws[k].S, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_64B));
+    CORR_CUDA(launch_slices(x.bia, x.naux, x.nocc, x.nvir, s.Qp, scheme, fmt, s.p, sws[k],
+                            c->stream));
     BatchInst& b = htab[k];
+    b.S = sws[k].S;
     b.eps = x.eps;
     b.sc = sws[k].sc;
     b.dg = sws[k].dg;
@@ -171,8 +161,6 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
   }
   c->launches += 3LL * n;
   CORR_CUDA(cudaMemcpyAsync(dtab, htab, sizeof(BatchInst) * n, cudaMemcpyHostToDevice, c->stream));
-  CORR_CUDA(cudaMemcpyAsync(dmaps, hmaps, sizeof(CUtensorMap) * n, cudaMemcpyHostToDevice,
-                            c->stream));
   CORR_CUDA(cudaMemcpyAsync(dorder, horder, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
   CORR_CUDA(cudaMemsetAsync(queue, 0, 8, c->stream));
   if (!c->batch_attrs_set) {
@@ -182,7 +170,7 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
   int grid = c->sms;
   if ((long long)grid > total) grid = (int)total;
   mark(c, 1);
-  CORR_CUDA(launch_energy_batch(dtab, dmaps, n, total, queue, fmt, scheme, stages, grid,
+  CORR_CUDA(launch_energy_batch(dtab, n, total, queue, fmt, scheme, stages, grid,
                                 unit_part, &c->dres->status, c->stream));
   mark(c, 2);
   CORR_CUDA(launch_batch_reduce(dtab, n, unit_part, dorder, out, c->stream));

@@ -9,6 +9,7 @@ namespace corr {
 
 // Device-side description of one instance of a batch.
 struct BatchInst {
+  const uint16_t* S;    // digit planes in the tiled layout (kernels.h)
   const double* eps;    // [o+v]
   const float* sc;      // [o*v] row factors 2^(e_r - e_ref)
   const float* dg;      // [o*v] FP64 diagonal in scaled units
@@ -20,7 +21,7 @@ struct BatchInst {
 
 size_t batch_kernel_smem(int stages);
 cudaError_t prepare_energy_batch();
-cudaError_t launch_energy_batch(const BatchInst* insts, const CUtensorMap* tmaps, int ninst,
+cudaError_t launch_energy_batch(const BatchInst* insts, int ninst,
                                 long long total, unsigned long long* queue, int fmt, int scheme,
                                 int stages, int grid, double* unit_part, int* status,
                                 cudaStream_t s);

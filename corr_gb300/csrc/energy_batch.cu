@@ -87,7 +87,7 @@ __device__ __forceinline__ UnitInfo unit_info(const BatchInst* __restrict__ in, 
 
 template <int STAGES, int SCHEME>
 __global__ void __launch_bounds__(NTHREADS, 1)
-    energy_batch_kernel(const BatchInst* __restrict__ insts, const CUtensorMap* __restrict__ tmaps,
+    energy_batch_kernel(const BatchInst* __restrict__ insts,
                         int ninst, long long total, unsigned long long* __restrict__ queue,
                         uint32_t idesc, double* __restrict__ unit_part, int* status) {
   using Ctl = BCtl<STAGES>;
@@ -139,8 +139,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         if (u < 0) break;
         const UnitInfo ui = unit_info(insts, ninst, u);
         const BatchInst& bi = insts[ui.inst];
-        const CUtensorMap* tm = tmaps + ui.inst;
-        const int A0 = ui.A * TILE, B0 = ui.B * TILE;
         const int nph = (ui.i == ui.j || ui.A == ui.B) ? 1 : 2;
         for (int phs = 0; phs < nph && ok; ++phs) {
           const int x = phs == 0 ? ui.i : ui.j;
@@ -153,11 +151,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             uint64_t* bar = &ctl->full[st];
             mbar_expect_tx(bar, STAGE_BYTES);
             uint8_t* sb = tiles + (size_t)st * STAGE_BYTES;
-            const int k0 = kb * KB;
 #pragma unroll
             for (int l = 0; l < 3; ++l) {
-              tma_load_3d(sb + (2 * l) * TILE_BYTES, tm, bar, k0, A0, l * bi.o + x);
-              tma_load_3d(sb + (2 * l + 1) * TILE_BYTES, tm, bar, k0, B0, l * bi.o + y);
+              bulk_load(sb + (2 * l) * TILE_BYTES,
+                        bi.S + slice_tile_offset(l, x, kb, ui.A, bi.o, bi.nkb, bi.ntiles),
+                        TILE_BYTES, bar);
+              bulk_load(sb + (2 * l + 1) * TILE_BYTES,
+                        bi.S + slice_tile_offset(l, y, kb, ui.B, bi.o, bi.nkb, bi.ntiles),
+                        TILE_BYTES, bar);
             }
             has[st] = true;
             last_ph[st] = ph;
@@ -459,14 +460,14 @@ cudaError_t prepare_energy_batch() {
 }
 
 template <int STAGES, int SCHEME>
-static void launch_batch_variant(const BatchInst* insts, const CUtensorMap* tmaps, int ninst,
+static void launch_batch_variant(const BatchInst* insts, int ninst,
                                  long long total, unsigned long long* queue, uint32_t idesc,
                                  int grid, double* unit_part, int* status, cudaStream_t s) {
   energy_batch_kernel<STAGES, SCHEME><<<grid, NTHREADS, batch_smem_bytes<STAGES>(), s>>>(
-      insts, tmaps, ninst, total, queue, idesc, unit_part, status);
+      insts, ninst, total, queue, idesc, unit_part, status);
 }
 
-cudaError_t launch_energy_batch(const BatchInst* insts, const CUtensorMap* tmaps, int ninst,
+cudaError_t launch_energy_batch(const BatchInst* insts, int ninst,
                                 long long total, unsigned long long* queue, int fmt, int scheme,
                                 int stages, int grid, double* unit_part, int* status,
                                 cudaStream_t s) {
@@ -474,17 +475,17 @@ cudaError_t launch_energy_batch(const BatchInst* insts, const CUtensorMap* tmaps
   const bool kara = scheme == kSchemeKara;
   if (stages == 3) {
     if (kara)
-      launch_batch_variant<3, kSchemeKara>(insts, tmaps, ninst, total, queue, idesc, grid,
+      launch_batch_variant<3, kSchemeKara>(insts, ninst, total, queue, idesc, grid,
                                            unit_part, status, s);
     else
-      launch_batch_variant<3, kSchemeDigits3>(insts, tmaps, ninst, total, queue, idesc, grid,
+      launch_batch_variant<3, kSchemeDigits3>(insts, ninst, total, queue, idesc, grid,
                                               unit_part, status, s);
   } else {
     if (kara)
-      launch_batch_variant<4, kSchemeKara>(insts, tmaps, ninst, total, queue, idesc, grid,
+      launch_batch_variant<4, kSchemeKara>(insts, ninst, total, queue, idesc, grid,
                                            unit_part, status, s);
     else
-      launch_batch_variant<4, kSchemeDigits3>(insts, tmaps, ninst, total, queue, idesc, grid,
+      launch_batch_variant<4, kSchemeDigits3>(insts, ninst, total, queue, idesc, grid,
                                               unit_part, status, s);
   }
   return cudaGetLastError();

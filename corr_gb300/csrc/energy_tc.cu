@@ -1,7 +1,9 @@
 // Precision-form fused RI-MP2 energy on the 5th-generation tensor cores.
 //
-// Input: the three 16-bit integer planes of B (split.cu), as one array
-// S[l][i][a][Qp] read through a 3-D TMA map over [3*nocc][nvir][Qp].
+// Input: the three 16-bit integer planes of B (split.cu) in the tiled
+// layout of kernels.h: every 128 x 32 operand tile is one contiguous,
+// pre-swizzled 8 KB block fetched with a linear bulk copy (whole 128-byte
+// lines from L2).
 // Work unit = (occupied pair i<=j, virtual tile pair A<=B), tiles of 128.
 //
 // Phase 1 forms D1[a][b] = (ia|jb) for a in A, b in B; phase 2 forms
@@ -20,7 +22,7 @@
 // with 1/D as an IEEE-rounded FP32 reciprocal and FP64 sums per unit.
 //
 // CTA = 6 warps, persistent, one CTA per SM:
-//   warp 0     TMA producer (one thread), 6 tiles of 128x32 per stage, 4 stages
+//   warp 0     bulk-copy producer (one thread), 6 tiles of 128x32 per stage, 4 stages
 //   warp 1     TMEM owner + MMA issuer (one thread), tcgen05.mma kind::f16
 //   warps 2-5  epilogue, one TMEM lane quarter each
 // Every wait is bounded (common.cuh); on a timeout the CTA winds down and the
@@ -70,7 +72,7 @@ __device__ __forceinline__ void unit_decode(long long u, const EnergyShape& sh, 
 
 template <int SCHEME>
 __global__ void __launch_bounds__(NTHREADS, 1)
-    energy_tc_kernel(const __grid_constant__ CUtensorMap tm, const double* __restrict__ eps,
+    energy_tc_kernel(const uint16_t* __restrict__ S, const double* __restrict__ eps,
                      const float* __restrict__ sc, const float* __restrict__ dg,
                      const double* __restrict__ scale, EnergyShape sh, int nkb, uint32_t idesc,
                      double* __restrict__ partials, int* status) {
@@ -102,7 +104,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == 0) {
     // ------------------------------------------------------------ producer
     if (lane == 0) {
-      prefetch_tmap(&tm);
       int st = 0;
       uint32_t ph = 0;
       uint32_t last_ph[STAGES];
@@ -112,7 +113,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       for (long long u = blockIdx.x; u < sh.nunits && ok; u += gridDim.x) {
         int i, j, A, B;
         unit_decode(u, sh, &i, &j, &A, &B);
-        const int A0 = A * TILE, B0 = B * TILE;
         const int nph = (i == j || A == B) ? 1 : 2;
         for (int phs = 0; phs < nph && ok; ++phs) {
           const int x = phs == 0 ? i : j;  // row operand slab
@@ -125,11 +125,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             uint64_t* bar = &ctl->full[st];
             mbar_expect_tx(bar, STAGE_BYTES);
             uint8_t* sb = tiles + (size_t)st * STAGE_BYTES;
-            const int k0 = kb * KB;
 #pragma unroll
             for (int l = 0; l < 3; ++l) {
-              tma_load_3d(sb + (2 * l) * TILE_BYTES, &tm, bar, k0, A0, l * o + x);
-              tma_load_3d(sb + (2 * l + 1) * TILE_BYTES, &tm, bar, k0, B0, l * o + y);
+              bulk_load(sb + (2 * l) * TILE_BYTES,
+                        S + slice_tile_offset(l, x, kb, A, o, nkb, sh.ntiles), TILE_BYTES, bar);
+              bulk_load(sb + (2 * l + 1) * TILE_BYTES,
+                        S + slice_tile_offset(l, y, kb, B, o, nkb, sh.ntiles), TILE_BYTES, bar);
             }
             has[st] = true;
             last_ph[st] = ph;
@@ -375,17 +376,17 @@ cudaError_t prepare_energy_tc() {
                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
 }
 
-cudaError_t launch_energy_tc(const CUtensorMap& tmap, const double* eps, const float* sc,
+cudaError_t launch_energy_tc(const uint16_t* S, const double* eps, const float* sc,
                              const float* dg, const double* scale, const EnergyShape& sh, int Qp,
                              int fmt, int scheme, double* partials, int grid, int* status,
                              cudaStream_t s) {
   const uint32_t idesc = idesc_f16((uint32_t)fmt, TILE, TILE);
   if (scheme == kSchemeKara)
     energy_tc_kernel<kSchemeKara><<<grid, NTHREADS, kSmemBytes, s>>>(
-        tmap, eps, sc, dg, scale, sh, Qp / KB, idesc, partials, status);
+        S, eps, sc, dg, scale, sh, Qp / KB, idesc, partials, status);
   else
     energy_tc_kernel<kSchemeDigits3><<<grid, NTHREADS, kSmemBytes, s>>>(
-        tmap, eps, sc, dg, scale, sh, Qp / KB, idesc, partials, status);
+        S, eps, sc, dg, scale, sh, Qp / KB, idesc, partials, status);
   return cudaGetLastError();
 }
 

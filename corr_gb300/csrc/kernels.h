@@ -22,8 +22,23 @@ EnergyShape make_energy_shape(int nocc, int nvir, int naux, int tile);
 
 // ---- slice pre-pass (split.cu) ---------------------------------------------
 // Device buffers of the precision form's pre-pass (R = nocc*nvir rows).
+// Tiled digit layout read by the energy kernels: plane l, occupied i, 32-wide
+// Q block kb, 128-row virtual tile A -> one 8 KB tile of 128 rows x 32 Q
+// (16-bit), stored as the 64-byte-swizzled shared-memory image (the 16-byte
+// chunk c of row r sits at chunk c ^ ((r >> 1) & 3)).  Offsets in elements.
+__host__ __device__ inline size_t slice_tile_offset(int l, int i, int kb, int A, int nocc,
+                                                    int nkb, int ntiles) {
+  return ((((size_t)l * nocc + i) * nkb + kb) * ntiles + A) * 4096;
+}
+__host__ __device__ inline size_t slice_chunk_offset(int row, int chunk) {
+  return (size_t)row * 32 + (size_t)((chunk ^ ((row >> 1) & 3)) * 8);
+}
+inline size_t slice_bytes(int nocc, int nvir, int Qp) {
+  return (size_t)3 * nocc * (Qp / 32) * ((nvir + 127) / 128) * 8192;
+}
+
 struct SliceWork {
-  uint16_t* S;     // [3][R][Qp] integer slices (fp16 or bf16 encoding)
+  uint16_t* S;     // 3 digit planes in the tiled layout (fp16 or bf16 encoding)
   int* erow;       // [R] row exponents
   double* diag;    // [R] FP64 sum_Q B^2
   float* sc;       // [R] 2^(e_r - e_ref)
@@ -40,18 +55,17 @@ inline int scheme_for_precision(int precision) {
 }
 inline int format_for_scheme(int scheme) { return scheme == kSchemeKara ? 0 : 1; }  // 0 FP16
 int slice_bits_for(int Qp);
-cudaError_t launch_slices(const double* b, int naux, long long R, int Qp, int scheme, int fmt,
-                          int p, SliceWork w, cudaStream_t s);
+cudaError_t launch_slices(const double* b, int naux, int nocc, int nvir, int Qp, int scheme,
+                          int fmt, int p, SliceWork w, cudaStream_t s);
 // Sum per-CTA partial pairs {os, ss} in fixed order, times `scale` (device),
 // into out[4] = {E_SS, E_OS, E, E_SCS}.
 cudaError_t launch_energy_reduce(const double* partials, int n, const double* scale, double* out,
                                  cudaStream_t s);
 
 // ---- fused energy kernels ---------------------------------------------------
-// tcgen05 precision form (energy_tc.cu).  tmap: 3-D map over the slice
-// array viewed as [3*nocc][nvir][Qp] (16-bit), box {32, 128, 1}, 64B swizzle.
+// tcgen05 precision form (energy_tc.cu) over the tiled digit planes S.
 // scale: the SliceWork scale pair (the kernel reads 1/L from scale[1]).
-cudaError_t launch_energy_tc(const CUtensorMap& tmap, const double* eps, const float* sc,
+cudaError_t launch_energy_tc(const uint16_t* S, const double* eps, const float* sc,
                              const float* dg, const double* scale, const EnergyShape& sh, int Qp,
                              int fmt, int scheme, double* partials, int grid, int* status,
                              cudaStream_t s);

@@ -130,7 +130,7 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
       sw->dg = static_cast<float*>(w.take((size_t)R * 4));
       sw->eref = static_cast<int*>(w.take(16));
       sw->scale = static_cast<double*>(w.take(16));
-      sw->S = static_cast<uint16_t*>(w.take((size_t)3 * R * Qp * 2));
+      sw->S = static_cast<uint16_t*>(w.take(slice_bytes(nocc, nvir, Qp)));
     }
   };
   Header* hdr;
@@ -157,16 +157,8 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
     const int scheme = scheme_for_precision(precision);
     const int fmt = format_for_scheme(scheme);
     const int p = slice_bits_for(Qp);
-    CORR_CUDA(launch_slices(bia, naux, R, Qp, scheme, fmt, p, sw, s));
-    CUtensorMap tm;
-    const uint64_t dims[3] = {(uint64_t)Qp, (uint64_t)nvir, (uint64_t)3 * nocc};
-    const uint64_t strides[2] = {(uint64_t)Qp * 2, (uint64_t)nvir * Qp * 2};
-    const uint32_t box[3] = {32, (uint32_t)kTcTile, 1};
-    CORR_TRY(encode_tmap(&tm,
-                         fmt == 0 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
-                                  : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
-                         3, sw.S, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_64B));
-    CORR_CUDA(launch_energy_tc(tm, eps, sw.sc, sw.dg, sw.scale, sh, Qp, fmt, scheme, partials,
+    CORR_CUDA(launch_slices(bia, naux, nocc, nvir, Qp, scheme, fmt, p, sw, s));
+    CORR_CUDA(launch_energy_tc(sw.S, eps, sw.sc, sw.dg, sw.scale, sh, Qp, fmt, scheme, partials,
                                grid, &hdr->status, s));
     CORR_CUDA(launch_energy_reduce(partials, grid, sw.scale, hdr->e, s));
   }

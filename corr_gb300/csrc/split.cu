@@ -242,120 +242,94 @@ __device__ __forceinline__ uint16_t to16i(int v) {
   return __bfloat16_as_ushort(__int2bfloat16_rn(v));
 }
 
-// B[Q][r] -> slices S[l][r][Qp], l = 0..2, zero padded for Q >= naux.
-// Block = 256 threads on a 64 (Q) x 64 (r) tile: reads are coalesced along r
-// (the reference layout), each thread then converts 16 consecutive Q of one r
-// and writes 32 contiguous bytes per slice plane.  Digit extraction is integer
-// arithmetic: X = round(B 2^(2(p+1) - e_r)), s0 = round(X / L^2),
-// s1 = round((X - s0 L^2) / L), s2 = remainder.
-template <int FMT>
+// B[Q][r] -> digit planes in the tiled layout of the energy kernels
+// (kernels.h, slice_tile_offset): one 8 KB tile per (plane, i, 32-Q block,
+// 128-row virtual tile), each stored exactly as the 64-byte-swizzled shared
+// memory image the tensor-core descriptors read, so the kernels fetch a
+// tile with one linear bulk copy.  Rows a >= nvir of the last tile and
+// Q >= naux are zero.
+//
+// Block = 256 threads on a 64 (padded row) x 64 (Q) tile: reads coalesced
+// along r, then each thread converts 16 consecutive Q of one row and stores
+// two 16-byte chunks per plane.  Digits by integer arithmetic on the IEEE
+// fields: scheme 0 (levels) X = round(B 2^(2(p+1) - e_r)), s0 = round(X/L^2),
+// s1 = round((X - s0 L^2)/L), s2 = remainder; scheme 1 (Karatsuba) as
+// kara_digits, planes s0, s0 + s1, s1.
+template <int SCHEME, int FMT>
 __global__ void __launch_bounds__(256) slice_kernel(const double* __restrict__ b, int naux,
-                                                    long long R, int Qp, int p,
+                                                    int nocc, int nvir, int Qp, int p,
                                                     const int* __restrict__ erow,
+                                                    const int* __restrict__ kglob,
                                                     uint16_t* __restrict__ S) {
   __shared__ double tile[64][65];
   const int t = threadIdx.x;
+  const int ntiles = (nvir + 127) / 128, vp = ntiles * 128;
+  const long long R = (long long)nocc * nvir, Rp = (long long)nocc * vp;
   const long long r0 = (long long)blockIdx.x * 64;
   const int q0 = blockIdx.y * 64;
   {
     const int c = t & 63;
+    const long long rp = r0 + c;
+    const int i = (int)(rp / vp), a = (int)(rp % vp);
+    const bool real = rp < Rp && a < nvir;
+    const long long r = (long long)i * nvir + a;
 #pragma unroll 4
     for (int k = t >> 6; k < 64; k += 4) {
       const int q = q0 + k;
-      const long long r = r0 + c;
-      tile[k][c] = (q < naux && r < R) ? b[(long long)q * R + r] : 0.0;
+      tile[k][c] = (q < naux && real) ? b[(long long)q * R + r] : 0.0;
     }
   }
   __syncthreads();
   const int rl = t >> 2, qc = (t & 3) * 16;
-  const long long r = r0 + rl;
-  if (r >= R || q0 + qc >= Qp) return;
-  const int e = erow[r];
+  const long long rp = r0 + rl;
+  if (rp >= Rp || q0 + qc >= Qp) return;
+  const int i = (int)(rp / vp), a = (int)(rp % vp);
+  const int e = a < nvir ? erow[(long long)i * nvir + a] : INT_MIN / 4;
   const bool live = e > INT_MIN / 8;
-  const int lb = p + 1;            // bits per level
-  const int k2 = 2 * lb - e;       // X = B 2^k2
   __align__(16) uint16_t h0[16];
   __align__(16) uint16_t h1[16];
   __align__(16) uint16_t h2[16];
+  if (SCHEME == kSchemeKara) {
+    const int k = live ? *kglob : 0;
 #pragma unroll
-  for (int k = 0; k < 16; ++k) {
-    const int X = live ? round_scaled(tile[qc + k][rl], k2) : 0;
-    const int s0 = (X + (1 << (2 * lb - 1))) >> (2 * lb);
-    const int rem = X - (s0 << (2 * lb));
-    const int s1 = (rem + (1 << (lb - 1))) >> lb;
-    const int s2 = rem - (s1 << lb);
-    h0[k] = to16i<FMT>(s0);
-    h1[k] = to16i<FMT>(s1);
-    h2[k] = to16i<FMT>(s2);
-  }
-  const size_t plane = (size_t)R * Qp;
-  const size_t at = (size_t)r * Qp + q0 + qc;  // 16 x 2 B, 32-byte aligned (Qp % 32 == 0)
-  uint4* d0 = reinterpret_cast<uint4*>(S + at);
-  uint4* d1 = reinterpret_cast<uint4*>(S + plane + at);
-  uint4* d2 = reinterpret_cast<uint4*>(S + 2 * plane + at);
-  const uint4* v0 = reinterpret_cast<const uint4*>(h0);
-  const uint4* v1 = reinterpret_cast<const uint4*>(h1);
-  const uint4* v2 = reinterpret_cast<const uint4*>(h2);
-  d0[0] = v0[0];
-  d0[1] = v0[1];
-  d1[0] = v1[0];
-  d1[1] = v1[1];
-  d2[0] = v2[0];
-  d2[1] = v2[1];
-}
-
-// Scheme 1 slices: planes S[0] = s0, S[1] = u = s0 + s1, S[2] = s1 (FP16),
-// same tiling and store pattern as slice_kernel.
-__global__ void __launch_bounds__(256) slice_kara_kernel(const double* __restrict__ b, int naux,
-                                                         long long R, int Qp,
-                                                         const int* __restrict__ erow,
-                                                         const int* __restrict__ kglob,
-                                                         uint16_t* __restrict__ S) {
-  __shared__ double tile[64][65];
-  const int t = threadIdx.x;
-  const long long r0 = (long long)blockIdx.x * 64;
-  const int q0 = blockIdx.y * 64;
-  {
-    const int c = t & 63;
-#pragma unroll 4
-    for (int k = t >> 6; k < 64; k += 4) {
-      const int q = q0 + k;
-      const long long r = r0 + c;
-      tile[k][c] = (q < naux && r < R) ? b[(long long)q * R + r] : 0.0;
+    for (int j = 0; j < 16; ++j) {
+      int s0 = 0, s1 = 0;
+      if (live) kara_digits(round_scaled64(tile[qc + j][rl], 24 - e), k, &s0, &s1);
+      h0[j] = to16i<FMT>(s0);
+      h1[j] = to16i<FMT>(s0 + s1);
+      h2[j] = to16i<FMT>(s1);
+    }
+  } else {
+    const int lb = p + 1;       // bits per level
+    const int k2 = 2 * lb - e;  // X = B 2^k2
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const int X = live ? round_scaled(tile[qc + j][rl], k2) : 0;
+      const int s0 = (X + (1 << (2 * lb - 1))) >> (2 * lb);
+      const int rem = X - (s0 << (2 * lb));
+      const int s1 = (rem + (1 << (lb - 1))) >> lb;
+      const int s2 = rem - (s1 << lb);
+      h0[j] = to16i<FMT>(s0);
+      h1[j] = to16i<FMT>(s1);
+      h2[j] = to16i<FMT>(s2);
     }
   }
-  __syncthreads();
-  const int rl = t >> 2, qc = (t & 3) * 16;
-  const long long r = r0 + rl;
-  if (r >= R || q0 + qc >= Qp) return;
-  const int e = erow[r];
-  const bool live = e > INT_MIN / 8;
-  const int k = *kglob;
-  __align__(16) uint16_t h0[16];
-  __align__(16) uint16_t h1[16];
-  __align__(16) uint16_t h2[16];
-#pragma unroll
-  for (int j = 0; j < 16; ++j) {
-    int s0 = 0, s1 = 0;
-    if (live) kara_digits(round_scaled64(tile[qc + j][rl], 24 - e), k, &s0, &s1);
-    h0[j] = to16i<0>(s0);
-    h1[j] = to16i<0>(s0 + s1);
-    h2[j] = to16i<0>(s1);
-  }
-  const size_t plane = (size_t)R * Qp;
-  const size_t at = (size_t)r * Qp + q0 + qc;
-  uint4* d0 = reinterpret_cast<uint4*>(S + at);
-  uint4* d1 = reinterpret_cast<uint4*>(S + plane + at);
-  uint4* d2 = reinterpret_cast<uint4*>(S + 2 * plane + at);
+  const int q = q0 + qc;
+  const int nkb = Qp / 32, kb = q / 32, c0 = (q % 32) / 8;
+  const size_t plane = (size_t)nocc * nkb * ntiles * 4096;
+  const size_t base = slice_tile_offset(0, i, kb, a / 128, nocc, nkb, ntiles);
+  const int row = a % 128;
+  const size_t at0 = base + slice_chunk_offset(row, c0);
+  const size_t at1 = base + slice_chunk_offset(row, c0 + 1);
   const uint4* v0 = reinterpret_cast<const uint4*>(h0);
   const uint4* v1 = reinterpret_cast<const uint4*>(h1);
   const uint4* v2 = reinterpret_cast<const uint4*>(h2);
-  d0[0] = v0[0];
-  d0[1] = v0[1];
-  d1[0] = v1[0];
-  d1[1] = v1[1];
-  d2[0] = v2[0];
-  d2[1] = v2[1];
+  *reinterpret_cast<uint4*>(S + at0) = v0[0];
+  *reinterpret_cast<uint4*>(S + at1) = v0[1];
+  *reinterpret_cast<uint4*>(S + plane + at0) = v1[0];
+  *reinterpret_cast<uint4*>(S + plane + at1) = v1[1];
+  *reinterpret_cast<uint4*>(S + 2 * plane + at0) = v2[0];
+  *reinterpret_cast<uint4*>(S + 2 * plane + at1) = v2[1];
 }
 
 // Per-row FP32 factors for the energy kernel: sc_r = 2^(e_r - e_ref) and the
@@ -425,25 +399,30 @@ int slice_bits_for(int Qp) {
   return p;
 }
 
-cudaError_t launch_slices(const double* b, int naux, long long R, int Qp, int scheme, int fmt,
-                          int p, SliceWork w, cudaStream_t s) {
+cudaError_t launch_slices(const double* b, int naux, int nocc, int nvir, int Qp, int scheme,
+                          int fmt, int p, SliceWork w, cudaStream_t s) {
+  const long long R = (long long)nocc * nvir;
   cudaError_t e = cudaMemsetAsync(w.eref, 0x80, sizeof(int), s);  // very negative start
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(w.eref + 1, 0x7f, sizeof(int), s);  // level exponent: min-reduced
   if (e != cudaSuccess) return e;
-  dim3 grid((unsigned)((R + 63) / 64), (unsigned)((Qp + 63) / 64));
+  const long long Rp = (long long)nocc * ((nvir + 127) / 128) * 128;
+  dim3 grid((unsigned)((Rp + 63) / 64), (unsigned)((Qp + 63) / 64));
   if (scheme == kSchemeKara) {
     rowstat_kara_kernel<<<(unsigned)((R + 31) / 32), dim3(32, 8), 0, s>>>(b, naux, R, w.erow,
                                                                           w.diag, w.eref,
                                                                           w.eref + 1);
-    slice_kara_kernel<<<grid, 256, 0, s>>>(b, naux, R, Qp, w.erow, w.eref + 1, w.S);
+    slice_kernel<kSchemeKara, 0><<<grid, 256, 0, s>>>(b, naux, nocc, nvir, Qp, p, w.erow,
+                                                      w.eref + 1, w.S);
   } else {
     rowstat_kernel<<<(unsigned)((R + 31) / 32), dim3(32, 8), 0, s>>>(b, naux, R, p, w.erow,
                                                                      w.diag, w.eref);
     if (fmt == 0)
-      slice_kernel<0><<<grid, 256, 0, s>>>(b, naux, R, Qp, p, w.erow, w.S);
+      slice_kernel<kSchemeDigits3, 0><<<grid, 256, 0, s>>>(b, naux, nocc, nvir, Qp, p, w.erow,
+                                                           w.eref + 1, w.S);
     else
-      slice_kernel<1><<<grid, 256, 0, s>>>(b, naux, R, Qp, p, w.erow, w.S);
+      slice_kernel<kSchemeDigits3, 1><<<grid, 256, 0, s>>>(b, naux, nocc, nvir, Qp, p, w.erow,
+                                                           w.eref + 1, w.S);
   }
   rowfactor_kernel<<<(unsigned)((R + 255) / 256 < 1024 ? (R + 255) / 256 : 1024), 256, 0, s>>>(
       w.erow, w.diag, R, w.eref, scheme == kSchemeKara ? -1 : p + 1, w.sc, w.dg, w.scale);
