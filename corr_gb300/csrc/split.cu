@@ -105,29 +105,66 @@ __device__ __forceinline__ int ceil_log2(double y) {
 
 constexpr int kKaraMaxK = 10;
 
+// Row statistics are taken by blocks of 32 rows x QG Q-groups: for a fixed
+// Q the 32 threads of a warp read 32 consecutive rows (coalesced), and every
+// thread keeps kUnroll independent loads in flight.
+constexpr int QG = 32;
+constexpr int kUnroll = 4;
+
+// Pass 1 over one row slice: max |B| (as IEEE bits) and sum B^2 (FP64).
+__device__ __forceinline__ void row_pass1(const double* __restrict__ b, int naux, long long R,
+                                          long long r, int ty, unsigned long long* mo,
+                                          double* so) {
+  unsigned long long m[kUnroll] = {};
+  double s[kUnroll] = {};
+  int q = ty;
+  for (; q + (kUnroll - 1) * QG < naux; q += kUnroll * QG) {
+    double x[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) x[u] = b[(long long)(q + u * QG) * R + r];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      const unsigned long long ax = abs_bits(x[u]);
+      m[u] = ax > m[u] ? ax : m[u];
+      s[u] = fma(x[u], x[u], s[u]);
+    }
+  }
+  for (; q < naux; q += QG) {
+    const double x = b[(long long)q * R + r];
+    const unsigned long long ax = abs_bits(x);
+    m[0] = ax > m[0] ? ax : m[0];
+    s[0] = fma(x, x, s[0]);
+  }
+  unsigned long long mm = m[0];
+  double ss = s[0];
+#pragma unroll
+  for (int u = 1; u < kUnroll; ++u) {
+    mm = m[u] > mm ? m[u] : mm;
+    ss += s[u];
+  }
+  *mo = mm;
+  *so = ss;
+}
+
 // Scheme 1: per row r, e_r and the FP64 diagonal (first pass), then the
-// digit statistics of the second pass and the largest admissible level
-// exponent k_r (global minimum by atomicMin into kglob).  Block = 32 rows x
-// 8 Q-groups.
-__global__ void rowstat_kara_kernel(const double* __restrict__ b, int naux, long long R,
-                                    int* __restrict__ erow, double* __restrict__ diag, int* eref,
-                                    int* kglob) {
-  __shared__ unsigned long long smax[8][32];
-  __shared__ double ssum[8][32];
-  __shared__ double sb[8][32], scc[8][32];
-  __shared__ int sa[8][32], sm0[8][32];
+// digit statistics of the second pass (a re-read that the L2 serves: a
+// block's rows were read just before) and the largest admissible level
+// exponent k_r, min-reduced into kglob.  Block = 32 rows x QG Q-groups.
+__global__ void __launch_bounds__(32 * QG) rowstat_kara_kernel(const double* __restrict__ b,
+                                                               int naux, long long R,
+                                                               int* __restrict__ erow,
+                                                               double* __restrict__ diag,
+                                                               int* eref, int* kglob) {
+  __shared__ unsigned long long smax[QG][32];
+  __shared__ double ssum[QG][32];
+  __shared__ float sb[QG][32], scc[QG][32];
+  __shared__ int sa[QG][32], sm0[QG][32];
   __shared__ int se[32];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const long long r = (long long)blockIdx.x * 32 + tx;
   unsigned long long m = 0;
   double s = 0.0;
-  if (r < R)
-    for (int q = ty; q < naux; q += 8) {
-      const double x = b[(long long)q * R + r];
-      const unsigned long long ax = abs_bits(x);
-      m = ax > m ? ax : m;
-      s = fma(x, x, s);
-    }
+  if (r < R) row_pass1(b, naux, R, r, ty, &m, &s);
   smax[ty][tx] = m;
   ssum[ty][tx] = s;
   __syncthreads();
@@ -135,7 +172,7 @@ __global__ void rowstat_kara_kernel(const double* __restrict__ b, int naux, long
   if (ty == 0) {
     int e = INT_MIN / 4;
     if (r < R) {
-      for (int k = 1; k < 8; ++k) {
+      for (int k = 1; k < QG; ++k) {
         m = smax[k][tx] > m ? smax[k][tx] : m;
         s += ssum[k][tx];
       }
@@ -158,8 +195,9 @@ __global__ void rowstat_kara_kernel(const double* __restrict__ b, int naux, long
   const bool live = r < R && e > INT_MIN / 8;
   int a = 0, m0 = 0;
   float bb = 0.f, cc = 0.f;
-  if (live)
-    for (int q = ty; q < naux; q += 8) {
+  if (live) {
+#pragma unroll 4
+    for (int q = ty; q < naux; q += QG) {
       const long long X24 = round_scaled64(b[(long long)q * R + r], 24 - e);
       const long long h = (X24 + (1ll << 23)) >> 24;
       const float rf = (float)(int)(X24 - (h << 24));
@@ -169,20 +207,21 @@ __global__ void rowstat_kara_kernel(const double* __restrict__ b, int naux, long
       bb = fmaf((float)s0, rf, bb);
       cc = fmaf(rf, rf, cc);
     }
+  }
   sa[ty][tx] = a;
   sm0[ty][tx] = m0;
-  sb[ty][tx] = (double)bb;
-  scc[ty][tx] = (double)cc;
+  sb[ty][tx] = bb;
+  scc[ty][tx] = cc;
   __syncthreads();
   if (ty == 0 && live) {
     double bsum = 0.0, csum = 0.0;
-    for (int k = 0; k < 8; ++k) {
+    for (int k = 0; k < QG; ++k) {
       if (k) {
         a += sa[k][tx];
         m0 = max(m0, sm0[k][tx]);
       }
-      bsum += sb[k][tx];
-      csum += scc[k][tx];
+      bsum += (double)sb[k][tx];
+      csum += (double)scc[k][tx];
     }
     const double A = (double)a, Bx = bsum * 0x1p-24, C = csum * 0x1p-48;
     const double marg = 1.0 + 0x1p-10;
@@ -200,30 +239,26 @@ __global__ void rowstat_kara_kernel(const double* __restrict__ b, int naux, long
   }
 }
 
-// Row statistics over Q for each r: e_r, the FP64 diagonal sum_Q B^2, and the
-// global maximum exponent (atomicMax).  Block = 32 rows x 8 Q-groups.  The
-// maximum is taken on the integer bit patterns (no FP64 compare); the
-// diagonal needs one FP64 FMA per element.
-__global__ void rowstat_kernel(const double* __restrict__ b, int naux, long long R, int p,
-                               int* __restrict__ erow, double* __restrict__ diag, int* eref) {
-  __shared__ unsigned long long smax[8][32];
-  __shared__ double ssum[8][32];
+// Row statistics over Q for each r (scheme 0): e_r, the FP64 diagonal
+// sum_Q B^2, and the global maximum exponent (atomicMax).  The maximum is
+// taken on the integer bit patterns (no FP64 compare); the diagonal needs one
+// FP64 FMA per element.
+__global__ void __launch_bounds__(32 * QG) rowstat_kernel(const double* __restrict__ b, int naux,
+                                                          long long R, int p,
+                                                          int* __restrict__ erow,
+                                                          double* __restrict__ diag, int* eref) {
+  __shared__ unsigned long long smax[QG][32];
+  __shared__ double ssum[QG][32];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const long long r = (long long)blockIdx.x * 32 + tx;
   unsigned long long m = 0;
   double s = 0.0;
-  if (r < R)
-    for (int q = ty; q < naux; q += 8) {
-      const double x = b[(long long)q * R + r];
-      const unsigned long long ax = abs_bits(x);
-      m = ax > m ? ax : m;
-      s = fma(x, x, s);
-    }
+  if (r < R) row_pass1(b, naux, R, r, ty, &m, &s);
   smax[ty][tx] = m;
   ssum[ty][tx] = s;
   __syncthreads();
   if (ty == 0 && r < R) {
-    for (int k = 1; k < 8; ++k) {
+    for (int k = 1; k < QG; ++k) {
       m = smax[k][tx] > m ? smax[k][tx] : m;
       s += ssum[k][tx];
     }
@@ -409,13 +444,13 @@ cudaError_t launch_slices(const double* b, int naux, int nocc, int nvir, int Qp,
   const long long Rp = (long long)nocc * ((nvir + 127) / 128) * 128;
   dim3 grid((unsigned)((Rp + 63) / 64), (unsigned)((Qp + 63) / 64));
   if (scheme == kSchemeKara) {
-    rowstat_kara_kernel<<<(unsigned)((R + 31) / 32), dim3(32, 8), 0, s>>>(b, naux, R, w.erow,
+    rowstat_kara_kernel<<<(unsigned)((R + 31) / 32), dim3(32, QG), 0, s>>>(b, naux, R, w.erow,
                                                                           w.diag, w.eref,
                                                                           w.eref + 1);
     slice_kernel<kSchemeKara, 0><<<grid, 256, 0, s>>>(b, naux, nocc, nvir, Qp, p, w.erow,
                                                       w.eref + 1, w.S);
   } else {
-    rowstat_kernel<<<(unsigned)((R + 31) / 32), dim3(32, 8), 0, s>>>(b, naux, R, p, w.erow,
+    rowstat_kernel<<<(unsigned)((R + 31) / 32), dim3(32, QG), 0, s>>>(b, naux, R, p, w.erow,
                                                                      w.diag, w.eref);
     if (fmt == 0)
       slice_kernel<kSchemeDigits3, 0><<<grid, 256, 0, s>>>(b, naux, nocc, nvir, Qp, p, w.erow,
