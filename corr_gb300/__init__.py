@@ -141,6 +141,10 @@ class Context:
         check(self._L.corr_rimp2_energy_batched_async(self._h, n, arr, _prec(precision),
                                                       _ptr(out)))
 
+    def set_energy_policy(self, cluster):
+        """1: multicast cluster form of the energy kernel where it applies; 0: one-CTA form."""
+        check(self._L.corr_set_energy_policy(self._h, int(cluster)))
+
     def set_batch_policy(self, order, stages):
         check(self._L.corr_set_batch_policy(self._h, int(order), int(stages)))
 

@@ -1,5 +1,6 @@
 // C-ABI layer: context, status/error reporting, host/device argument staging,
 // TMA descriptor encoding and dispatch of the RI-MP2 energy kernels.
+#include <algorithm>
 #include <cudaTypedefs.h>
 
 #include <cmath>
@@ -247,6 +248,13 @@ int corr_sync(corr_context* c) {
   return CORR_OK;
 }
 
+int corr_set_energy_policy(corr_context* c, int cluster) {
+  CORR_CHECK_ARG(c != nullptr, "null context");
+  CORR_CHECK_ARG(cluster == 0 || cluster == 1, "corr_set_energy_policy: cluster must be 0 or 1");
+  c->tc_policy = cluster;
+  return CORR_OK;
+}
+
 int corr_set_timing(corr_context* c, int enable) {
   CORR_CHECK_ARG(c != nullptr, "null context");
   if (enable && !c->ev[0])
@@ -320,7 +328,7 @@ size_t energy_scratch_bytes(corr_context* c, int nocc, int nvir, int naux, int p
   SliceWork sw{};
   double* part;
   Carver cv{nullptr, 0};
-  energy_carve(cv, nocc, nvir, Qp, tc, energy_grid(c, sh, tc), &sw, &part);
+  energy_carve(cv, nocc, nvir, Qp, tc, 2 * c->sms, &sw, &part);  // partials of any grid
   return cv.used + 256;
 }
 
@@ -337,7 +345,7 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
   const int grid = energy_grid(c, sh, tc);
   SliceWork sw{};
   double* partials;
-  energy_carve(w, nocc, nvir, Qp, tc, grid, &sw, &partials);
+  energy_carve(w, nocc, nvir, Qp, tc, 2 * c->sms, &sw, &partials);
   if (!tc) {
     mark(c, 1);
     CORR_CUDA(launch_energy_fp64(d_b, d_e, sh, partials, grid, c->stream));
@@ -351,14 +359,20 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
   const int p = slice_bits_for(Qp);
   CORR_CUDA(launch_slices(d_b, naux, nocc, nvir, Qp, scheme, fmt, p, sw, c->stream));
   if (!c->attrs_set) {
-    CORR_CUDA(prepare_energy_tc());
+    CORR_CUDA(prepare_energy_tc(&c->tc_clusters));
     c->attrs_set = true;
   }
+  // 2 x 2 multicast clusters when at least 8 fit and nocc leaves little
+  // padding (pairs outside i <= j < nocc in the diagonal blocks are idle)
+  const long long cwork = energy_tc_cluster_work(sh);
+  const bool cluster = c->tc_policy == 1 && c->tc_clusters >= 8 && nocc >= 8;
+  const int lgrid =
+      cluster ? kTcCluster * (int)std::min<long long>(c->tc_clusters, cwork) : grid;
   mark(c, 1);
-  CORR_CUDA(launch_energy_tc(sw.S, d_e, sw.sc, sw.dg, sw.scale, sh, Qp, fmt, scheme, partials,
-                             grid, &c->dres->status, c->stream));
+  CORR_CUDA(launch_energy_tc(sw.S, d_e, sw.sc, sw.dg, sw.scale, sh, Qp, fmt, scheme, cluster,
+                             partials, lgrid, &c->dres->status, c->stream));
   mark(c, 2);
-  CORR_CUDA(launch_energy_reduce(partials, grid, sw.scale, out_e, c->stream));
+  CORR_CUDA(launch_energy_reduce(partials, lgrid, sw.scale, out_e, c->stream));
   c->launches += 5;  // rowstat, slice, rowfactor, energy, reduce
   return CORR_OK;
 }

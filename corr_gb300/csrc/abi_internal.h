@@ -48,6 +48,8 @@ struct corr_context {
   float t_prepass = 0.f, t_kernel = 0.f, t_total = 0.f;
   long long launches = 0;
   bool attrs_set = false;  // one-time kernel attributes (kept out of graph capture)
+  int tc_clusters = 0;     // 4-CTA clusters of the energy kernel that fit at once
+  int tc_policy = 0;       // 0: one-CTA form (default), 1: cluster form when it applies
   // batched driver
   bool batch_attrs_set = false;
   int batch_order = 1;   // 0 input order, 1 cost-descending

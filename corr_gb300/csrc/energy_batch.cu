@@ -121,21 +121,30 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
   if (warp == 0) {
     // ------------------------------------------------------------ producer
-    if (lane == 0) {
+    // Lane 0 takes units from the queue and paces the stages; lanes 0-5
+    // issue each stage's six copies in one instruction.
+    {
       int st = 0;
       uint32_t ph = 0;
       uint32_t last_ph[STAGES];
       bool has[STAGES];
       for (int s = 0; s < STAGES; ++s) has[s] = false;
       bool ok = true;
+      const int l = lane >> 1;
+      const bool colop = (lane & 1) != 0;
       for (long long t = 0; ok; ++t) {
         const int slot = (int)(t % RING);
         const uint32_t use = (uint32_t)(t / RING);
-        if (!mbar_wait(&ctl->uempty[slot], (use & 1) ^ 1, abort, status)) break;
-        long long u = (long long)atomicAdd(queue, 1ull);
-        if (u >= total) u = -1;
-        ctl->uring[slot] = u;
-        mbar_arrive(&ctl->ufull[slot]);
+        long long u = -2;  // -2: wait failed, -1: queue drained
+        if (lane == 0) {
+          if (mbar_wait(&ctl->uempty[slot], (use & 1) ^ 1, abort, status)) {
+            u = (long long)atomicAdd(queue, 1ull);
+            if (u >= total) u = -1;
+            ctl->uring[slot] = u;
+            mbar_arrive(&ctl->ufull[slot]);
+          }
+        }
+        u = __shfl_sync(0xffffffffu, u, 0);
         if (u < 0) break;
         const UnitInfo ui = unit_info(insts, ninst, u);
         const BatchInst& bi = insts[ui.inst];
@@ -143,23 +152,21 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         for (int phs = 0; phs < nph && ok; ++phs) {
           const int x = phs == 0 ? ui.i : ui.j;
           const int y = phs == 0 ? ui.j : ui.i;
+          const int slab = colop ? y : x, tile = colop ? ui.B : ui.A;
           for (int kb = 0; kb < bi.nkb; ++kb) {
-            if (!mbar_wait(&ctl->empty[st], ph ^ 1, abort, status)) {
+            bool got = true;
+            if (lane == 0) got = mbar_wait(&ctl->empty[st], ph ^ 1, abort, status);
+            if (!__shfl_sync(0xffffffffu, got ? 1 : 0, 0)) {
               ok = false;
               break;
             }
             uint64_t* bar = &ctl->full[st];
-            mbar_expect_tx(bar, STAGE_BYTES);
-            uint8_t* sb = tiles + (size_t)st * STAGE_BYTES;
-#pragma unroll
-            for (int l = 0; l < 3; ++l) {
-              bulk_load(sb + (2 * l) * TILE_BYTES,
-                        bi.S + slice_tile_offset(l, x, kb, ui.A, bi.o, bi.nkb, bi.ntiles),
+            if (lane == 0) mbar_expect_tx(bar, STAGE_BYTES);
+            __syncwarp();
+            if (lane < 6)
+              bulk_load(tiles + (size_t)st * STAGE_BYTES + (2 * l + (colop ? 1 : 0)) * TILE_BYTES,
+                        bi.S + slice_tile_offset(l, slab, kb, tile, bi.o, bi.nkb, bi.ntiles),
                         TILE_BYTES, bar);
-              bulk_load(sb + (2 * l + 1) * TILE_BYTES,
-                        bi.S + slice_tile_offset(l, y, kb, ui.B, bi.o, bi.nkb, bi.ntiles),
-                        TILE_BYTES, bar);
-            }
             has[st] = true;
             last_ph[st] = ph;
             if (++st == STAGES) {
@@ -169,9 +176,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           }
         }
       }
-      int never = 0;
-      for (int s = 0; s < STAGES; ++s)
-        if (has[s]) mbar_wait(&ctl->full[s], last_ph[s], &never, status);
+      if (lane == 0) {
+        int never = 0;
+        for (int s = 0; s < STAGES; ++s)
+          if (has[s]) mbar_wait(&ctl->full[s], last_ph[s], &never, status);
+      }
+      __syncwarp();
     }
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer

@@ -21,8 +21,22 @@
 //   E_OS -= f w (D1^2 + D2^2)/D,  E_SS -= f w (D1 - D2)^2/D,
 // with 1/D as an IEEE-rounded FP32 reciprocal and FP64 sums per unit.
 //
+// Cluster form (CL): 2 x 2 clusters of CTAs.  A cluster takes a block pair
+// (a <= b) of occupied indices and a tile pair; CTA (r, c) of the cluster
+// computes the pair (i, j) = (2a + r, 2b + c).  The D1 row tile (i, A) is
+// needed by both CTAs of cluster row r and the column tile (j, B) by both
+// CTAs of cluster column c (in phase 2 the roles swap: rows (j, A) per column,
+// columns (i, B) per row), so each CTA copies one 64-row half of each shared
+// tile and multicasts it to the CTAs that need it: half the L2 -> SM stream
+// of the plain form.  A stage of CTA X is written by X and its two partners,
+// so its `empty` barrier waits for three consumer releases (tcgen05.commit
+// multicast).  All four CTAs run the same phase sequence: tile pairs A != B
+// always take two phases (for i == j the second recomputes D2 = D1), pairs
+// outside i <= j < nocc load their share and contribute with weight 0.
+//
 // CTA = 6 warps, persistent, one CTA per SM:
-//   warp 0     bulk-copy producer (one thread), 6 tiles of 128x32 per stage, 4 stages
+//   warp 0     bulk-copy producer (lane 0 paces, lanes 0-5 copy), 6 tiles of 128x32 per
+//              stage, 4 stages
 //   warp 1     TMEM owner + MMA issuer (one thread), tcgen05.mma kind::f16
 //   warps 2-5  epilogue, one TMEM lane quarter each
 // Every wait is bounded (common.cuh); on a timeout the CTA winds down and the
@@ -40,6 +54,7 @@ constexpr int KB = 32;                        // 16-bit Q elements per stage row
 constexpr int STAGES = 4;
 constexpr int NTILES = 6;                     // 3 slices x (row operand, col operand)
 constexpr int TILE_BYTES = TILE * KB * 2;     // 8 KB
+constexpr int HALF_BYTES = TILE_BYTES / 2;    // 64 rows of a tile (cluster form)
 constexpr int STAGE_BYTES = NTILES * TILE_BYTES;
 constexpr int NTHREADS = 192;
 constexpr uint32_t TMEM_COLS = 512;
@@ -63,14 +78,43 @@ struct Ctl {
 
 constexpr size_t kSmemBytes = (size_t)STAGES * STAGE_BYTES + sizeof(Ctl) + 1024;
 
-__device__ __forceinline__ void unit_decode(long long u, const EnergyShape& sh, int* i, int* j,
-                                            int* A, int* B) {
-  int p = (int)(u / sh.ntpairs), tp = (int)(u % sh.ntpairs);
-  pair_decode(p, sh.nocc, i, j);
-  tpair_decode(tp, sh.ntiles, A, B);
+struct Unit {
+  int i, j, A, B;  // occupied pair (clamped into range) and tile pair
+  int nph;         // MMA phases: 1 (D2 from D1) or 2
+  bool valid;      // contributes to the energy
+};
+
+// Work item k of this CTA's sequence.  Plain: unit k = (pair, tile pair).
+// Cluster: super-unit k = (block pair, tile pair), this CTA's (r, c) member.
+template <bool CL>
+__device__ __forceinline__ Unit unit_at(long long k, const EnergyShape& sh, int r, int c) {
+  Unit u;
+  const int tp = (int)(k % sh.ntpairs);
+  tpair_decode(tp, sh.ntiles, &u.A, &u.B);
+  if (!CL) {
+    pair_decode((int)(k / sh.ntpairs), sh.nocc, &u.i, &u.j);
+    u.nph = (u.i == u.j || u.A == u.B) ? 1 : 2;
+    u.valid = true;
+  } else {
+    int a, b;
+    pair_decode((int)(k / sh.ntpairs), (sh.nocc + 1) / 2, &a, &b);
+    const int i = 2 * a + r, j = 2 * b + c;
+    u.valid = i < sh.nocc && j < sh.nocc && i <= j;
+    u.i = i < sh.nocc ? i : sh.nocc - 1;
+    u.j = j < sh.nocc ? j : sh.nocc - 1;
+    u.nph = u.A == u.B ? 1 : 2;
+  }
+  return u;
 }
 
-template <int SCHEME>
+template <bool CL>
+__device__ __forceinline__ long long work_count(const EnergyShape& sh) {
+  if (!CL) return sh.nunits;
+  const long long nb = (sh.nocc + 1) / 2;
+  return nb * (nb + 1) / 2 * sh.ntpairs;
+}
+
+template <int SCHEME, bool CL>
 __global__ void __launch_bounds__(NTHREADS, 1)
     energy_tc_kernel(const uint16_t* __restrict__ S, const double* __restrict__ eps,
                      const float* __restrict__ sc, const float* __restrict__ dg,
@@ -82,11 +126,19 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   Ctl* ctl = reinterpret_cast<Ctl*>(tiles + (size_t)STAGES * STAGE_BYTES);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int o = sh.nocc, v = sh.nvir;
+  // cluster coordinates and multicast groups (rank q = 2r + c)
+  const int q4 = CL ? (int)cluster_ctarank() : 0;
+  const int cr = q4 >> 1, cc = q4 & 1;
+  const uint16_t grow = (uint16_t)(3u << (2 * cr));  // CTAs of cluster row cr
+  const uint16_t gcol = (uint16_t)(5u << cc);        // CTAs of cluster column cc
+  const long long first = CL ? (long long)cluster_id_x() : (long long)blockIdx.x;
+  const long long stride = CL ? (long long)cluster_count_x() : (long long)gridDim.x;
+  const long long nwork = work_count<CL>(sh);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(&ctl->full[s], 1);
-      mbar_init(&ctl->empty[s], 1);
+      mbar_init(&ctl->empty[s], CL ? 3 : 1);
     }
     mbar_init(&ctl->afull, 1);
     mbar_init(&ctl->aempty, 4);
@@ -97,40 +149,57 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == 1) tmem_alloc(&ctl->tmem, TMEM_COLS);
   tc_fence_before();
   __syncthreads();
+  if (CL) cluster_sync();  // partners' barriers exist before any multicast
   tc_fence_after();
   const uint32_t tmem = ctl->tmem;
   volatile int* abort = &ctl->abort;
 
   if (warp == 0) {
     // ------------------------------------------------------------ producer
-    if (lane == 0) {
+    // The whole warp runs the loop: lane 0 waits for a free stage and arms
+    // its barrier, then lanes 0-5 issue the stage's six copies in one
+    // instruction (one copy per lane issues several times faster than six
+    // copies in sequence from one thread).
+    {
       int st = 0;
       uint32_t ph = 0;
       uint32_t last_ph[STAGES];
       bool has[STAGES];
       for (int s = 0; s < STAGES; ++s) has[s] = false;
       bool ok = true;
-      for (long long u = blockIdx.x; u < sh.nunits && ok; u += gridDim.x) {
-        int i, j, A, B;
-        unit_decode(u, sh, &i, &j, &A, &B);
-        const int nph = (i == j || A == B) ? 1 : 2;
-        for (int phs = 0; phs < nph && ok; ++phs) {
-          const int x = phs == 0 ? i : j;  // row operand slab
-          const int y = phs == 0 ? j : i;  // column operand slab
+      const int l = lane >> 1;            // digit plane of this lane's copy
+      const bool colop = (lane & 1) != 0;  // row (even lane) or column operand
+      for (long long k = first; k < nwork && ok; k += stride) {
+        const Unit w = unit_at<CL>(k, sh, cr, cc);
+        for (int phs = 0; phs < w.nph && ok; ++phs) {
+          const int x = phs == 0 ? w.i : w.j;  // row operand slab
+          const int y = phs == 0 ? w.j : w.i;  // column operand slab
+          // cluster: the row tile is shared along the cluster row in phase 1
+          // and along the cluster column in phase 2 (and the column tile the
+          // other way); this CTA copies its half of each
+          const uint16_t mrow = phs == 0 ? grow : gcol, mcol = phs == 0 ? gcol : grow;
+          const int hrow = phs == 0 ? cc : cr, hcol = phs == 0 ? cr : cc;
+          const int slab = colop ? y : x, tile = colop ? w.B : w.A;
+          const uint16_t mask = colop ? mcol : mrow;
+          const int half = colop ? hcol : hrow;
           for (int kb = 0; kb < nkb; ++kb) {
-            if (!mbar_wait(&ctl->empty[st], ph ^ 1, abort, status)) {
+            bool got = true;
+            if (lane == 0) got = mbar_wait(&ctl->empty[st], ph ^ 1, abort, status);
+            if (!__shfl_sync(0xffffffffu, got ? 1 : 0, 0)) {
               ok = false;
               break;
             }
             uint64_t* bar = &ctl->full[st];
-            mbar_expect_tx(bar, STAGE_BYTES);
-            uint8_t* sb = tiles + (size_t)st * STAGE_BYTES;
-#pragma unroll
-            for (int l = 0; l < 3; ++l) {
-              bulk_load(sb + (2 * l) * TILE_BYTES,
-                        S + slice_tile_offset(l, x, kb, A, o, nkb, sh.ntiles), TILE_BYTES, bar);
-              bulk_load(sb + (2 * l + 1) * TILE_BYTES,
-                        S + slice_tile_offset(l, y, kb, B, o, nkb, sh.ntiles), TILE_BYTES, bar);
+            if (lane == 0) mbar_expect_tx(bar, STAGE_BYTES);
+            __syncwarp();
+            uint8_t* sb = tiles + (size_t)st * STAGE_BYTES + (2 * l + (colop ? 1 : 0)) * TILE_BYTES;
+            if (lane < 6) {
+              const uint16_t* src = S + slice_tile_offset(l, slab, kb, tile, o, nkb, sh.ntiles);
+              if (CL)
+                bulk_load_mc(sb + half * HALF_BYTES, src + half * (HALF_BYTES / 2), HALF_BYTES,
+                             bar, mask);
+              else
+                bulk_load(sb, src, TILE_BYTES, bar);
             }
             has[st] = true;
             last_ph[st] = ph;
@@ -141,10 +210,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           }
         }
       }
-      // Never leave with a bulk copy still landing in shared memory.
-      int never = 0;
-      for (int s = 0; s < STAGES; ++s)
-        if (has[s]) mbar_wait(&ctl->full[s], last_ph[s], &never, status);
+      // Never leave with a bulk copy still landing in shared memory; in the
+      // cluster form also wait for the partners' releases of the last fills
+      // (their remote arrivals target this CTA's barriers).
+      if (lane == 0) {
+        int never = 0;
+        for (int s = 0; s < STAGES; ++s)
+          if (has[s]) mbar_wait(&ctl->full[s], last_ph[s], &never, status);
+        if (CL)
+          for (int s = 0; s < STAGES; ++s)
+            if (has[s]) mbar_wait(&ctl->empty[s], last_ph[s], &never, status);
+      }
+      __syncwarp();
     }
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
@@ -153,11 +230,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       uint32_t ph = 0;
       uint32_t nuse = 0;
       bool ok = true;
-      for (long long u = blockIdx.x; u < sh.nunits && ok; u += gridDim.x) {
-        int i, j, A, B;
-        unit_decode(u, sh, &i, &j, &A, &B);
-        const int nph = (i == j || A == B) ? 1 : 2;
-        for (int phs = 0; phs < nph && ok; ++phs) {
+      const uint16_t release = (uint16_t)(grow | gcol);  // this CTA and its two partners
+      for (long long k = first; k < nwork && ok; k += stride) {
+        const Unit w = unit_at<CL>(k, sh, cr, cc);
+        for (int phs = 0; phs < w.nph && ok; ++phs) {
           if (!mbar_wait(&ctl->aempty, (nuse & 1) ^ 1, abort, status)) {
             ok = false;
             break;
@@ -183,7 +259,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               const uint32_t acc = (kb | kk) ? 1u : 0u;
               issue_digit_mmas<SCHEME>(c0, c1, c2, r, q, idesc, acc);
             }
-            tc_commit(&ctl->empty[st]);  // stage reusable once these MMAs finish
+            // stage reusable once these MMAs finish (in every CTA that wrote it)
+            if (CL)
+              tc_commit_mc(&ctl->empty[st], release);
+            else
+              tc_commit(&ctl->empty[st]);
             if (++st == STAGES) {
               st = 0;
               ph ^= 1;
@@ -208,9 +288,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     double tot_os = 0.0, tot_ss = 0.0;
     bool dead = false;
     uint32_t nuse = 0;
-    for (long long u = blockIdx.x; u < sh.nunits; u += gridDim.x) {
-      int i, j, A, B;
-      unit_decode(u, sh, &i, &j, &A, &B);
+    for (long long k = first; k < nwork; k += stride) {
+      const Unit w = unit_at<CL>(k, sh, cr, cc);
+      const int i = w.i, j = w.j, A = w.A, B = w.B;
+      const bool two = w.nph == 2;
       const int A0 = A * TILE, B0 = B * TILE;
       const bool same = (i == j);
       {
@@ -240,7 +321,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       if (!got) dead = true;
       if (!dead) {
         tc_fence_after();
-        if (same) {
+        if (!two && same) {
           // D2 == D1: fold straight into the energy
 #pragma unroll 1
           for (int c = 0; c < TILE; c += 32) {
@@ -255,8 +336,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
             uos += (double)fos;
           }
-        } else if (A == B) {
-          // Diagonal tile pair: D2 = D1^T.  Four rounds; in round k warp q
+        } else if (!two) {
+          // Diagonal tile pair (A == B): D2 = D1^T.  Four rounds; in round k warp q
           // publishes its D1 block of column chunk (q+k)%4 and takes the block
           // of warp (q-k)%4, which is the D1^T block of column chunk (q-k)%4.
 #pragma unroll 1
@@ -301,8 +382,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       }
       ++nuse;
 
-      // ---- phase 2: D2 (i != j, A != B): rows from slab j, columns from slab i
-      if (!same && A != B) {
+      // ---- phase 2: D2 (two-phase units): rows from slab j, columns from slab i
+      if (two) {
         named_bar(1, 128);  // everyone is done with the phase-1 column scales
         if (B0 + et < v) ctl->scb[et] = sc[(size_t)i * v + B0 + et];
         named_bar(1, 128);
@@ -338,7 +419,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         }
         ++nuse;
       }
-      const double fw = (A < B ? 2.0 : 1.0) * (same ? 0.5 : 1.0);
+      const double fw = w.valid ? (A < B ? 2.0 : 1.0) * (same ? 0.5 : 1.0) : 0.0;
       tot_os -= fw * uos;
       tot_ss -= fw * uss;
       named_bar(1, 128);  // smem db/scb are rewritten by the next unit
@@ -361,33 +442,89 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   __syncwarp();
   tc_fence_before();
   __syncthreads();
+  // no CTA of a cluster leaves while a partner may still address its shared memory
+  if (CL) cluster_sync();
   tc_fence_after();
   if (warp == 1) tmem_dealloc(tmem, TMEM_COLS);
 }
 
 }  // namespace
 
-cudaError_t prepare_energy_tc() {
-  cudaError_t e = cudaFuncSetAttribute(energy_tc_kernel<kSchemeDigits3>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)kSmemBytes);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(energy_tc_kernel<kSchemeKara>,
+template <int SCHEME, bool CL>
+static cudaError_t set_smem_attr() {
+  return cudaFuncSetAttribute(energy_tc_kernel<SCHEME, CL>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
+}
+
+template <int SCHEME, bool CL>
+static cudaError_t launch_variant(int grid, cudaStream_t s, const uint16_t* S, const double* eps,
+                                  const float* sc, const float* dg, const double* scale,
+                                  const EnergyShape& sh, int nkb, uint32_t idesc,
+                                  double* partials, int* status) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(NTHREADS);
+  cfg.dynamicSmemBytes = kSmemBytes;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL ? kTcCluster : 1;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = CL ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, energy_tc_kernel<SCHEME, CL>, S, eps, sc, dg, scale, sh, nkb,
+                            idesc, partials, status);
+}
+
+cudaError_t prepare_energy_tc(int* max_clusters) {
+  cudaError_t e = set_smem_attr<kSchemeDigits3, false>();
+  if (e == cudaSuccess) e = set_smem_attr<kSchemeKara, false>();
+  if (e == cudaSuccess) e = set_smem_attr<kSchemeDigits3, true>();
+  if (e == cudaSuccess) e = set_smem_attr<kSchemeKara, true>();
+  if (e != cudaSuccess) return e;
+  // how many 4-CTA clusters of this kernel fit on the device at once
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kTcCluster);
+  cfg.blockDim = dim3(NTHREADS);
+  cfg.dynamicSmemBytes = kSmemBytes;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = kTcCluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  e = cudaOccupancyMaxActiveClusters(&n, energy_tc_kernel<kSchemeKara, true>, &cfg);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    n = 0;  // no cluster form on this device
+  }
+  *max_clusters = n;
+  return cudaSuccess;
+}
+
+long long energy_tc_cluster_work(const EnergyShape& sh) {
+  const long long nb = (sh.nocc + 1) / 2;
+  return nb * (nb + 1) / 2 * sh.ntpairs;
 }
 
 cudaError_t launch_energy_tc(const uint16_t* S, const double* eps, const float* sc,
                              const float* dg, const double* scale, const EnergyShape& sh, int Qp,
-                             int fmt, int scheme, double* partials, int grid, int* status,
-                             cudaStream_t s) {
+                             int fmt, int scheme, bool cluster, double* partials, int grid,
+                             int* status, cudaStream_t s) {
   const uint32_t idesc = idesc_f16((uint32_t)fmt, TILE, TILE);
+  const int nkb = Qp / KB;
   if (scheme == kSchemeKara)
-    energy_tc_kernel<kSchemeKara><<<grid, NTHREADS, kSmemBytes, s>>>(
-        S, eps, sc, dg, scale, sh, Qp / KB, idesc, partials, status);
-  else
-    energy_tc_kernel<kSchemeDigits3><<<grid, NTHREADS, kSmemBytes, s>>>(
-        S, eps, sc, dg, scale, sh, Qp / KB, idesc, partials, status);
-  return cudaGetLastError();
+    return cluster ? launch_variant<kSchemeKara, true>(grid, s, S, eps, sc, dg, scale, sh, nkb,
+                                                       idesc, partials, status)
+                   : launch_variant<kSchemeKara, false>(grid, s, S, eps, sc, dg, scale, sh, nkb,
+                                                        idesc, partials, status);
+  return cluster ? launch_variant<kSchemeDigits3, true>(grid, s, S, eps, sc, dg, scale, sh, nkb,
+                                                        idesc, partials, status)
+                 : launch_variant<kSchemeDigits3, false>(grid, s, S, eps, sc, dg, scale, sh, nkb,
+                                                         idesc, partials, status);
 }
 
 }  // namespace corr

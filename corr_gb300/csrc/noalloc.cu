@@ -58,7 +58,8 @@ int setup_device(int device, DeviceScratch* out) {
     }
     int sms = 0;
     CORR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    CORR_CUDA(prepare_energy_tc());
+    int clusters = 0;  // the allocation-free entry point runs the one-CTA form
+    CORR_CUDA(prepare_energy_tc(&clusters));
     d.sms = sms;
     d.ptr = p;
   }
@@ -158,8 +159,8 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
     const int fmt = format_for_scheme(scheme);
     const int p = slice_bits_for(Qp);
     CORR_CUDA(launch_slices(bia, naux, nocc, nvir, Qp, scheme, fmt, p, sw, s));
-    CORR_CUDA(launch_energy_tc(sw.S, eps, sw.sc, sw.dg, sw.scale, sh, Qp, fmt, scheme, partials,
-                               grid, &hdr->status, s));
+    CORR_CUDA(launch_energy_tc(sw.S, eps, sw.sc, sw.dg, sw.scale, sh, Qp, fmt, scheme, false,
+                               partials, grid, &hdr->status, s));
     CORR_CUDA(launch_energy_reduce(partials, grid, sw.scale, hdr->e, s));
   }
   Header h;

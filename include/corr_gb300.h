@@ -153,6 +153,14 @@ int corr_rimp2_energy_batched(corr_context* ctx, int n, const corr_rimp2_instanc
 int corr_rimp2_energy_batched_async(corr_context* ctx, int n, const corr_rimp2_instance* inst,
                                     int precision, double* energies_dev);
 
+/* Form of the tcgen05 energy kernel used by corr_rimp2_energy(_async) and
+ * corr_rimp2_energy_from_3index (no counterpart in the reference): 0 (the
+ * default) = one CTA per work stream; 1 = 2x2 clusters that multicast shared
+ * operand tiles, used when nocc >= 8 and at least 8 clusters fit on the
+ * device (half the L2 traffic, but slower on GB300 at the measured sizes).
+ * Both give the same energies up to FP64 summation order. */
+int corr_set_energy_policy(corr_context* ctx, int cluster);
+
 /* Launch variant of the batched kernel: unit order (0 = input order,
  * 1 = costliest instance first) and shared-memory pipeline depth (3 or 4). */
 int corr_set_batch_policy(corr_context* ctx, int order, int stages);

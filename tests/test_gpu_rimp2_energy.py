@@ -101,3 +101,23 @@ def test_split_wide_dynamic_range(ctx, prec):
     got = ctx.rimp2_energy(B, eps, o, v, X, prec)
     assert abs(got.e_total - ref[2]) <= 2e-7 * abs(ref[2]), (prec, got, ref)
     assert abs(got.e_os - ref[1]) <= 2e-7 * abs(ref[1]), (prec, got, ref)
+
+
+@pytest.mark.parametrize("o,v,X", [(8, 130, 70), (9, 257, 100), (13, 360, 300), (40, 360, 1200)])
+@pytest.mark.parametrize("prec", ["split_fp16", "split_bf16"])
+def test_cluster_form_matches_one_cta_form(ctx, o, v, X, prec):
+    """The 2x2 multicast cluster form (odd nocc leaves idle members in the
+    last block) against the one-CTA form: same digit products, different
+    FP64 summation order."""
+    B, eps = O.synth_rimp2(o, v, X, 31 + o)
+    one = ctx.rimp2_energy(B, eps, o, v, X, prec)
+    ctx.set_energy_policy(1)
+    try:
+        clu = ctx.rimp2_energy(B, eps, o, v, X, prec)
+    finally:
+        ctx.set_energy_policy(0)
+    for a, b in zip(clu.as_tuple(), one.as_tuple()):
+        assert abs(a - b) <= 1e-9 * abs(one.e_total), (prec, clu, one)
+    if o * v * X <= 13 * 360 * 300:
+        ref = O.rimp2_energy(B, eps, o, v)
+        assert abs(clu.e_total - ref[2]) <= 2e-7 * abs(ref[2]), (prec, clu, ref)
