@@ -323,7 +323,7 @@ static int energy_grid(corr_context* c, const EnergyShape& sh, bool tc) {
 
 size_t energy_scratch_bytes(corr_context* c, int nocc, int nvir, int naux, int precision) {
   const bool tc = precision != CORR_PREC_FP64;
-  const int Qp = ((naux + 31) / 32) * 32;
+  const int Qp = padded_naux(naux);
   const EnergyShape sh = make_energy_shape(nocc, nvir, naux, tc ? kTcTile : kF64Tile);
   SliceWork sw{};
   double* part;
@@ -339,7 +339,7 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
                       const double* d_e, int precision, double* res) {
   double* out_e = res ? res : c->dres->e;
   const bool tc = precision != CORR_PREC_FP64;
-  const int Qp = ((naux + 31) / 32) * 32;
+  const int Qp = padded_naux(naux);
   const long long R = (long long)nocc * nvir;
   const EnergyShape sh = make_energy_shape(nocc, nvir, naux, tc ? kTcTile : kF64Tile);
   const int grid = energy_grid(c, sh, tc);

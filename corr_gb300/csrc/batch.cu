@@ -68,7 +68,7 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
   for (int k = 0; k < n; ++k) {
     const corr_rimp2_instance& x = in[order[k]];
     Shape& s = shp[k];
-    s.Qp = ((x.naux + 31) / 32) * 32;
+    s.Qp = padded_naux(x.naux);
     s.p = slice_bits_for(s.Qp);
     s.R = (long long)x.nocc * x.nvir;
     s.sh = make_energy_shape(x.nocc, x.nvir, x.naux, tc ? kTcTile : kF64Tile);

@@ -190,6 +190,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       uint32_t ph = 0;
       uint32_t nuse = 0;
       bool ok = true;
+      const uint64_t dbase = smem_desc(smem_u32(tiles), 16, 512, SW64);  // tile 0, stage 0
       for (long long t = 0; ok; ++t) {
         const int slot = (int)(t % RING);
         const uint32_t use = (uint32_t)(t / RING);
@@ -213,15 +214,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               break;
             }
             tc_fence_after();
-            const uint32_t sb = smem_u32(tiles + (size_t)st * STAGE_BYTES);
+            const uint64_t ds = dbase + (uint64_t)(((uint32_t)st * STAGE_BYTES) >> 4);
 #pragma unroll
             for (int kk = 0; kk < KB / 16; ++kk) {
-              const uint32_t off = (uint32_t)kk * 32u;
               uint64_t r[3], q[3];
 #pragma unroll
               for (int l = 0; l < 3; ++l) {
-                r[l] = smem_desc(sb + (uint32_t)(2 * l) * TILE_BYTES + off, 16, 512, SW64);
-                q[l] = smem_desc(sb + (uint32_t)(2 * l + 1) * TILE_BYTES + off, 16, 512, SW64);
+                r[l] = ds + (uint64_t)(((2 * l) * TILE_BYTES + kk * 32) >> 4);
+                q[l] = ds + (uint64_t)(((2 * l + 1) * TILE_BYTES + kk * 32) >> 4);
               }
               const uint32_t acc = (kb | kk) ? 1u : 0u;
               issue_digit_mmas<SCHEME>(c0, c1, c2, r, q, idesc, acc);

@@ -50,9 +50,10 @@ namespace corr {
 namespace {
 
 constexpr int TILE = kTcTile;                 // 128
-constexpr int KB = 32;                        // 16-bit Q elements per stage row (64 B)
+constexpr int KB = 32;                        // 16-bit Q elements per tile row (64 B)
+constexpr int KBS = 1;                        // 32-wide Q blocks per pipeline stage
 constexpr int STAGES = 4;
-constexpr int NTILES = 6;                     // 3 slices x (row operand, col operand)
+constexpr int NTILES = 6 * KBS;               // KBS x 3 digit planes x (row, column operand)
 constexpr int TILE_BYTES = TILE * KB * 2;     // 8 KB
 constexpr int HALF_BYTES = TILE_BYTES / 2;    // 64 rows of a tile (cluster form)
 constexpr int STAGE_BYTES = NTILES * TILE_BYTES;
@@ -167,8 +168,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       bool has[STAGES];
       for (int s = 0; s < STAGES; ++s) has[s] = false;
       bool ok = true;
-      const int l = lane >> 1;            // digit plane of this lane's copy
-      const bool colop = (lane & 1) != 0;  // row (even lane) or column operand
+      // lane -> (Q block of the stage, digit plane, row/column operand)
+      const int kbo = lane / 6, l = (lane % 6) >> 1;
+      const bool colop = (lane & 1) != 0;
       for (long long k = first; k < nwork && ok; k += stride) {
         const Unit w = unit_at<CL>(k, sh, cr, cc);
         for (int phs = 0; phs < w.nph && ok; ++phs) {
@@ -182,7 +184,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           const int slab = colop ? y : x, tile = colop ? w.B : w.A;
           const uint16_t mask = colop ? mcol : mrow;
           const int half = colop ? hcol : hrow;
-          for (int kb = 0; kb < nkb; ++kb) {
+          for (int ks = 0; ks < nkb; ks += KBS) {
+            const int kb = ks + kbo;
             bool got = true;
             if (lane == 0) got = mbar_wait(&ctl->empty[st], ph ^ 1, abort, status);
             if (!__shfl_sync(0xffffffffu, got ? 1 : 0, 0)) {
@@ -192,8 +195,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             uint64_t* bar = &ctl->full[st];
             if (lane == 0) mbar_expect_tx(bar, STAGE_BYTES);
             __syncwarp();
-            uint8_t* sb = tiles + (size_t)st * STAGE_BYTES + (2 * l + (colop ? 1 : 0)) * TILE_BYTES;
-            if (lane < 6) {
+            uint8_t* sb =
+                tiles + (size_t)st * STAGE_BYTES + (6 * kbo + 2 * l + (colop ? 1 : 0)) * TILE_BYTES;
+            if (lane < NTILES) {
               const uint16_t* src = S + slice_tile_offset(l, slab, kb, tile, o, nkb, sh.ntiles);
               if (CL)
                 bulk_load_mc(sb + half * HALF_BYTES, src + half * (HALF_BYTES / 2), HALF_BYTES,
@@ -231,6 +235,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       uint32_t nuse = 0;
       bool ok = true;
       const uint16_t release = (uint16_t)(grow | gcol);  // this CTA and its two partners
+      // shared-memory descriptor of tile 0 of stage 0 (every tile address is
+      // below 2^18, so offsets added to the 14-bit start field never carry out)
+      const uint64_t dbase = smem_desc(smem_u32(tiles), 16, 512, SW64);
       for (long long k = first; k < nwork && ok; k += stride) {
         const Unit w = unit_at<CL>(k, sh, cr, cc);
         for (int phs = 0; phs < w.nph && ok; ++phs) {
@@ -240,23 +247,25 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           }
           tc_fence_after();
           const uint32_t c0 = tmem, c1 = tmem + 128u, c2 = tmem + 256u;
-          for (int kb = 0; kb < nkb; ++kb) {
+          for (int ks = 0; ks < nkb; ks += KBS) {
             if (!mbar_wait(&ctl->full[st], ph, abort, status)) {
               ok = false;
               break;
             }
             tc_fence_after();
-            const uint32_t sb = smem_u32(tiles + (size_t)st * STAGE_BYTES);
+            // descriptor of this stage: the base descriptor plus the stage's
+            // address offset in the 16-byte units of the start-address field
+            const uint64_t ds = dbase + (uint64_t)(((uint32_t)st * STAGE_BYTES) >> 4);
 #pragma unroll
-            for (int kk = 0; kk < KB / 16; ++kk) {
-              const uint32_t off = (uint32_t)kk * 32u;  // 16 elements x 2 B
+            for (int j = 0; j < KBS * (KB / 16); ++j) {
+              const int kbo = j / (KB / 16), kk = j % (KB / 16);
               uint64_t r[3], q[3];
 #pragma unroll
               for (int l = 0; l < 3; ++l) {
-                r[l] = smem_desc(sb + (uint32_t)(2 * l) * TILE_BYTES + off, 16, 512, SW64);
-                q[l] = smem_desc(sb + (uint32_t)(2 * l + 1) * TILE_BYTES + off, 16, 512, SW64);
+                r[l] = ds + (uint64_t)(((6 * kbo + 2 * l) * TILE_BYTES + kk * 32) >> 4);
+                q[l] = ds + (uint64_t)(((6 * kbo + 2 * l + 1) * TILE_BYTES + kk * 32) >> 4);
               }
-              const uint32_t acc = (kb | kk) ? 1u : 0u;
+              const uint32_t acc = (ks | j) ? 1u : 0u;
               issue_digit_mmas<SCHEME>(c0, c1, c2, r, q, idesc, acc);
             }
             // stage reusable once these MMAs finish (in every CTA that wrote it)
@@ -321,12 +330,26 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       if (!got) dead = true;
       if (!dead) {
         tc_fence_after();
+        // Phase-1 result (scaled D1, FP32) to the stash columns, then the
+        // accumulators go back to the MMA issuer at once: the rest of this
+        // unit's epilogue overlaps the next phase's MMAs.
+#pragma unroll 1
+        for (int c = 0; c < TILE; c += 32) {
+          float d1[32];
+          load_level_sum<SCHEME>(tq, c, inv_l, inv_l2, sca1, ctl->scb, d1);
+          tmem_st32(tq + COL_STASH + (uint32_t)c, d1);
+        }
+        tc_wait_st();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&ctl->aempty);
         if (!two && same) {
           // D2 == D1: fold straight into the energy
 #pragma unroll 1
           for (int c = 0; c < TILE; c += 32) {
             float d1[32];
-            load_level_sum<SCHEME>(tq, c, inv_l, inv_l2, sca1, ctl->scb, d1);
+            tmem_ld32(tq + COL_STASH + (uint32_t)c, d1);
+            tc_wait_ld();
             float fos = 0.f;
 #pragma unroll
             for (int k = 0; k < 32; ++k) {
@@ -344,7 +367,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           for (int k = 0; k < 4; ++k) {
             float d[32];
             const int cw = 32 * ((q + k) & 3);
-            load_level_sum<SCHEME>(tq, cw, inv_l, inv_l2, sca1, ctl->scb, d);
+            tmem_ld32(tq + COL_STASH + (uint32_t)cw, d);
+            tc_wait_ld();
 #pragma unroll
             for (int x = 0; x < 32; ++x) ctl->tbuf[q][lane][x] = d[x];
             named_bar(1, 128);
@@ -353,7 +377,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             float d2[32];
 #pragma unroll
             for (int x = 0; x < 32; ++x) d2[x] = ctl->tbuf[wr][x][lane];
-            load_level_sum<SCHEME>(tq, cr, inv_l, inv_l2, sca1, ctl->scb, d);
+            tmem_ld32(tq + COL_STASH + (uint32_t)cr, d);
+            tc_wait_ld();
             float fos = 0.f, fss = 0.f;
 #pragma unroll
             for (int x = 0; x < 32; ++x) {
@@ -367,18 +392,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             uss += (double)fss;
             named_bar(1, 128);  // tbuf is rewritten in the next round
           }
-        } else {
-#pragma unroll 1
-          for (int c = 0; c < TILE; c += 32) {
-            float d1[32];
-            load_level_sum<SCHEME>(tq, c, inv_l, inv_l2, sca1, ctl->scb, d1);
-            tmem_st32(tq + COL_STASH + (uint32_t)c, d1);
-          }
-          tc_wait_st();
         }
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&ctl->aempty);
       }
       ++nuse;
 
@@ -395,17 +409,24 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         if (!got) dead = true;
         if (!dead) {
           tc_fence_after();
-#pragma unroll 1
+          // D2 (scaled, FP32) into registers, then release the accumulators
+          float d2a[TILE];
+#pragma unroll
+          for (int c = 0; c < TILE; c += 16)
+            load_level_sum16<SCHEME>(tq, c, inv_l, inv_l2, sca2, ctl->scb, d2a + c);
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&ctl->aempty);
+#pragma unroll
           for (int c = 0; c < TILE; c += 32) {
-            float d2[32], d1[32];
-            load_level_sum<SCHEME>(tq, c, inv_l, inv_l2, sca2, ctl->scb, d2);
+            float d1[32];
             tmem_ld32(tq + COL_STASH + (uint32_t)c, d1);
             tc_wait_ld();
             float fos = 0.f, fss = 0.f;
 #pragma unroll
             for (int k = 0; k < 32; ++k) {
               const float r = __frcp_rn(da + ctl->db[c + k]);
-              const float x = d1[k], y = d2[k];
+              const float x = d1[k], y = d2a[c + k];
               fos = fmaf(fmaf(x, x, y * y), r, fos);
               const float df = x - y;
               fss = fmaf(df * df, r, fss);
@@ -413,9 +434,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             uos += (double)fos;
             uss += (double)fss;
           }
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&ctl->aempty);
         }
         ++nuse;
       }

@@ -33,6 +33,8 @@ __host__ __device__ inline size_t slice_tile_offset(int l, int i, int kb, int A,
 __host__ __device__ inline size_t slice_chunk_offset(int row, int chunk) {
   return (size_t)row * 32 + (size_t)((chunk ^ ((row >> 1) & 3)) * 8);
 }
+// naux padded for the tensor-core forms (whole 32-wide Q blocks)
+inline int padded_naux(int naux) { return ((naux + 31) / 32) * 32; }
 inline size_t slice_bytes(int nocc, int nvir, int Qp) {
   return (size_t)3 * nocc * (Qp / 32) * ((nvir + 127) / 128) * 8192;
 }

@@ -113,7 +113,7 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
   cudaStream_t s = static_cast<cudaStream_t>(stream);
 
   const bool tc = precision != CORR_PREC_FP64;
-  const int Qp = ((naux + 31) / 32) * 32;
+  const int Qp = padded_naux(naux);
   const long long R = (long long)nocc * nvir;
   const EnergyShape sh = make_energy_shape(nocc, nvir, naux, tc ? kTcTile : kF64Tile);
   int grid = tc ? ds.sms : 2 * ds.sms;

@@ -25,6 +25,19 @@ __device__ __forceinline__ void tmem_st32(uint32_t taddr, const float* v) {
       : "memory");
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+
 __device__ __forceinline__ void tc_wait_st() {
   asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
@@ -44,6 +57,23 @@ __device__ __forceinline__ void load_level_sum(uint32_t tb, int c, float inv_l, 
   tc_wait_ld();
 #pragma unroll
   for (int k = 0; k < 32; ++k) {
+    const float l1 = SCHEME == 1 ? (a1[k] - a0[k]) - a2[k] : a1[k];
+    const float t = fmaf(a2[k], inv_l2, fmaf(l1, inv_l, a0[k]));
+    d[k] = t * (sca * scb[c + k]);
+  }
+}
+
+// As load_level_sum for 16 columns [c, c+16) (fewer live registers).
+template <int SCHEME>
+__device__ __forceinline__ void load_level_sum16(uint32_t tb, int c, float inv_l, float inv_l2,
+                                                 float sca, const float* scb, float* d) {
+  float a0[16], a1[16], a2[16];
+  tmem_ld16(tb + 0u + (uint32_t)c, a0);
+  tmem_ld16(tb + 128u + (uint32_t)c, a1);
+  tmem_ld16(tb + 256u + (uint32_t)c, a2);
+  tc_wait_ld();
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
     const float l1 = SCHEME == 1 ? (a1[k] - a0[k]) - a2[k] : a1[k];
     const float t = fmaf(a2[k], inv_l2, fmaf(l1, inv_l, a0[k]));
     d[k] = t * (sca * scb[c + k]);
