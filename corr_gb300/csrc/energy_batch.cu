@@ -291,11 +291,24 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       if (!got) dead = true;
       if (!dead) {
         tc_fence_after();
+        // phase-1 result to the stash columns; the accumulators go back to
+        // the MMA issuer before the energy arithmetic (energy_tc.cu)
+#pragma unroll 1
+        for (int c = 0; c < TILE; c += 32) {
+          float d1[32];
+          load_level_sum<SCHEME>(tq, c, inv_l, inv_l2, sca1, ctl->scb, d1);
+          tmem_st32(tq + COL_STASH + (uint32_t)c, d1);
+        }
+        tc_wait_st();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&ctl->aempty);
         if (same) {
 #pragma unroll 1
           for (int c = 0; c < TILE; c += 32) {
             float d1[32];
-            load_level_sum<SCHEME>(tq, c, inv_l, inv_l2, sca1, ctl->scb, d1);
+            tmem_ld32(tq + COL_STASH + (uint32_t)c, d1);
+            tc_wait_ld();
             float fos = 0.f;
 #pragma unroll
             for (int k = 0; k < 32; ++k) {
@@ -310,7 +323,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           for (int k = 0; k < 4; ++k) {
             float d[32];
             const int cw = 32 * ((q + k) & 3);
-            load_level_sum<SCHEME>(tq, cw, inv_l, inv_l2, sca1, ctl->scb, d);
+            tmem_ld32(tq + COL_STASH + (uint32_t)cw, d);
+            tc_wait_ld();
 #pragma unroll
             for (int x = 0; x < 32; ++x) ctl->tbuf[q][lane][x] = d[x];
             named_bar(1, 128);
@@ -319,7 +333,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             float d2[32];
 #pragma unroll
             for (int x = 0; x < 32; ++x) d2[x] = ctl->tbuf[wr][x][lane];
-            load_level_sum<SCHEME>(tq, cr, inv_l, inv_l2, sca1, ctl->scb, d);
+            tmem_ld32(tq + COL_STASH + (uint32_t)cr, d);
+            tc_wait_ld();
             float fos = 0.f, fss = 0.f;
 #pragma unroll
             for (int x = 0; x < 32; ++x) {
@@ -333,18 +348,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             uss += (double)fss;
             named_bar(1, 128);
           }
-        } else {
-#pragma unroll 1
-          for (int c = 0; c < TILE; c += 32) {
-            float d1[32];
-            load_level_sum<SCHEME>(tq, c, inv_l, inv_l2, sca1, ctl->scb, d1);
-            tmem_st32(tq + COL_STASH + (uint32_t)c, d1);
-          }
-          tc_wait_st();
         }
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&ctl->aempty);
       }
       ++nuse;
 
@@ -360,17 +364,23 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         if (!got) dead = true;
         if (!dead) {
           tc_fence_after();
-#pragma unroll 1
+          float d2a[TILE];
+#pragma unroll
+          for (int c = 0; c < TILE; c += 16)
+            load_level_sum16<SCHEME>(tq, c, inv_l, inv_l2, sca2, ctl->scb, d2a + c);
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&ctl->aempty);
+#pragma unroll
           for (int c = 0; c < TILE; c += 32) {
-            float d2[32], d1[32];
-            load_level_sum<SCHEME>(tq, c, inv_l, inv_l2, sca2, ctl->scb, d2);
+            float d1[32];
             tmem_ld32(tq + COL_STASH + (uint32_t)c, d1);
             tc_wait_ld();
             float fos = 0.f, fss = 0.f;
 #pragma unroll
             for (int k = 0; k < 32; ++k) {
               const float r = __frcp_rn(da + ctl->db[c + k]);
-              const float x = d1[k], y = d2[k];
+              const float x = d1[k], y = d2a[c + k];
               fos = fmaf(fmaf(x, x, y * y), r, fos);
               const float df = x - y;
               fss = fmaf(df * df, r, fss);
@@ -378,9 +388,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             uos += (double)fos;
             uss += (double)fss;
           }
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&ctl->aempty);
         }
         ++nuse;
       }
