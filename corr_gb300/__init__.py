@@ -141,6 +141,11 @@ class Context:
         check(self._L.corr_rimp2_energy_batched_async(self._h, n, arr, _prec(precision),
                                                       _ptr(out)))
 
+    def selftest_wait_timeout(self, limit_ms=50):
+        """Run the kernels' bounded-wait path on purpose (raises CorrError with
+        status CORR_ERR_DEVICE_TIMEOUT; the context stays usable)."""
+        check(self._L.corr_selftest_wait_timeout(self._h, int(limit_ms)))
+
     def set_energy_policy(self, cluster):
         """1: multicast cluster form of the energy kernel where it applies; 0: one-CTA form."""
         check(self._L.corr_set_energy_policy(self._h, int(cluster)))

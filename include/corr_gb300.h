@@ -153,6 +153,13 @@ int corr_rimp2_energy_batched(corr_context* ctx, int n, const corr_rimp2_instanc
 int corr_rimp2_energy_batched_async(corr_context* ctx, int n, const corr_rimp2_instance* inst,
                                     int precision, double* energies_dev);
 
+/* Diagnostic (no counterpart in the reference): run the kernels' bounded-wait
+ * path on purpose.  One CTA waits on an mbarrier phase that nothing completes,
+ * with the same primitive every tcgen05-kernel wait uses, for limit_ms
+ * (1..2000) milliseconds; the call then returns CORR_ERR_DEVICE_TIMEOUT and
+ * the context remains usable. */
+int corr_selftest_wait_timeout(corr_context* ctx, int limit_ms);
+
 /* Form of the tcgen05 energy kernel used by corr_rimp2_energy(_async) and
  * corr_rimp2_energy_from_3index (no counterpart in the reference): 0 (the
  * default) = one CTA per work stream; 1 = 2x2 clusters that multicast shared

@@ -45,3 +45,13 @@ def test_no_device_or_bad_args(lib):
     assert lib.corr_create(None, 0, None) == 1  # CORR_ERR_BAD_ARG
     out = _lib.MP2Energy()
     assert lib.corr_rimp2_energy(None, 1, 1, 1, None, None, 0, ctypes.byref(out)) == 1
+
+
+def test_selftest_rejects_bad_limit_without_gpu():
+    """Argument checking of the diagnostic happens before any device work."""
+    import ctypes
+
+    from corr_gb300 import _lib
+
+    L = _lib.load()
+    assert L.corr_selftest_wait_timeout(None, 10) == 1  # CORR_ERR_BAD_ARG
