@@ -146,36 +146,92 @@ __device__ __forceinline__ void row_pass1(const double* __restrict__ b, int naux
   *so = ss;
 }
 
-// Scheme 1: per row r, e_r and the FP64 diagonal (first pass), then the
-// digit statistics of the second pass (a re-read that the L2 serves: a
-// block's rows were read just before) and the largest admissible level
-// exponent k_r, min-reduced into kglob.  Block = 32 rows x QG Q-groups.
+// |x| truncated to FP32 from its IEEE fields (integer operations only; GB300's
+// FP64 pipe is the slow one): relative error below 2^-23, always low; 0 for
+// |x| < 2^-126 and 2^127 for |x| >= 2^128.
+__device__ __forceinline__ float abs_to_float_trunc(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+  const int E = (int)(b >> 52) - 1023;
+  if (E < -126) return 0.0f;
+  if (E > 127) return 1.7014118346046923e38f;
+  return __uint_as_float((unsigned)((E + 127) << 23) | (unsigned)((b >> 29) & 0x7fffffu));
+}
+
+// Pass 1 of scheme 1 over one row slice: max |B| (IEEE bits) and an FP32
+// estimate of sum B^2 (only used to pick the row scale, with a margin).
+__device__ __forceinline__ void row_pass1_est(const double* __restrict__ b, int naux, long long R,
+                                              long long r, int ty, unsigned long long* mo,
+                                              float* so) {
+  unsigned long long m[kUnroll] = {};
+  float s[kUnroll] = {};
+  int q = ty;
+  for (; q + (kUnroll - 1) * QG < naux; q += kUnroll * QG) {
+    double x[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) x[u] = b[(long long)(q + u * QG) * R + r];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      const unsigned long long ax = abs_bits(x[u]);
+      m[u] = ax > m[u] ? ax : m[u];
+      const float f = abs_to_float_trunc(x[u]);
+      s[u] = fmaf(f, f, s[u]);
+    }
+  }
+  for (; q < naux; q += QG) {
+    const double x = b[(long long)q * R + r];
+    const unsigned long long ax = abs_bits(x);
+    m[0] = ax > m[0] ? ax : m[0];
+    const float f = abs_to_float_trunc(x);
+    s[0] = fmaf(f, f, s[0]);
+  }
+  unsigned long long mm = m[0];
+  float ss = s[0];
+#pragma unroll
+  for (int u = 1; u < kUnroll; ++u) {
+    mm = m[u] > mm ? m[u] : mm;
+    ss += s[u];
+  }
+  *mo = mm;
+  *so = ss;
+}
+
+// Scheme 1: per row r, e_r from the row maximum and an FP32 norm estimate
+// (first pass), then, in a second pass (a re-read that the L2 serves: a
+// block's rows were read just before), the digit statistics, the largest
+// admissible level exponent k_r (min-reduced into kglob) and the diagonal
+// sum_Q B^2 from the exact 128-bit integer sum of the fixed-point squares
+// X24^2 (|x - X24 2^-24| <= 2^-25 with ||x|| ~ 2^11.5: relative error below
+// 1e-9).  Block = 32 rows x QG Q-groups.
 __global__ void __launch_bounds__(32 * QG) rowstat_kara_kernel(const double* __restrict__ b,
                                                                int naux, long long R,
                                                                int* __restrict__ erow,
                                                                double* __restrict__ diag,
                                                                int* eref, int* kglob) {
   __shared__ unsigned long long smax[QG][32];
-  __shared__ double ssum[QG][32];
+  __shared__ float ssum[QG][32];
   __shared__ float sb[QG][32], scc[QG][32];
   __shared__ int sa[QG][32], sm0[QG][32];
+  __shared__ unsigned long long sdl[QG][32], sdh[QG][32];
   __shared__ int se[32];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const long long r = (long long)blockIdx.x * 32 + tx;
   unsigned long long m = 0;
-  double s = 0.0;
-  if (r < R) row_pass1(b, naux, R, r, ty, &m, &s);
+  float sf = 0.f;
+  if (r < R) row_pass1_est(b, naux, R, r, ty, &m, &sf);
   smax[ty][tx] = m;
-  ssum[ty][tx] = s;
+  ssum[ty][tx] = sf;
   __syncthreads();
   const double hs = 0.5 * sqrt((double)naux);
   if (ty == 0) {
     int e = INT_MIN / 4;
     if (r < R) {
+      float sfl = sf;
       for (int k = 1; k < QG; ++k) {
         m = smax[k][tx] > m ? smax[k][tx] : m;
-        s += ssum[k][tx];
+        sfl += ssum[k][tx];
       }
+      // the FP32 estimate is low by at most ~2^-22 + (naux + 32) 2^-24 relative
+      const double s = (double)sfl * (1.0 + 0x1p-16 + (double)(naux + 32) * 0x1p-23);
       const bool live = m != 0 && (m >> 52) != 0;
       if (live) {
         const double mx = __longlong_as_double((long long)m);
@@ -186,7 +242,7 @@ __global__ void __launch_bounds__(32 * QG) rowstat_kara_kernel(const double* __r
         atomicMax(eref, e);
       }
       erow[r] = e;
-      diag[r] = s;
+      if (!live) diag[r] = 0.0;
     }
     se[tx] = e;
   }
@@ -195,6 +251,7 @@ __global__ void __launch_bounds__(32 * QG) rowstat_kara_kernel(const double* __r
   const bool live = r < R && e > INT_MIN / 8;
   int a = 0, m0 = 0;
   float bb = 0.f, cc = 0.f;
+  unsigned __int128 dsq = 0;  // exact sum of X24^2 (< 2^72 each)
   if (live) {
 #pragma unroll 4
     for (int q = ty; q < naux; q += QG) {
@@ -202,6 +259,8 @@ __global__ void __launch_bounds__(32 * QG) rowstat_kara_kernel(const double* __r
       const long long h = (X24 + (1ll << 23)) >> 24;
       const float rf = (float)(int)(X24 - (h << 24));
       const int s0 = (int)h;
+      const unsigned long long ax = (unsigned long long)(X24 < 0 ? -X24 : X24);
+      dsq += (unsigned __int128)ax * ax;
       a += s0 * s0;
       m0 = max(m0, abs(s0));
       bb = fmaf((float)s0, rf, bb);
@@ -212,17 +271,27 @@ __global__ void __launch_bounds__(32 * QG) rowstat_kara_kernel(const double* __r
   sm0[ty][tx] = m0;
   sb[ty][tx] = bb;
   scc[ty][tx] = cc;
+  sdl[ty][tx] = (unsigned long long)dsq;
+  sdh[ty][tx] = (unsigned long long)(dsq >> 64);
   __syncthreads();
   if (ty == 0 && live) {
-    double bsum = 0.0, csum = 0.0;
+    // FP32 sums of the FP32 partials: their error (< 2^-19 relative) sits
+    // far inside the 2^-10 margins of the bounds below
+    float bsf = 0.f, csf = 0.f;
+    unsigned __int128 dt = 0;
     for (int k = 0; k < QG; ++k) {
       if (k) {
         a += sa[k][tx];
         m0 = max(m0, sm0[k][tx]);
       }
-      bsum += (double)sb[k][tx];
-      csum += (double)scc[k][tx];
+      bsf += sb[k][tx];
+      csf += scc[k][tx];
+      dt += ((unsigned __int128)sdh[k][tx] << 64) | sdl[k][tx];
     }
+    const double bsum = (double)bsf, csum = (double)csf;
+    // diag = sum X24^2 2^(2e - 48)
+    const double dhi = (double)(unsigned long long)(dt >> 64), dlo = (double)(unsigned long long)dt;
+    diag[r] = ldexp(fma(dhi, 0x1p64, dlo), 2 * e - 48);
     const double A = (double)a, Bx = bsum * 0x1p-24, C = csum * 0x1p-48;
     const double marg = 1.0 + 0x1p-10;
     const double slack = (0.5 + 0x1p-10) * sqrt((double)naux);
