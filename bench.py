@@ -48,8 +48,11 @@ def parse():
     ap.add_argument("--precision", default="split_fp16",
                     choices=["split_fp16", "split_bf16", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="rimp2", choices=["rimp2", "batch256"],
-                    help="batch256: 256 uneven RI-MP2 instances in one batched launch")
+    ap.add_argument("--batch-count", type=int, default=256,
+                    help="instances of the batched workload (256 by default)")
+    ap.add_argument("--workload", default="rimp2", choices=["rimp2", "batch256", "ri_pipeline"],
+                    help="batch256: 256 uneven RI-MP2 instances in one batched launch; "
+                         "ri_pipeline: time-to-E_corr from the 3-index integrals")
     return ap.parse_args()
 
 
@@ -202,9 +205,9 @@ def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    from oracle import oracle as O
+    from corr_gb300 import workloads as W
 
-    B, eps = O.synth_rimp2(NOCC, NVIR, NAUX, SEED)
+    B, eps = W.synth_rimp2(NOCC, NVIR, NAUX, SEED)
     nocc_s = 6  # 36 of the 1600 pair GEMMs per step
     for _ in range(args.warmup):
         cpu_sample(B, eps, nocc_s, min_seconds=0.0, max_reps=1)
@@ -238,7 +241,7 @@ def run_ours(args):
     import torch
 
     import corr_gb300
-    from oracle import oracle as O
+    from corr_gb300 import workloads as W
 
     ws, rank, local = dist_env()
     dist = None
@@ -252,7 +255,7 @@ def run_ours(args):
     dev = torch.cuda.current_device()
     stream = torch.cuda.current_stream()
 
-    B, eps = O.synth_rimp2(NOCC, NVIR, NAUX, SEED)
+    B, eps = W.synth_rimp2(NOCC, NVIR, NAUX, SEED)
     Bd = torch.from_numpy(B).to(dev)
     ed = torch.from_numpy(eps).to(dev)
     ctx = corr_gb300.Context(dev, stream=stream)
@@ -429,11 +432,11 @@ def run_batch(args):
     import torch
 
     import corr_gb300
-    from oracle import oracle as O
+    from corr_gb300 import workloads as W
 
     torch.cuda.set_device(0)
     stream = torch.cuda.current_stream()
-    sizes = O.synth_batch_sizes(256, 5005)
+    sizes = W.synth_batch_sizes(256, 5005)[:max(1, min(256, args.batch_count))]
     g = torch.Generator(device="cuda")
     g.manual_seed(5006)
     items = []
@@ -485,12 +488,12 @@ def run_batch(args):
     e64 = np.array(e64)
     dE = np.abs(split - e64)
     line = {
-        "metric": "batched RI-MP2 instances/s (256 uneven instances)",
+        "metric": f"batched RI-MP2 instances/s ({len(items)} uneven instances)",
         "value": len(items) / (ms * 1e-3), "unit": "instances/s", "n_gpus": 1,
         "steps": steps, "warmup": max(3, args.warmup), "ms_per_step": ms,
         "higher_is_better": True, "dtype": "bf16" if prec == "split_bf16" else "f16",
         "data": "synthetic",
-        "config": {"workload": "256 instances, nocc~U{5..60}, nvir=nocc*U{4..8}, "
+        "config": {"workload": f"{len(items)} instances, nocc~U{{5..60}}, nvir=nocc*U{{4..8}}, "
                                "naux=round(3.5 nvir), seed 5005/5006",
                    "precision": prec, "policy": {"order": order, "stages": stages,
                                                  "autotune_ms": tune_ms},
@@ -504,10 +507,63 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def run_pipeline(args):
+    """RI-MP2 time-to-E_corr from the 3-index integrals at the water-cluster
+    sizes (nbf=480, nocc=100, naux=1520): (P|ia) transform, metric (Cholesky
+    under the inertia certificate, else Jacobi), energy.  Inputs are seeded
+    synthetic stand-ins resident on the GPU (corr_gb300.workloads); the
+    tests run the same pipeline on the molecular integrals.  Split form vs
+    FP64 form of the same call."""
+    import torch
+
+    import corr_gb300
+    from corr_gb300 import workloads as W
+
+    torch.cuda.set_device(0)
+    N, o, X = 480, 100, 1520
+    v = N - o
+    mos, eps, J, P = W.synth_ri_pipeline(N, o, X, 303)
+    ctx = corr_gb300.Context(0)
+    prec = args.precision if args.precision != "fp64" else "split_fp16"
+    for _ in range(max(3, args.warmup)):
+        e_split, ncut = ctx.rimp2_energy_from_3index(2 * o, mos, eps, J, P, prec)
+    steps = max(3, min(args.steps, 10))
+    ts = []
+    for _ in range(steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e_split, ncut = ctx.rimp2_energy_from_3index(2 * o, mos, eps, J, P, prec)
+        ts.append(time.perf_counter() - t0)
+    ms = statistics.median(ts) * 1e3
+    t0 = time.perf_counter()
+    e64, _ = ctx.rimp2_energy_from_3index(2 * o, mos, eps, J, P, "fp64")
+    f64_ms = (time.perf_counter() - t0) * 1e3
+    flops = (2.0 * X * N * N * o + 2.0 * X * o * v * N + 1.0 * X * X * o * v
+             + 2.0 * o * o * v * v * X)
+    line = {
+        "metric": "RI-MP2 time-to-E_corr from 3-index integrals (water-cluster sizes)",
+        "value": ms, "unit": "ms", "n_gpus": 1, "steps": steps, "warmup": max(3, args.warmup),
+        "ms_per_step": ms, "higher_is_better": False,
+        "dtype": "bf16" if prec == "split_bf16" else "f16", "data": "synthetic",
+        "config": {"workload": f"nbf={N} nocc={o} naux={X}, seeded synthetic J, (P|mn), C, eps "
+                               "resident on the GPU (seed 303)", "precision": prec,
+                   "metric_path": "cholesky" if ncut == 0 else f"jacobi, {ncut} cut"},
+        "tflops_algorithmic": flops / (ms * 1e-3) / 1e12,
+        "fp64_form": {"ms": f64_ms, "split_speedup": f64_ms / ms},
+        "energy": {"split": e_split.e_total, "fp64": e64.e_total,
+                   "abs_err_vs_fp64": abs(e_split.e_total - e64.e_total)},
+        "cpu_baseline": None,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "batch256":
         run_batch(args)
+        return
+    if args.workload == "ri_pipeline":
+        run_pipeline(args)
         return
     if args.impl == "reference":
         run_reference(args)

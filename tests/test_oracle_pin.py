@@ -180,3 +180,19 @@ def test_ri_metric_with_cut_eigenvalues_vs_live_reference():
     G_ref = np.einsum("Pmn,Pls->mnls", bpq_ref, bpq_ref)
     G = np.einsum("Pmn,Pls->mnls", bpq, bpq)
     assert np.abs(G - G_ref).max() <= 1e-8 * np.abs(G_ref).max()
+
+
+def test_bench_workloads_match_the_oracle_inputs():
+    """The benchmark's input generators (corr_gb300.workloads) produce the
+    same arrays as the oracle's, so bench lines and parity tests describe the
+    same workload."""
+    import numpy as np
+
+    from corr_gb300 import workloads as W
+    from oracle import oracle as O
+
+    for args in ((3, 20, 40, 7), (40, 360, 64, 2024)):
+        b1, e1 = W.synth_rimp2(*args)
+        b2, e2 = O.synth_rimp2(*args)
+        assert np.array_equal(b1, b2) and np.array_equal(e1, e2)
+    assert W.synth_batch_sizes(256, 5005) == O.synth_batch_sizes(256, 5005)
