@@ -340,7 +340,6 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
   double* out_e = res ? res : c->dres->e;
   const bool tc = precision != CORR_PREC_FP64;
   const int Qp = padded_naux(naux);
-  const long long R = (long long)nocc * nvir;
   const EnergyShape sh = make_energy_shape(nocc, nvir, naux, tc ? kTcTile : kF64Tile);
   const int grid = energy_grid(c, sh, tc);
   SliceWork sw{};

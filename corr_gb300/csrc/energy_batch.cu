@@ -121,8 +121,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
   if (warp == 0) {
     // ------------------------------------------------------------ producer
-    // Lane 0 takes units from the queue and paces the stages; lanes 0-5
-    // issue each stage's six copies in one instruction.
+    // Lane 0 takes units from the queue and paces the stages; lanes 0 and 1
+    // copy a stage's row and column operand (three adjacent planes each).
     {
       int st = 0;
       uint32_t ph = 0;
@@ -130,7 +130,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       bool has[STAGES];
       for (int s = 0; s < STAGES; ++s) has[s] = false;
       bool ok = true;
-      const int l = lane >> 1;
       const bool colop = (lane & 1) != 0;
       for (long long t = 0; ok; ++t) {
         const int slot = (int)(t % RING);
@@ -163,10 +162,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             uint64_t* bar = &ctl->full[st];
             if (lane == 0) mbar_expect_tx(bar, STAGE_BYTES);
             __syncwarp();
-            if (lane < 6)
-              bulk_load(tiles + (size_t)st * STAGE_BYTES + (2 * l + (colop ? 1 : 0)) * TILE_BYTES,
-                        bi.S + slice_tile_offset(l, slab, kb, tile, bi.o, bi.nkb, bi.ntiles),
-                        TILE_BYTES, bar);
+            if (lane < 2)  // the three adjacent planes of the row / column operand
+              bulk_load(tiles + (size_t)st * STAGE_BYTES + 3 * (colop ? 1 : 0) * TILE_BYTES,
+                        bi.S + slice_tile_offset(0, slab, kb, tile, bi.o, bi.nkb, bi.ntiles),
+                        3 * TILE_BYTES, bar);
             has[st] = true;
             last_ph[st] = ph;
             if (++st == STAGES) {
@@ -220,8 +219,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               uint64_t r[3], q[3];
 #pragma unroll
               for (int l = 0; l < 3; ++l) {
-                r[l] = ds + (uint64_t)(((2 * l) * TILE_BYTES + kk * 32) >> 4);
-                q[l] = ds + (uint64_t)(((2 * l + 1) * TILE_BYTES + kk * 32) >> 4);
+                r[l] = ds + (uint64_t)((l * TILE_BYTES + kk * 32) >> 4);
+                q[l] = ds + (uint64_t)(((3 + l) * TILE_BYTES + kk * 32) >> 4);
               }
               const uint32_t acc = (kb | kk) ? 1u : 0u;
               issue_digit_mmas<SCHEME>(c0, c1, c2, r, q, idesc, acc);

@@ -35,8 +35,8 @@
 // outside i <= j < nocc load their share and contribute with weight 0.
 //
 // CTA = 6 warps, persistent, one CTA per SM:
-//   warp 0     bulk-copy producer (lane 0 paces, lanes 0-5 copy), 6 tiles of 128x32 per
-//              stage, 4 stages
+//   warp 0     bulk-copy producer (lane 0 paces; lanes 0-1 copy the row and column
+//              operand, 3 adjacent planes of 128x32 each), 4 stages
 //   warp 1     TMEM owner + MMA issuer (one thread), tcgen05.mma kind::f16
 //   warps 2-5  epilogue, one TMEM lane quarter each
 // Every wait is bounded (common.cuh); on a timeout the CTA winds down and the
@@ -168,9 +168,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       bool has[STAGES];
       for (int s = 0; s < STAGES; ++s) has[s] = false;
       bool ok = true;
-      // lane -> (Q block of the stage, digit plane, row/column operand)
-      const int kbo = lane / 6, l = (lane % 6) >> 1;
+      // Shared-memory slots of a stage: [row operand planes 0-2][column
+      // operand planes 0-2] per 32-wide Q block.  One-CTA form: lane 2 kbo +
+      // colop copies the three adjacent planes of its operand (24 KB).
+      // Cluster form: lane 6 kbo + 2 l + colop copies its 64-row half of one
+      // plane tile.
+      const int kbo = CL ? lane / 6 : lane >> 1;
+      const int l = CL ? (lane % 6) >> 1 : 0;
       const bool colop = (lane & 1) != 0;
+      const int ncopy = CL ? NTILES : 2 * KBS;
       for (long long k = first; k < nwork && ok; k += stride) {
         const Unit w = unit_at<CL>(k, sh, cr, cc);
         for (int phs = 0; phs < w.nph && ok; ++phs) {
@@ -196,14 +202,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             if (lane == 0) mbar_expect_tx(bar, STAGE_BYTES);
             __syncwarp();
             uint8_t* sb =
-                tiles + (size_t)st * STAGE_BYTES + (6 * kbo + 2 * l + (colop ? 1 : 0)) * TILE_BYTES;
-            if (lane < NTILES) {
+                tiles + (size_t)st * STAGE_BYTES + (6 * kbo + 3 * (colop ? 1 : 0) + l) * TILE_BYTES;
+            if (lane < ncopy) {
               const uint16_t* src = S + slice_tile_offset(l, slab, kb, tile, o, nkb, sh.ntiles);
               if (CL)
                 bulk_load_mc(sb + half * HALF_BYTES, src + half * (HALF_BYTES / 2), HALF_BYTES,
                              bar, mask);
               else
-                bulk_load(sb, src, TILE_BYTES, bar);
+                bulk_load(sb, src, 3 * TILE_BYTES, bar);
             }
             has[st] = true;
             last_ph[st] = ph;
@@ -262,8 +268,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               uint64_t r[3], q[3];
 #pragma unroll
               for (int l = 0; l < 3; ++l) {
-                r[l] = ds + (uint64_t)(((6 * kbo + 2 * l) * TILE_BYTES + kk * 32) >> 4);
-                q[l] = ds + (uint64_t)(((6 * kbo + 2 * l + 1) * TILE_BYTES + kk * 32) >> 4);
+                r[l] = ds + (uint64_t)(((6 * kbo + l) * TILE_BYTES + kk * 32) >> 4);
+                q[l] = ds + (uint64_t)(((6 * kbo + 3 + l) * TILE_BYTES + kk * 32) >> 4);
               }
               const uint32_t acc = (ks | j) ? 1u : 0u;
               issue_digit_mmas<SCHEME>(c0, c1, c2, r, q, idesc, acc);

@@ -22,13 +22,16 @@ EnergyShape make_energy_shape(int nocc, int nvir, int naux, int tile);
 
 // ---- slice pre-pass (split.cu) ---------------------------------------------
 // Device buffers of the precision form's pre-pass (R = nocc*nvir rows).
-// Tiled digit layout read by the energy kernels: plane l, occupied i, 32-wide
-// Q block kb, 128-row virtual tile A -> one 8 KB tile of 128 rows x 32 Q
+// Tiled digit layout read by the energy kernels: occupied i, 32-wide Q block
+// kb, 128-row virtual tile A, digit plane l -> one 8 KB tile of 128 rows x 32 Q
 // (16-bit), stored as the 64-byte-swizzled shared-memory image (the 16-byte
-// chunk c of row r sits at chunk c ^ ((r >> 1) & 3)).  Offsets in elements.
+// chunk c of row r sits at chunk c ^ ((r >> 1) & 3)).  The three planes of one
+// (i, kb, A) are adjacent (24 KB), so an operand of a pipeline stage is one
+// copy.  Offsets in elements.
 __host__ __device__ inline size_t slice_tile_offset(int l, int i, int kb, int A, int nocc,
                                                     int nkb, int ntiles) {
-  return ((((size_t)l * nocc + i) * nkb + kb) * ntiles + A) * 4096;
+  (void)nocc;
+  return ((((size_t)i * nkb + kb) * ntiles + A) * 3 + l) * 4096;
 }
 __host__ __device__ inline size_t slice_chunk_offset(int row, int chunk) {
   return (size_t)row * 32 + (size_t)((chunk ^ ((row >> 1) & 3)) * 8);

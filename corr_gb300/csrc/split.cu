@@ -347,7 +347,7 @@ __device__ __forceinline__ uint16_t to16i(int v) {
 }
 
 // B[Q][r] -> digit planes in the tiled layout of the energy kernels
-// (kernels.h, slice_tile_offset): one 8 KB tile per (plane, i, 32-Q block,
+// (kernels.h, slice_tile_offset): one 8 KB tile per (i, 32-Q block, plane,
 // 128-row virtual tile), each stored exactly as the 64-byte-swizzled shared
 // memory image the tensor-core descriptors read, so the kernels fetch a
 // tile with one linear bulk copy.  Rows a >= nvir of the last tile and
@@ -420,7 +420,7 @@ __global__ void __launch_bounds__(256) slice_kernel(const double* __restrict__ b
   }
   const int q = q0 + qc;
   const int nkb = Qp / 32, kb = q / 32, c0 = (q % 32) / 8;
-  const size_t plane = (size_t)nocc * nkb * ntiles * 4096;
+  const size_t plane = 4096;  // the three planes of a tile are adjacent
   const size_t base = slice_tile_offset(0, i, kb, a / 128, nocc, nkb, ntiles);
   const int row = a % 128;
   const size_t at0 = base + slice_chunk_offset(row, c0);
