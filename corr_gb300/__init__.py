@@ -299,6 +299,32 @@ class Context:
                                                     ctypes.byref(out), ctypes.byref(ncut)))
         return out, ncut.value
 
+    # -- dense FP64 helpers (src/MATH/ops_mat.cc) ----------------------------
+    def dgemm(self, A, B, transa=False, transb=False, alpha=1.0, beta=0.0, out=None):
+        """C = alpha op(A) op(B) + beta C for row-major 2-D arrays (mat_mat_T:
+        transb, mat_T_mat: transa).  `out` is read when beta != 0."""
+        m = A.shape[1] if transa else A.shape[0]
+        k = A.shape[0] if transa else A.shape[1]
+        n = B.shape[0] if transb else B.shape[1]
+        if (B.shape[1] if transb else B.shape[0]) != k:
+            raise ValueError("dgemm: inner dimensions differ")
+        if beta != 0.0 and out is None:
+            raise ValueError("dgemm: beta != 0 needs out")
+        out = self._out(A, (m, n), out)
+        check(self._L.corr_dgemm(self._h, int(transa), int(transb), m, n, k, float(alpha), _ptr(A),
+                                 A.shape[1], _ptr(B), B.shape[1], float(beta), _ptr(out), n))
+        return out
+
+    def syev(self, A, w=None, vecs=None):
+        """diag_mat (ops_mat.cc:21): eigenvalues ascending and vecs[k] =
+        eigenvector k of the symmetric matrix A (its row-major lower triangle
+        is read, as dsyev reads it there)."""
+        n = A.shape[0]
+        w = self._out(A, (n,), w)
+        vecs = self._out(A, (n, n), vecs)
+        check(self._L.corr_syev(self._h, n, _ptr(A), _ptr(w), _ptr(vecs)))
+        return w, vecs
+
 
 _DEFAULT = None
 

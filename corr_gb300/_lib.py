@@ -91,6 +91,8 @@ SIGNATURES = {
     "corr_ri_apply_metric": [_vp, _i, _ll, _vp, _vp, _vp],
     "corr_rimp2_energy_from_3index": [_vp, _i, _i, _i, _vp, _vp, _vp, _vp, _i,
                                       ctypes.POINTER(MP2Energy), ctypes.POINTER(_i)],
+    "corr_dgemm": [_vp, _i, _i, _i, _i, _i, _d, _vp, _i, _vp, _i, _d, _vp, _i],
+    "corr_syev": [_vp, _i, _vp, _vp, _vp],
 }
 _RESTYPES = {"corr_version": ctypes.c_char_p, "corr_last_error": ctypes.c_char_p}
 

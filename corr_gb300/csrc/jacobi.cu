@@ -15,6 +15,7 @@
 // Veselic, "Jacobi's method is more accurate than QR", 1992), and sweeps repeat
 // until one sweep rotates no pair (at most 40).  The cutoff and the assembly
 // V f(Lambda) V^T (gemm_fp64.cu) follow the reference.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -123,14 +124,19 @@ __global__ void frob_kernel(const double* __restrict__ A, int n, double* __restr
   }
 }
 
-// Copy J (naux x naux) into the padded n x n work matrix; V = identity.
-__global__ void jacobi_init(const double* __restrict__ J, int m, int n, double* __restrict__ A,
-                            double* __restrict__ V) {
+// Copy the symmetric m x m matrix J into the padded n x n work matrix from one
+// triangle, as dsyev reads it: upper == 1 takes the row-major upper triangle
+// (LAPACKE_dsyev(LAPACK_ROW_MAJOR, 'V', 'U'), ri.cc:49), upper == 0 the
+// row-major lower one (Fortran dsyev with UPLO = 'U' on a row-major array,
+// ops_mat.cc:44).  V = identity.
+__global__ void jacobi_init(const double* __restrict__ J, int m, int n, int upper,
+                            double* __restrict__ A, double* __restrict__ V) {
   const long long nn = (long long)n * n;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn;
        e += (long long)gridDim.x * blockDim.x) {
     const int x = (int)(e / n), y = (int)(e % n);
-    A[e] = (x < m && y < m) ? J[(size_t)x * m + y] : 0.0;
+    const int lo = x < y ? x : y, hi = x < y ? y : x;
+    A[e] = (x < m && y < m) ? (upper ? J[(size_t)lo * m + hi] : J[(size_t)hi * m + lo]) : 0.0;
     V[e] = (x == y) ? 1.0 : 0.0;
   }
 }
@@ -153,6 +159,80 @@ __global__ void take_diag(const double* __restrict__ A, int n, int m, double* __
 
 }  // namespace
 
+// Cyclic sweeps on the padded n x n work matrix A (in place -> eigenvalues on
+// the diagonal) accumulating the rotations into V (columns = eigenvectors),
+// until a sweep rotates no pair (at most 40 sweeps).
+static int jacobi_sweeps(corr_context* c, double* A, double* V, double2* cs, int* rotated,
+                         int n) {
+  cudaStream_t s = c->stream;
+  const int h = n / 2;
+  const long long napply = (long long)h * h + (long long)n * h;
+  const int agrid = (int)((napply + 255) / 256);
+  for (int sweeps = 0; sweeps < 40 && n >= 2; ++sweeps) {
+    CORR_CUDA(cudaMemsetAsync(rotated, 0, sizeof(int), s));
+    for (int r = 0; r < n - 1; ++r) {
+      jacobi_params<<<(h + 127) / 128, 128, 0, s>>>(A, n, r, cs, rotated);
+      jacobi_apply<<<agrid, 256, 0, s>>>(A, V, n, r, cs);
+    }
+    CORR_CUDA(cudaGetLastError());
+    c->launches += 2LL * (n - 1);
+    int hrot = 0;
+    CORR_CUDA(cudaMemcpyAsync(&hrot, rotated, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CORR_CUDA(cudaStreamSynchronize(s));
+    if (!hrot) break;
+  }
+  return CORR_OK;
+}
+
+// vecs[k][x] = V[x][perm[k]] (row k = eigenvector k), w[k] = lam[perm[k]]
+__global__ void gather_eigvecs(const double* __restrict__ V, int n, int m,
+                               const int* __restrict__ perm, double* __restrict__ vecs) {
+  const long long mm = (long long)m * m;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < mm;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(e / m), x = (int)(e % m);
+    vecs[e] = V[(size_t)x * n + perm[k]];
+  }
+}
+
+// Symmetric eigendecomposition (the semantics of diag_mat, src/MATH/ops_mat.cc:21-45,
+// i.e. LAPACK dsyev with JOBZ='V'): eigenvalues ascending into w, eigenvector k
+// as row k of vecs (m x m).  A, w, vecs: device pointers.  Workspace: the
+// caller reserved jacobi_workspace_bytes(m) + m * 4 + 256 bytes at ws.
+int sym_eig_device(corr_context* c, void* ws, const double* Ain, int m, double* w, double* vecs) {
+  const int n = m + (m & 1);
+  Carver cw{ws, 0};
+  double* A = static_cast<double*>(cw.take((size_t)n * n * 8));
+  double* V = static_cast<double*>(cw.take((size_t)n * n * 8));
+  (void)cw.take((size_t)n * n * 8);
+  double2* cs = static_cast<double2*>(cw.take((size_t)n * 16));
+  int* rotated = static_cast<int*>(cw.take((size_t)1024 * 16));
+  int* dperm = static_cast<int*>(cw.take((size_t)m * 4));
+  cudaStream_t s = c->stream;
+  const int ig = (int)std::min<long long>(((long long)n * n + 255) / 256, 4096);
+  jacobi_init<<<ig, 256, 0, s>>>(Ain, m, n, 0, A, V);
+  CORR_CUDA(cudaGetLastError());
+  c->launches += 1;
+  CORR_TRY(jacobi_sweeps(c, A, V, cs, rotated, n));
+  double* dlam = reinterpret_cast<double*>(cs);  // n doubles of room
+  take_diag<<<(m + 255) / 256, 256, 0, s>>>(A, n, m, dlam);
+  std::vector<double> lam(m), ws_sorted(m);
+  std::vector<int> perm(m);
+  CORR_CUDA(cudaMemcpyAsync(lam.data(), dlam, (size_t)m * 8, cudaMemcpyDeviceToHost, s));
+  CORR_CUDA(cudaStreamSynchronize(s));
+  for (int k = 0; k < m; ++k) perm[k] = k;
+  std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return lam[a] < lam[b]; });
+  for (int k = 0; k < m; ++k) ws_sorted[k] = lam[perm[k]];
+  CORR_CUDA(cudaMemcpyAsync(dperm, perm.data(), (size_t)m * 4, cudaMemcpyHostToDevice, s));
+  CORR_CUDA(cudaMemcpyAsync(w, ws_sorted.data(), (size_t)m * 8, cudaMemcpyHostToDevice, s));
+  const int gg = (int)std::min<long long>(((long long)m * m + 255) / 256, 4096);
+  gather_eigvecs<<<gg, 256, 0, s>>>(V, n, m, dperm, vecs);
+  CORR_CUDA(cudaGetLastError());
+  CORR_CUDA(cudaStreamSynchronize(s));  // the host vectors above are read by the copies
+  c->launches += 2;
+  return CORR_OK;
+}
+
 // Eigen-decomposition + reference cutoff + assembly.  J, out: device pointers
 // (m x m).  Workspace carved from c->ws (caller already reserved
 // jacobi_workspace_bytes(m)).
@@ -173,7 +253,7 @@ int ri_inv_sqrt_device(corr_context* c, void* ws, const double* J, int m, double
   double* part = static_cast<double*>(w.take((size_t)fgrid * 16));
   cudaStream_t s = c->stream;
   const int ig = (int)std::min<long long>(((long long)n * n + 255) / 256, 4096);
-  jacobi_init<<<ig, 256, 0, s>>>(J, m, n, A, V);
+  jacobi_init<<<ig, 256, 0, s>>>(J, m, n, 1, A, V);
   CORR_CUDA(cudaGetLastError());
   c->launches += 1;
   std::vector<double> hp((size_t)fgrid * 2);
@@ -187,23 +267,7 @@ int ri_inv_sqrt_device(corr_context* c, void* ws, const double* J, int m, double
     set_error("RI metric is zero");
     return CORR_ERR_NOT_PD;
   }
-  int* rotated = reinterpret_cast<int*>(part);
-  const int h = n / 2;
-  const long long napply = (long long)h * h + (long long)n * h;
-  const int agrid = (int)((napply + 255) / 256);
-  for (int sweeps = 0; sweeps < 40 && n >= 2; ++sweeps) {
-    CORR_CUDA(cudaMemsetAsync(rotated, 0, sizeof(int), s));
-    for (int r = 0; r < n - 1; ++r) {
-      jacobi_params<<<(h + 127) / 128, 128, 0, s>>>(A, n, r, cs, rotated);
-      jacobi_apply<<<agrid, 256, 0, s>>>(A, V, n, r, cs);
-    }
-    CORR_CUDA(cudaGetLastError());
-    c->launches += 2LL * (n - 1);
-    int hrot = 0;
-    CORR_CUDA(cudaMemcpyAsync(&hrot, rotated, sizeof(int), cudaMemcpyDeviceToHost, s));
-    CORR_CUDA(cudaStreamSynchronize(s));
-    if (!hrot) break;
-  }
+  CORR_TRY(jacobi_sweeps(c, A, V, cs, reinterpret_cast<int*>(part), n));
   // eigenvalues -> reference cutoff (ri.cc:56-66) on the host (m values)
   double* dlam = W;  // reuse W's head as a scratch vector before W is written
   take_diag<<<(m + 255) / 256, 256, 0, s>>>(A, n, m, dlam);

@@ -9,9 +9,11 @@
 //   CORR_RIMP2_PRECISION     fp64 (default) | split_fp16 | split_bf16
 #include "corr_shim.h"
 
+#include <climits>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <iomanip>
 #include <iostream>
 #include <mutex>
@@ -126,4 +128,104 @@ void run_canonical_mp2_ri(systeminfo* sysinfo, pHF* postHF) {
 void calculate_ri_from_integrals(int naux, int nroao, const double* J, const double* Pmn,
                                  double* BPQ) {
   check(corr_calculate_ri(ctx(), naux, nroao, J, Pmn, BPQ), "calculate_ri");
+}
+
+void read_transform_ri(std::string prefix, int nroe, int nroao, int naux_2, double* MOs,
+                       double* Bia) {
+  const size_t n = (size_t)naux_2 * nroao * nroao;
+  std::vector<double> bpq(n);
+  std::ifstream f(prefix + ".rimp2", std::ios::binary);
+  if (!f || !f.read(reinterpret_cast<char*>(bpq.data()), (std::streamsize)(n * sizeof(double)))) {
+    std::cerr << "corr_gb300: read_transform_ri cannot read " << n << " doubles from " << prefix
+              << ".rimp2\n";
+    std::abort();
+  }
+  check(corr_transform_ri(ctx(), nroe, nroao, naux_2, MOs, bpq.data(), Bia), "read_transform_ri");
+}
+
+// ---- src/MATH/ops_mat.cc ----------------------------------------------------
+
+namespace {
+
+int dim(long long np, const char* what) {
+  if (np < 1 || np > INT_MAX) {
+    std::cerr << "corr_gb300: " << what << ": matrix size " << np << " out of range\n";
+    std::abort();
+  }
+  return (int)np;
+}
+
+// f = op(a) op(b), n x n row-major
+void square_gemm(int n, int ta, int tb, const double* a, const double* b, double* f,
+                 const char* what) {
+  check(corr_dgemm(ctx(), ta, tb, n, n, n, 1.0, a, n, b, n, 0.0, f, n), what);
+}
+
+}  // namespace
+
+// ops_mat.cc:21-45: dsyev(JOBZ='V', UPLO='U') of a row-major array, i.e. its
+// lower triangle; vals ascending, vecs[k*n + i] = component i of vector k.
+void diag_mat(int nroao, double* mat, double* vals, double* vecs) {
+  check(corr_syev(ctx(), nroao, mat, vals, vecs), "diag_mat");
+}
+
+// ops_mat.cc:53-69: dummat = tmat mat, mat = dummat tmat.
+void symmortho_mat(int nroao, double* mat, double* tmat, double* dummat) {
+  square_gemm(nroao, 0, 0, tmat, mat, dummat, "symmortho_mat");
+  square_gemm(nroao, 0, 0, dummat, tmat, mat, "symmortho_mat");
+}
+
+// ops_mat.cc:75-88: MOs <- MOs tmat^T row by row; tmpvec keeps the last row.
+void transform_MOs(int nroao, double* MOs, double* tmat, double* tmpvec) {
+  const size_t n = (size_t)nroao;
+  std::vector<double> out(n * n);
+  square_gemm(nroao, 0, 1, MOs, tmat, out.data(), "transform_MOs");
+  std::memcpy(MOs, out.data(), n * n * sizeof(double));
+  std::memcpy(tmpvec, out.data() + (n - 1) * n, n * sizeof(double));
+}
+
+// mat_f = mat_i1 mat_i2 (declared at ops_mat.h:5 and :8, used by the
+// commented-out trans_mat of ops_mat.cc:159-190)
+void mat_mat(int np, double* mat_i1, double* mat_i2, double* mat_f) {
+  square_gemm(dim(np, "mat_mat"), 0, 0, mat_i1, mat_i2, mat_f, "mat_mat");
+}
+void mat_mat(long long int np, double* mat_i1, double* mat_i2, double* mat_f) {
+  square_gemm(dim(np, "mat_mat"), 0, 0, mat_i1, mat_i2, mat_f, "mat_mat");
+}
+
+// ops_mat.cc:93-105, :122-134: mat_f = mat_i1 mat_i2^T
+void mat_mat_T(int np, double* mat_i1, double* mat_i2, double* mat_f) {
+  square_gemm(dim(np, "mat_mat_T"), 0, 1, mat_i1, mat_i2, mat_f, "mat_mat_T");
+}
+void mat_mat_T(long long int np, double* mat_i1, double* mat_i2, double* mat_f) {
+  square_gemm(dim(np, "mat_mat_T"), 0, 1, mat_i1, mat_i2, mat_f, "mat_mat_T");
+}
+
+// ops_mat.cc:107-119, :136-148: mat_f = mat_i1^T mat_i2
+void mat_T_mat(int np, double* mat_i1, double* mat_i2, double* mat_f) {
+  square_gemm(dim(np, "mat_T_mat"), 1, 0, mat_i1, mat_i2, mat_f, "mat_T_mat");
+}
+void mat_T_mat(long long int np, double* mat_i1, double* mat_i2, double* mat_f) {
+  square_gemm(dim(np, "mat_T_mat"), 1, 0, mat_i1, mat_i2, mat_f, "mat_T_mat");
+}
+
+// ops_mat.cc:155-190 (declared at ops_mat.h:11-12): dir == 0: tmpmat = mat
+// trans, mat = trans^T tmpmat; otherwise tmpmat = trans mat, mat = tmpmat trans^T.
+void trans_mat(long long int np, double* mat, double* trans, double* tmpmat, int dir) {
+  const int n = dim(np, "trans_mat");
+  if (dir == 0) {
+    square_gemm(n, 0, 0, mat, trans, tmpmat, "trans_mat");
+    square_gemm(n, 1, 0, trans, tmpmat, mat, "trans_mat");
+  } else {
+    square_gemm(n, 0, 0, trans, mat, tmpmat, "trans_mat");
+    square_gemm(n, 0, 1, tmpmat, trans, mat, "trans_mat");
+  }
+}
+void trans_mat(int np, double* mat, double* trans, double* tmpmat, int dir) {
+  trans_mat((long long int)np, mat, trans, tmpmat, dir);
+}
+
+// ops_mat.cc:192-198: vo = mat vi
+void pmv(double* mat, double* vi, double* vo, int nroao) {
+  check(corr_dgemm(ctx(), 0, 0, nroao, 1, nroao, 1.0, mat, nroao, vi, 1, 0.0, vo, 1), "pmv");
 }

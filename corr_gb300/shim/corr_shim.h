@@ -9,8 +9,12 @@
 #ifndef CORR_SHIM_H
 #define CORR_SHIM_H
 
+#include <string>
+
 #ifdef CORR_SHIM_USE_REFERENCE_HEADERS
 #include "UTIL/util.h"
+#include "MATH/ops_mat.h"
+#include "POSTHF/motrans.h"
 #else
 struct pHF {  // src/UTIL/util.h:7-13
   double* FMo;
@@ -65,5 +69,25 @@ void run_canonical_mp2_ri(systeminfo* sysinfo, pHF* postHF);
 // call writes BPQ (caller-allocated naux*nroao*nroao, as main.cc:151 does).
 void calculate_ri_from_integrals(int naux, int nroao, const double* J, const double* Pmn,
                                  double* BPQ);
+// src/POSTHF/motrans.h:12 (defined at ri.cc:109-144): BPQ[naux_2][nroao][nroao]
+// read raw from prefix + ".rimp2", transformed into the caller's Bia.  A
+// missing or short file aborts (the reference would transform uninitialised
+// memory).
+void read_transform_ri(std::string prefix, int nroe, int nroao, int naux_2, double* MOs,
+                       double* Bia);
+
+// Dense FP64 helpers of src/MATH/ops_mat.h, row-major np x np, on the GPU.
+void diag_mat(int nroao, double* mat, double* vals, double* vecs);          // ops_mat.h:3
+void symmortho_mat(int nroao, double* mat, double* tmat, double* dummat);   // ops_mat.h:4
+void transform_MOs(int nroao, double* MOs, double* tmat, double* tmpvec);   // ops_mat.cc:75
+void mat_mat(int np, double* mat_i1, double* mat_i2, double* mat_f);        // ops_mat.h:5
+void mat_mat_T(int np, double* mat_i1, double* mat_i2, double* mat_f);      // ops_mat.h:6
+void mat_T_mat(int np, double* mat_i1, double* mat_i2, double* mat_f);      // ops_mat.h:7
+void mat_mat(long long int np, double* mat_i1, double* mat_i2, double* mat_f);    // ops_mat.h:8
+void mat_mat_T(long long int np, double* mat_i1, double* mat_i2, double* mat_f);  // ops_mat.h:9
+void mat_T_mat(long long int np, double* mat_i1, double* mat_i2, double* mat_f);  // ops_mat.h:10
+void trans_mat(int np, double* mat, double* trans, double* tmpmat, int dir);      // ops_mat.h:11
+void trans_mat(long long int np, double* mat, double* trans, double* tmpmat, int dir);  // :12
+void pmv(double* mat, double* vi, double* vo, int nroao);                   // ops_mat.h:13
 
 #endif

@@ -288,6 +288,27 @@ int corr_rimp2_energy_from_3index(corr_context* ctx, int nroe, int nroao, int na
                                   const double* pmn, int precision, corr_mp2_energy* out,
                                   int* ncut);
 
+/* ---- dense FP64 helpers (src/MATH/ops_mat.cc) ---------------------------- */
+
+/* C = alpha op(A) op(B) + beta C, all row-major FP64: op(A) is m x k (A stored
+ * m x k with lda >= k, or k x m with lda >= m when transa = 1), op(B) is k x n
+ * (B stored k x n, ldb >= n, or n x k, ldb >= k when transb = 1), ldc >= n.
+ * One kernel on the FP64 tensor path.  Covers the reference's mat_mat_T
+ * (ops_mat.cc:93-105, :122-134: transb = 1), mat_T_mat (ops_mat.cc:107-119,
+ * :136-148: transa = 1), symmortho_mat (ops_mat.cc:53-69: two calls),
+ * transform_MOs (ops_mat.cc:75-88: mos tmat^T) and pmv (ops_mat.cc:192-198:
+ * n = 1).  When C is a host pointer and beta != 0 it is read first. */
+int corr_dgemm(corr_context* ctx, int transa, int transb, int m, int n, int k, double alpha,
+               const double* A, int lda, const double* B, int ldb, double beta, double* C,
+               int ldc);
+
+/* Replaces diag_mat (ops_mat.cc:21-45, LAPACK dsyev with JOBZ='V'): the
+ * eigenvalues of the symmetric n x n matrix A in ascending order in w[n], and
+ * vecs[k*n + i] = component i of the eigenvector of w[k] (dsyev's column-major
+ * output read row-major).  Cyclic Jacobi in FP64 on the GPU; each eigenvector's
+ * sign is arbitrary, as LAPACK's.  A is not modified.  n <= 32768. */
+int corr_syev(corr_context* ctx, int n, const double* A, double* w, double* vecs);
+
 #ifdef __cplusplus
 }
 #endif

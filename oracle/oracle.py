@@ -323,3 +323,53 @@ def build_fmo(mos, fmat):
     lib().oracle_build_fmo(N, _p(np.ascontiguousarray(mos)), _p(np.ascontiguousarray(fmat)),
                            _p(out))
     return out
+
+
+# ---------------------------------------------------------------------------
+# Dense helpers: src/MATH/ops_mat.cc, and read_transform_ri (ri.cc:109-144)
+# ---------------------------------------------------------------------------
+
+def diag_mat(mat):
+    """ops_mat.cc:21-45: dsyev(JOBZ='V', UPLO='U') of the row-major array,
+    which LAPACK reads column-major, i.e. the row-major LOWER triangle.
+    Returns (vals ascending, vecs) with vecs[k] = eigenvector of vals[k]."""
+    A = np.tril(np.asarray(mat, dtype=np.float64))
+    A = A + np.tril(A, -1).T
+    w, V = np.linalg.eigh(A)
+    return w, np.ascontiguousarray(V.T)
+
+
+def symmortho_mat(mat, tmat):
+    """ops_mat.cc:53-69: dummat = tmat mat, mat <- dummat tmat.  Returns
+    (new mat, dummat)."""
+    dum = tmat @ mat
+    return dum @ tmat, dum
+
+
+def transform_MOs(mos, tmat):
+    """ops_mat.cc:75-88: MOs[x][y] <- sum_z tmat[y][z] MOs[x][z] = (MOs tmat^T);
+    tmpvec ends as the last transformed row.  Returns (new MOs, tmpvec)."""
+    out = mos @ tmat.T
+    return out, out[-1].copy()
+
+
+def mat_mat_T(a, b):
+    """ops_mat.cc:93-105, :122-134: f = a b^T."""
+    return a @ b.T
+
+
+def mat_T_mat(a, b):
+    """ops_mat.cc:107-119, :136-148: f = a^T b."""
+    return a.T @ b
+
+
+def pmv(mat, vi):
+    """ops_mat.cc:192-198: vo = mat vi."""
+    return mat @ vi
+
+
+def read_transform_ri(path, nroe, nroao, naux, mos):
+    """ri.cc:109-144: BPQ[naux][nroao][nroao] read raw (native doubles) from
+    `path` (prefix + ".rimp2"), then the transform_ri contractions."""
+    bpq = np.fromfile(path, dtype=np.float64, count=naux * nroao * nroao)
+    return transform_ri(nroe, mos, bpq.reshape(naux, nroao, nroao))

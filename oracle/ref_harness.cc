@@ -261,6 +261,12 @@ void ref_transform_ri(int nroe, int nroao, int naux, const double* mos, const do
   transform_ri(&si, &oe, &ph);
 }
 
+// src/POSTHF/ri.cc:109 read_transform_ri: BPQ read from prefix + ".rimp2".
+void ref_read_transform_ri(const char* prefix, int nroe, int nroao, int naux, const double* mos,
+                           double* bia_out) {
+  read_transform_ri(std::string(prefix), nroe, nroao, naux, const_cast<double*>(mos), bia_out);
+}
+
 // The reference's RHF (src/main.cc:102-117): calc_S12, core guess
 // (check_initial_guess, ops_rhf.cc:15), run_scf (scf.cc:145) with 100
 // iterations.  Inputs S, T, V (H = T + V) and the packed ERIs; outputs the MO

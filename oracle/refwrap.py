@@ -126,6 +126,15 @@ def transform_ri(nroe, mos, bpq):
     return out
 
 
+def read_transform_ri(prefix, nroe, nroao, naux, mos):
+    """src/POSTHF/ri.cc:109: Bia from the raw BPQ file prefix + ".rimp2"."""
+    o = nroe // 2
+    out = np.zeros((naux, o, nroao - o))
+    lib().ref_read_transform_ri(str(prefix).encode(), nroe, nroao, naux,
+                                _p(np.ascontiguousarray(mos)), _p(out))
+    return out
+
+
 def rhf(nroe, ion_rep, S, T, V, packed):
     """src/SCF: calc_S12, core guess, run_scf (100 iterations).
     Returns (mos[p][mu], Fmat, MOens, E_HF)."""
@@ -139,3 +148,63 @@ def rhf(nroe, ion_rep, S, T, V, packed):
                   ctypes.c_longlong(packed.nrofint), _p(packed.sortcount, _i64p),
                   _p(packed.intval), _p(packed.intnums, _u16p), _p(mos), _p(f), _p(e), _p(eh))
     return mos, f, e, float(eh[0])
+
+
+# ---- src/MATH/ops_mat.cc (mangled C++ symbols of the unmodified sources) ----
+
+def _sq(*arrs):
+    return [np.ascontiguousarray(a, dtype=np.float64) for a in arrs]
+
+
+def diag_mat(mat):
+    """ops_mat.cc:21 -> (vals, vecs)."""
+    (m,) = _sq(mat)
+    n = m.shape[0]
+    vals, vecs = np.zeros(n), np.zeros((n, n))
+    getattr(lib(), "_Z8diag_matiPdS_S_")(n, _p(m), _p(vals), _p(vecs))
+    return vals, vecs
+
+
+def symmortho_mat(mat, tmat):
+    """ops_mat.cc:53 -> (mat, dummat)."""
+    m, t = _sq(mat, tmat)
+    m = m.copy()
+    dum = np.zeros_like(m)
+    getattr(lib(), "_Z13symmortho_matiPdS_S_")(m.shape[0], _p(m), _p(t), _p(dum))
+    return m, dum
+
+
+def transform_MOs(mos, tmat):
+    """ops_mat.cc:75 -> (MOs, tmpvec)."""
+    c, t = _sq(mos, tmat)
+    c = c.copy()
+    tmp = np.zeros(c.shape[0])
+    getattr(lib(), "_Z13transform_MOsiPdS_S_")(c.shape[0], _p(c), _p(t), _p(tmp))
+    return c, tmp
+
+
+def _mm(sym, a, b, wide):
+    a, b = _sq(a, b)
+    f = np.zeros_like(a)
+    fn = getattr(lib(), sym)
+    fn.argtypes = [ctypes.c_longlong if wide else ctypes.c_int, _dp, _dp, _dp]
+    fn(a.shape[0], _p(a), _p(b), _p(f))
+    return f
+
+
+def mat_mat_T(a, b, wide=False):
+    """ops_mat.cc:93 (int) / :122 (long long)."""
+    return _mm("_Z9mat_mat_TxPdS_S_" if wide else "_Z9mat_mat_TiPdS_S_", a, b, wide)
+
+
+def mat_T_mat(a, b, wide=False):
+    """ops_mat.cc:107 (int) / :136 (long long)."""
+    return _mm("_Z9mat_T_matxPdS_S_" if wide else "_Z9mat_T_matiPdS_S_", a, b, wide)
+
+
+def pmv(mat, vi):
+    """ops_mat.cc:192."""
+    m, v = _sq(mat, vi)
+    vo = np.zeros(m.shape[0])
+    getattr(lib(), "_Z3pmvPdS_S_i")(_p(m), _p(v), _p(vo), m.shape[0])
+    return vo

@@ -55,3 +55,18 @@ def test_selftest_rejects_bad_limit_without_gpu():
 
     L = _lib.load()
     assert L.corr_selftest_wait_timeout(None, 10) == 1  # CORR_ERR_BAD_ARG
+
+
+def test_dense_helpers_reject_bad_args_without_gpu():
+    """corr_dgemm / corr_syev check their arguments before any device work."""
+    import ctypes
+
+    import numpy as np
+
+    from corr_gb300 import _lib
+
+    L = _lib.load()
+    a = np.zeros((2, 2))
+    p = ctypes.c_void_p(a.ctypes.data)
+    assert L.corr_dgemm(None, 0, 0, 2, 2, 2, 1.0, p, 2, p, 2, 0.0, p, 2) == 1
+    assert L.corr_syev(None, 2, p, p, p) == 1

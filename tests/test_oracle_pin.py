@@ -196,3 +196,46 @@ def test_bench_workloads_match_the_oracle_inputs():
         b2, e2 = O.synth_rimp2(*args)
         assert np.array_equal(b1, b2) and np.array_equal(e1, e2)
     assert W.synth_batch_sizes(256, 5005) == O.synth_batch_sizes(256, 5005)
+
+
+def _ops_mat_fixture():
+    import sys
+
+    sys.path.insert(0, GOLD_DIR)
+    import make_golden_ops_mat as M
+
+    return M, np.load(os.path.join(GOLD_DIR, "ops_mat.npz"))
+
+
+@pytest.mark.parametrize("n", [9, 33])
+def test_ops_mat_restatements_vs_golden(n):
+    """oracle.diag_mat & co. against the reference's ops_mat.cc outputs.  The
+    general-matrix case pins the triangle dsyev reads (row-major lower)."""
+    M, g = _ops_mat_fixture()
+    x = M.ops_mat_inputs(n, 500 + n)
+    tol = 1e-13 * n
+    for key in ("sym", "asym"):
+        w, V = O.diag_mat(x[key])
+        pre = f"n{n}_diag_" + ("" if key == "sym" else "asym_")
+        assert np.allclose(w, g[pre + "vals"], rtol=0, atol=tol)
+        # eigenvector signs are arbitrary: compare |<v_k, v_k^ref>|
+        assert np.allclose(np.abs((V * g[pre + "vecs"]).sum(1)), 1.0, atol=1e-10)
+    m, d = O.symmortho_mat(x["sym"], x["t"])
+    assert np.allclose(m, g[f"n{n}_symmortho_mat"], rtol=0, atol=tol)
+    assert np.allclose(d, g[f"n{n}_symmortho_dummat"], rtol=0, atol=tol)
+    c, t = O.transform_MOs(x["a"], x["t"])
+    assert np.allclose(c, g[f"n{n}_transform_MOs"], rtol=0, atol=tol)
+    assert np.allclose(t, g[f"n{n}_transform_MOs_tmpvec"], rtol=0, atol=tol)
+    for suf in ("", "_ll"):
+        assert np.allclose(O.mat_mat_T(x["a"], x["b"]), g[f"n{n}_mat_mat_T{suf}"], rtol=0, atol=tol)
+        assert np.allclose(O.mat_T_mat(x["a"], x["b"]), g[f"n{n}_mat_T_mat{suf}"], rtol=0, atol=tol)
+    assert np.allclose(O.pmv(x["a"], x["v"]), g[f"n{n}_pmv"], rtol=0, atol=tol)
+
+
+def test_read_transform_ri_restatement_vs_golden(tmp_path):
+    M, g = _ops_mat_fixture()
+    naux, N, nocc, seed = M.RI_FILE_CASE
+    bpq, mos = M.ri_file_inputs(naux, N, nocc, seed)
+    bpq.tofile(tmp_path / "case.rimp2")
+    got = O.read_transform_ri(str(tmp_path / "case.rimp2"), 2 * nocc, N, naux, mos)
+    assert np.allclose(got, g["read_transform_ri_bia"], rtol=0, atol=1e-14)

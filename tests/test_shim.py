@@ -13,7 +13,19 @@ REFERENCE_SYMBOLS = [
     "_Z17run_canonical_mp2P10systeminfoP3pHF",            # can_mp2.h:4
     "_Z12transform_riP10systeminfoP6OEintsP3pHF",         # ri.h:9
     "_Z20run_canonical_mp2_riP10systeminfoP3pHF",         # can_mp2.h:5
+    # motrans.h:12 read_transform_ri(std::string, int, int, int, double*, double*)
+    "_Z17read_transform_riNSt7__cxx1112basic_stringIcSt11char_traitsIcESaIcEEEiiiPdS5_",
+    "_Z8diag_matiPdS_S_",                                 # ops_mat.h:3
+    "_Z13symmortho_matiPdS_S_",                           # ops_mat.h:4
+    "_Z13transform_MOsiPdS_S_",                           # ops_mat.cc:75
+    "_Z9mat_mat_TiPdS_S_", "_Z9mat_mat_TxPdS_S_",         # ops_mat.h:6, :9
+    "_Z9mat_T_matiPdS_S_", "_Z9mat_T_matxPdS_S_",         # ops_mat.h:7, :10
+    "_Z3pmvPdS_S_i",                                      # ops_mat.h:13
 ]
+# declared in ops_mat.h:5, 8, 11-12 but defined nowhere in the reference (the
+# definitions in ops_mat.cc:155-190 are commented out); the shim provides them
+DECLARED_ONLY_SYMBOLS = ["_Z7mat_matiPdS_S_", "_Z7mat_matxPdS_S_", "_Z9trans_matiPdS_S_i",
+                         "_Z9trans_matxPdS_S_i"]
 
 
 def _defined(path):
@@ -27,7 +39,7 @@ def test_shim_exports_reference_symbols():
 
     build.build_shim()
     syms = _defined(SHIM_LIB)
-    for s in REFERENCE_SYMBOLS:
+    for s in REFERENCE_SYMBOLS + DECLARED_ONLY_SYMBOLS:
         assert s in syms, s
 
 
