@@ -53,7 +53,7 @@ struct corr_context {
   // batched driver
   bool batch_attrs_set = false;
   int batch_order = 1;   // 0 input order, 1 cost-descending
-  int batch_stages = 4;
+  int batch_stages = 3;
   corr::Workspace batch_out;
   void* pinned = nullptr;
   size_t pinned_cap = 0;

@@ -155,7 +155,7 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
     b.v = x.nvir;
     b.ntiles = s.sh.ntiles;
     b.ntpairs = s.sh.ntpairs;
-    b.nkb = s.Qp / 32;
+    b.nkb = s.Qp / kSliceQ;
     horder[k] = order[k];
     ub += s.sh.nunits;
   }
@@ -202,7 +202,7 @@ extern "C" {
 int corr_set_batch_policy(corr_context* c, int order, int stages) {
   CORR_CHECK_ARG(c != nullptr, "null context");
   CORR_CHECK_ARG(order == 0 || order == 1, "order policy must be 0 (input) or 1 (cost-descending)");
-  CORR_CHECK_ARG(stages == 3 || stages == 4, "stages must be 3 or 4");
+  CORR_CHECK_ARG(stages == 2 || stages == 3, "stages must be 2 or 3");
   c->batch_order = order;
   c->batch_stages = stages;
   return CORR_OK;
@@ -253,7 +253,7 @@ int corr_rimp2_batch_autotune(corr_context* c, int n, const corr_rimp2_instance*
   CORR_CUDA(cudaEventCreate(&e1));
   float best = 1e30f;
   int bo = c->batch_order, bs = c->batch_stages;
-  const int orders[2] = {0, 1}, stages[2] = {4, 3};
+  const int orders[2] = {0, 1}, stages[2] = {3, 2};
   for (int oi = 0; oi < 2; ++oi)
     for (int si = 0; si < 2; ++si) {
       // one untimed warm-up, then the median of three timed runs

@@ -25,14 +25,17 @@ namespace corr {
 namespace {
 
 constexpr int TILE = kTcTile;
-constexpr int KB = 32;
-constexpr int NTILES = 6;
+constexpr int KB = kSliceQ;
 constexpr int TILE_BYTES = TILE * KB * 2;
-constexpr int STAGE_BYTES = NTILES * TILE_BYTES;
+// a stage = the NPL digit planes of the row and of the column operand
+template <int SCHEME>
+constexpr int stage_bytes() {
+  return 2 * planes_for_scheme(SCHEME) * TILE_BYTES;
+}
 constexpr int NTHREADS = 192;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t COL_STASH = 384;
-constexpr uint32_t SW64 = 4;
+constexpr uint32_t SW128 = 2;
 constexpr int RING = 4;
 
 template <int STAGES>
@@ -54,9 +57,9 @@ struct BCtl {
   int wok[2][4];
 };
 
-template <int STAGES>
+template <int STAGES, int SCHEME>
 constexpr size_t batch_smem_bytes() {
-  return (size_t)STAGES * STAGE_BYTES + sizeof(BCtl<STAGES>) + 1024;
+  return (size_t)STAGES * stage_bytes<SCHEME>() + sizeof(BCtl<STAGES>) + 1024;
 }
 
 // Instance of global unit u: last instance whose first unit is <= u.
@@ -91,6 +94,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                         int ninst, long long total, unsigned long long* __restrict__ queue,
                         uint32_t idesc, double* __restrict__ unit_part, int* status) {
   using Ctl = BCtl<STAGES>;
+  constexpr int NPL = planes_for_scheme(SCHEME);
+  constexpr int STAGE_BYTES = stage_bytes<SCHEME>();
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   uint8_t* tiles = smem_raw + (((raw + 1023u) & ~1023u) - raw);
@@ -162,10 +167,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             uint64_t* bar = &ctl->full[st];
             if (lane == 0) mbar_expect_tx(bar, STAGE_BYTES);
             __syncwarp();
-            if (lane < 2)  // the three adjacent planes of the row / column operand
-              bulk_load(tiles + (size_t)st * STAGE_BYTES + 3 * (colop ? 1 : 0) * TILE_BYTES,
-                        bi.S + slice_tile_offset(0, slab, kb, tile, bi.o, bi.nkb, bi.ntiles),
-                        3 * TILE_BYTES, bar);
+            if (lane < 2)  // the NPL adjacent planes of the row / column operand
+              bulk_load(tiles + (size_t)st * STAGE_BYTES + NPL * (colop ? 1 : 0) * TILE_BYTES,
+                        bi.S + slice_tile_offset(0, slab, kb, tile, bi.nkb, bi.ntiles, NPL),
+                        NPL * TILE_BYTES, bar);
             has[st] = true;
             last_ph[st] = ph;
             if (++st == STAGES) {
@@ -189,7 +194,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       uint32_t ph = 0;
       uint32_t nuse = 0;
       bool ok = true;
-      const uint64_t dbase = smem_desc(smem_u32(tiles), 16, 512, SW64);  // tile 0, stage 0
+      const uint64_t dbase = smem_desc(smem_u32(tiles), 16, 1024, SW128);  // tile 0, stage 0
       for (long long t = 0; ok; ++t) {
         const int slot = (int)(t % RING);
         const uint32_t use = (uint32_t)(t / RING);
@@ -216,11 +221,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const uint64_t ds = dbase + (uint64_t)(((uint32_t)st * STAGE_BYTES) >> 4);
 #pragma unroll
             for (int kk = 0; kk < KB / 16; ++kk) {
-              uint64_t r[3], q[3];
+              uint64_t r[NPL], q[NPL];
 #pragma unroll
-              for (int l = 0; l < 3; ++l) {
+              for (int l = 0; l < NPL; ++l) {
                 r[l] = ds + (uint64_t)((l * TILE_BYTES + kk * 32) >> 4);
-                q[l] = ds + (uint64_t)(((3 + l) * TILE_BYTES + kk * 32) >> 4);
+                q[l] = ds + (uint64_t)(((NPL + l) * TILE_BYTES + kk * 32) >> 4);
               }
               const uint32_t acc = (kb | kk) ? 1u : 0u;
               issue_digit_mmas<SCHEME>(c0, c1, c2, r, q, idesc, acc);
@@ -457,21 +462,20 @@ __global__ void batch_reduce_kernel(const BatchInst* __restrict__ insts,
 }  // namespace
 
 size_t batch_kernel_smem(int stages) {
-  return stages == 3 ? batch_smem_bytes<3>() : batch_smem_bytes<4>();
+  return stages == 2 ? batch_smem_bytes<2, kSchemeDigits3>() : batch_smem_bytes<3, kSchemeDigits2>();
 }
 
 template <int STAGES, int SCHEME>
 static cudaError_t set_batch_attr() {
   return cudaFuncSetAttribute(energy_batch_kernel<STAGES, SCHEME>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)batch_smem_bytes<STAGES>());
+                              (int)batch_smem_bytes<STAGES, SCHEME>());
 }
 
 cudaError_t prepare_energy_batch() {
-  cudaError_t e = set_batch_attr<3, kSchemeDigits3>();
-  if (e == cudaSuccess) e = set_batch_attr<4, kSchemeDigits3>();
-  if (e == cudaSuccess) e = set_batch_attr<3, kSchemeKara>();
-  if (e == cudaSuccess) e = set_batch_attr<4, kSchemeKara>();
+  cudaError_t e = set_batch_attr<2, kSchemeDigits3>();
+  if (e == cudaSuccess) e = set_batch_attr<2, kSchemeDigits2>();
+  if (e == cudaSuccess) e = set_batch_attr<3, kSchemeDigits2>();
   return e;
 }
 
@@ -479,31 +483,25 @@ template <int STAGES, int SCHEME>
 static void launch_batch_variant(const BatchInst* insts, int ninst,
                                  long long total, unsigned long long* queue, uint32_t idesc,
                                  int grid, double* unit_part, int* status, cudaStream_t s) {
-  energy_batch_kernel<STAGES, SCHEME><<<grid, NTHREADS, batch_smem_bytes<STAGES>(), s>>>(
+  energy_batch_kernel<STAGES, SCHEME><<<grid, NTHREADS, batch_smem_bytes<STAGES, SCHEME>(), s>>>(
       insts, ninst, total, queue, idesc, unit_part, status);
 }
 
+// stages: 2 or 3 (the three-plane form fits two stages only and always runs 2)
 cudaError_t launch_energy_batch(const BatchInst* insts, int ninst,
                                 long long total, unsigned long long* queue, int fmt, int scheme,
                                 int stages, int grid, double* unit_part, int* status,
                                 cudaStream_t s) {
   const uint32_t idesc = idesc_f16((uint32_t)fmt, TILE, TILE);
-  const bool kara = scheme == kSchemeKara;
-  if (stages == 3) {
-    if (kara)
-      launch_batch_variant<3, kSchemeKara>(insts, ninst, total, queue, idesc, grid,
-                                           unit_part, status, s);
-    else
-      launch_batch_variant<3, kSchemeDigits3>(insts, ninst, total, queue, idesc, grid,
-                                              unit_part, status, s);
-  } else {
-    if (kara)
-      launch_batch_variant<4, kSchemeKara>(insts, ninst, total, queue, idesc, grid,
-                                           unit_part, status, s);
-    else
-      launch_batch_variant<4, kSchemeDigits3>(insts, ninst, total, queue, idesc, grid,
-                                              unit_part, status, s);
-  }
+  if (scheme != kSchemeDigits2)
+    launch_batch_variant<2, kSchemeDigits3>(insts, ninst, total, queue, idesc, grid, unit_part,
+                                            status, s);
+  else if (stages == 3)
+    launch_batch_variant<3, kSchemeDigits2>(insts, ninst, total, queue, idesc, grid, unit_part,
+                                            status, s);
+  else
+    launch_batch_variant<2, kSchemeDigits2>(insts, ninst, total, queue, idesc, grid, unit_part,
+                                            status, s);
   return cudaGetLastError();
 }
 

@@ -1,16 +1,19 @@
 // Precision-form fused RI-MP2 energy on the 5th-generation tensor cores.
 //
-// Input: the three 16-bit integer planes of B (split.cu) in the tiled
-// layout of kernels.h: every 128 x 32 operand tile is one contiguous,
-// pre-swizzled 8 KB block fetched with a linear bulk copy (whole 128-byte
-// lines from L2).
+// Input: the 16-bit integer digit planes of B (split.cu; three in scheme 0,
+// two in scheme 1) in the tiled layout of kernels.h: every 128 x 32 operand
+// tile is one contiguous, pre-swizzled 8 KB block fetched with a linear bulk
+// copy (whole 128-byte lines from L2).
 // Work unit = (occupied pair i<=j, virtual tile pair A<=B), tiles of 128.
 //
 // Phase 1 forms D1[a][b] = (ia|jb) for a in A, b in B; phase 2 forms
 // D2[a][b] = (ib|ja).  Each phase accumulates three exact integer sums in
 // TMEM (split.cu), by scheme:
 //   0: acc_m = sum_{k+l=m} s_k(row) . s_l(col)^T   (m = 0..2, six MMAs per K=16)
-//   1: P0 = s0.s0', Pm = u.u', P2 = s1.s1'        (three MMAs per K=16)
+//   1: acc_0 = s0.s0', acc_1 = s0.s1' + s1.s0', acc_2 = s1.s1'   (four MMAs per K=16)
+// Scheme 1 moves 4 KB of operands per 128x128x16 MMA (two planes of each
+// operand for four MMAs), half of what three planes for three products would:
+// the per-SM operand stream from L2, not the tensor core, bounds these kernels.
 // and the epilogue forms d = sc_row sc_col (value of the digits) in FP32 with
 // round-to-nearest (tc_common.cuh).
 // D1 is parked in TMEM columns 384-511 while D2 accumulates in 0-383.  For
@@ -36,7 +39,7 @@
 //
 // CTA = 6 warps, persistent, one CTA per SM:
 //   warp 0     bulk-copy producer (lane 0 paces; lanes 0-1 copy the row and column
-//              operand, 3 adjacent planes of 128x32 each), 4 stages
+//              operand, the adjacent planes of 128x32 each), 4 (scheme 0) or 6 stages
 //   warp 1     TMEM owner + MMA issuer (one thread), tcgen05.mma kind::f16
 //   warps 2-5  epilogue, one TMEM lane quarter each
 // Every wait is bounded (common.cuh); on a timeout the CTA winds down and the
@@ -50,21 +53,31 @@ namespace corr {
 namespace {
 
 constexpr int TILE = kTcTile;                 // 128
-constexpr int KB = 32;                        // 16-bit Q elements per tile row (64 B)
-constexpr int KBS = 1;                        // 32-wide Q blocks per pipeline stage
-constexpr int STAGES = 4;
-constexpr int NTILES = 6 * KBS;               // KBS x 3 digit planes x (row, column operand)
-constexpr int TILE_BYTES = TILE * KB * 2;     // 8 KB
+constexpr int KB = kSliceQ;                   // 16-bit Q elements per tile row (128 B)
+constexpr int KBS = 1;                        // Q blocks per pipeline stage
+constexpr int TILE_BYTES = TILE * KB * 2;     // 16 KB
 constexpr int HALF_BYTES = TILE_BYTES / 2;    // 64 rows of a tile (cluster form)
-constexpr int STAGE_BYTES = NTILES * TILE_BYTES;
+// Per scheme: NPL digit planes per operand, a stage = KBS x NPL planes x (row,
+// column operand) in a 192 KB ring: 3 stages of two planes (64 KB), 2 of three.
+template <int SCHEME>
+struct Geo {
+  static constexpr int NPL = planes_for_scheme(SCHEME);
+  static constexpr int STAGES = NPL == 2 ? 3 : 2;
+  static constexpr int NTILES = 2 * NPL * KBS;
+  static constexpr int STAGE_BYTES = NTILES * TILE_BYTES;
+};
+constexpr int MAX_STAGES = 3;
+constexpr size_t kRingBytes = (size_t)12 * TILE_BYTES;
+static_assert(Geo<0>::STAGES * Geo<0>::STAGE_BYTES <= (int)kRingBytes, "ring");
+static_assert(Geo<1>::STAGES * Geo<1>::STAGE_BYTES <= (int)kRingBytes, "ring");
 constexpr int NTHREADS = 192;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t COL_STASH = 384;           // parked D1
-constexpr uint32_t SW64 = 4;                  // descriptor layout type: 64B swizzle
+constexpr uint32_t SW128 = 2;                 // descriptor layout type: 128B swizzle
 
 struct Ctl {
-  uint64_t full[STAGES];
-  uint64_t empty[STAGES];
+  uint64_t full[MAX_STAGES];
+  uint64_t empty[MAX_STAGES];
   uint64_t afull;
   uint64_t aempty;
   uint64_t fin;
@@ -77,7 +90,7 @@ struct Ctl {
   int wok[2][4];          // per-warp wait outcome, combined into one decision
 };
 
-constexpr size_t kSmemBytes = (size_t)STAGES * STAGE_BYTES + sizeof(Ctl) + 1024;
+constexpr size_t kSmemBytes = kRingBytes + sizeof(Ctl) + 1024;
 
 struct Unit {
   int i, j, A, B;  // occupied pair (clamped into range) and tile pair
@@ -121,10 +134,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                      const float* __restrict__ sc, const float* __restrict__ dg,
                      const double* __restrict__ scale, EnergyShape sh, int nkb, uint32_t idesc,
                      double* __restrict__ partials, int* status) {
+  using G = Geo<SCHEME>;
+  constexpr int STAGES = G::STAGES, STAGE_BYTES = G::STAGE_BYTES, NPL = G::NPL;
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   uint8_t* tiles = smem_raw + (((raw + 1023u) & ~1023u) - raw);
-  Ctl* ctl = reinterpret_cast<Ctl*>(tiles + (size_t)STAGES * STAGE_BYTES);
+  Ctl* ctl = reinterpret_cast<Ctl*>(tiles + kRingBytes);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int o = sh.nocc, v = sh.nvir;
   // cluster coordinates and multicast groups (rank q = 2r + c)
@@ -168,15 +183,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       bool has[STAGES];
       for (int s = 0; s < STAGES; ++s) has[s] = false;
       bool ok = true;
-      // Shared-memory slots of a stage: [row operand planes 0-2][column
-      // operand planes 0-2] per 32-wide Q block.  One-CTA form: lane 2 kbo +
-      // colop copies the three adjacent planes of its operand (24 KB).
-      // Cluster form: lane 6 kbo + 2 l + colop copies its 64-row half of one
-      // plane tile.
-      const int kbo = CL ? lane / 6 : lane >> 1;
-      const int l = CL ? (lane % 6) >> 1 : 0;
+      // Shared-memory slots of a stage: [row operand planes][column operand
+      // planes] per 32-wide Q block.  One-CTA form: lane 2 kbo + colop copies
+      // the NPL adjacent planes of its operand.  Cluster form: lane
+      // 2 NPL kbo + 2 l + colop copies its 64-row half of one plane tile.
+      const int kbo = CL ? lane / (2 * NPL) : lane >> 1;
+      const int l = CL ? (lane % (2 * NPL)) >> 1 : 0;
       const bool colop = (lane & 1) != 0;
-      const int ncopy = CL ? NTILES : 2 * KBS;
+      const int ncopy = CL ? G::NTILES : 2 * KBS;
       for (long long k = first; k < nwork && ok; k += stride) {
         const Unit w = unit_at<CL>(k, sh, cr, cc);
         for (int phs = 0; phs < w.nph && ok; ++phs) {
@@ -202,14 +216,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             if (lane == 0) mbar_expect_tx(bar, STAGE_BYTES);
             __syncwarp();
             uint8_t* sb =
-                tiles + (size_t)st * STAGE_BYTES + (6 * kbo + 3 * (colop ? 1 : 0) + l) * TILE_BYTES;
+                tiles + (size_t)st * STAGE_BYTES +
+                (2 * NPL * kbo + NPL * (colop ? 1 : 0) + l) * TILE_BYTES;
             if (lane < ncopy) {
-              const uint16_t* src = S + slice_tile_offset(l, slab, kb, tile, o, nkb, sh.ntiles);
+              const uint16_t* src = S + slice_tile_offset(l, slab, kb, tile, nkb, sh.ntiles, NPL);
               if (CL)
                 bulk_load_mc(sb + half * HALF_BYTES, src + half * (HALF_BYTES / 2), HALF_BYTES,
                              bar, mask);
               else
-                bulk_load(sb, src, 3 * TILE_BYTES, bar);
+                bulk_load(sb, src, NPL * TILE_BYTES, bar);
             }
             has[st] = true;
             last_ph[st] = ph;
@@ -243,7 +258,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const uint16_t release = (uint16_t)(grow | gcol);  // this CTA and its two partners
       // shared-memory descriptor of tile 0 of stage 0 (every tile address is
       // below 2^18, so offsets added to the 14-bit start field never carry out)
-      const uint64_t dbase = smem_desc(smem_u32(tiles), 16, 512, SW64);
+      const uint64_t dbase = smem_desc(smem_u32(tiles), 16, 1024, SW128);
       for (long long k = first; k < nwork && ok; k += stride) {
         const Unit w = unit_at<CL>(k, sh, cr, cc);
         for (int phs = 0; phs < w.nph && ok; ++phs) {
@@ -258,18 +273,19 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               ok = false;
               break;
             }
-            tc_fence_after();
+            // (no tcgen05 fence: the bulk copies' mbarrier completion orders
+            // the shared-memory operands)
             // descriptor of this stage: the base descriptor plus the stage's
             // address offset in the 16-byte units of the start-address field
             const uint64_t ds = dbase + (uint64_t)(((uint32_t)st * STAGE_BYTES) >> 4);
 #pragma unroll
             for (int j = 0; j < KBS * (KB / 16); ++j) {
               const int kbo = j / (KB / 16), kk = j % (KB / 16);
-              uint64_t r[3], q[3];
+              uint64_t r[NPL], q[NPL];
 #pragma unroll
-              for (int l = 0; l < 3; ++l) {
-                r[l] = ds + (uint64_t)(((6 * kbo + l) * TILE_BYTES + kk * 32) >> 4);
-                q[l] = ds + (uint64_t)(((6 * kbo + 3 + l) * TILE_BYTES + kk * 32) >> 4);
+              for (int l = 0; l < NPL; ++l) {
+                r[l] = ds + (uint64_t)(((2 * NPL * kbo + l) * TILE_BYTES + kk * 32) >> 4);
+                q[l] = ds + (uint64_t)(((2 * NPL * kbo + NPL + l) * TILE_BYTES + kk * 32) >> 4);
               }
               const uint32_t acc = (ks | j) ? 1u : 0u;
               issue_digit_mmas<SCHEME>(c0, c1, c2, r, q, idesc, acc);
@@ -503,9 +519,9 @@ static cudaError_t launch_variant(int grid, cudaStream_t s, const uint16_t* S, c
 
 cudaError_t prepare_energy_tc(int* max_clusters) {
   cudaError_t e = set_smem_attr<kSchemeDigits3, false>();
-  if (e == cudaSuccess) e = set_smem_attr<kSchemeKara, false>();
+  if (e == cudaSuccess) e = set_smem_attr<kSchemeDigits2, false>();
   if (e == cudaSuccess) e = set_smem_attr<kSchemeDigits3, true>();
-  if (e == cudaSuccess) e = set_smem_attr<kSchemeKara, true>();
+  if (e == cudaSuccess) e = set_smem_attr<kSchemeDigits2, true>();
   if (e != cudaSuccess) return e;
   // how many 4-CTA clusters of this kernel fit on the device at once
   cudaLaunchConfig_t cfg = {};
@@ -520,7 +536,7 @@ cudaError_t prepare_energy_tc(int* max_clusters) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   int n = 0;
-  e = cudaOccupancyMaxActiveClusters(&n, energy_tc_kernel<kSchemeKara, true>, &cfg);
+  e = cudaOccupancyMaxActiveClusters(&n, energy_tc_kernel<kSchemeDigits2, true>, &cfg);
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
     n = 0;  // no cluster form on this device
@@ -540,10 +556,10 @@ cudaError_t launch_energy_tc(const uint16_t* S, const double* eps, const float* 
                              int* status, cudaStream_t s) {
   const uint32_t idesc = idesc_f16((uint32_t)fmt, TILE, TILE);
   const int nkb = Qp / KB;
-  if (scheme == kSchemeKara)
-    return cluster ? launch_variant<kSchemeKara, true>(grid, s, S, eps, sc, dg, scale, sh, nkb,
+  if (scheme == kSchemeDigits2)
+    return cluster ? launch_variant<kSchemeDigits2, true>(grid, s, S, eps, sc, dg, scale, sh, nkb,
                                                        idesc, partials, status)
-                   : launch_variant<kSchemeKara, false>(grid, s, S, eps, sc, dg, scale, sh, nkb,
+                   : launch_variant<kSchemeDigits2, false>(grid, s, S, eps, sc, dg, scale, sh, nkb,
                                                         idesc, partials, status);
   return cluster ? launch_variant<kSchemeDigits3, true>(grid, s, S, eps, sc, dg, scale, sh, nkb,
                                                         idesc, partials, status)

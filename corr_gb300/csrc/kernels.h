@@ -22,28 +22,30 @@ EnergyShape make_energy_shape(int nocc, int nvir, int naux, int tile);
 
 // ---- slice pre-pass (split.cu) ---------------------------------------------
 // Device buffers of the precision form's pre-pass (R = nocc*nvir rows).
-// Tiled digit layout read by the energy kernels: occupied i, 32-wide Q block
-// kb, 128-row virtual tile A, digit plane l -> one 8 KB tile of 128 rows x 32 Q
-// (16-bit), stored as the 64-byte-swizzled shared-memory image (the 16-byte
-// chunk c of row r sits at chunk c ^ ((r >> 1) & 3)).  The three planes of one
-// (i, kb, A) are adjacent (24 KB), so an operand of a pipeline stage is one
-// copy.  Offsets in elements.
-__host__ __device__ inline size_t slice_tile_offset(int l, int i, int kb, int A, int nocc,
-                                                    int nkb, int ntiles) {
-  (void)nocc;
-  return ((((size_t)i * nkb + kb) * ntiles + A) * 3 + l) * 4096;
+// Tiled digit layout read by the energy kernels: occupied i, 64-wide Q block
+// kb, 128-row virtual tile A, digit plane l -> one 16 KB tile of 128 rows x
+// 64 Q (16-bit), stored as the 128-byte-swizzled shared-memory image the
+// tensor-core descriptors read (the 16-byte chunk c of row r sits at chunk
+// c ^ (r & 7)).  The npl planes of one (i, kb, A) are adjacent (npl x 16 KB),
+// so an operand of a pipeline stage is one copy.  Offsets in elements.
+constexpr int kSliceQ = 64;                          // Q per tile row (128 bytes)
+constexpr int kSliceTileElems = 128 * kSliceQ;       // 8192 elements, 16 KB
+__host__ __device__ inline size_t slice_tile_offset(int l, int i, int kb, int A, int nkb,
+                                                    int ntiles, int npl) {
+  return ((((size_t)i * nkb + kb) * ntiles + A) * npl + l) * kSliceTileElems;
 }
 __host__ __device__ inline size_t slice_chunk_offset(int row, int chunk) {
-  return (size_t)row * 32 + (size_t)((chunk ^ ((row >> 1) & 3)) * 8);
+  return (size_t)row * kSliceQ + (size_t)((chunk ^ (row & 7)) * 8);
 }
-// naux padded for the tensor-core forms (whole 32-wide Q blocks)
-inline int padded_naux(int naux) { return ((naux + 31) / 32) * 32; }
+// naux padded for the tensor-core forms (whole 64-wide Q blocks)
+inline int padded_naux(int naux) { return ((naux + kSliceQ - 1) / kSliceQ) * kSliceQ; }
+// bytes of the digit planes (sized for three planes, enough for either scheme)
 inline size_t slice_bytes(int nocc, int nvir, int Qp) {
-  return (size_t)3 * nocc * (Qp / 32) * ((nvir + 127) / 128) * 8192;
+  return (size_t)3 * nocc * (Qp / kSliceQ) * ((nvir + 127) / 128) * (kSliceTileElems * 2);
 }
 
 struct SliceWork {
-  uint16_t* S;     // 3 digit planes in the tiled layout (fp16 or bf16 encoding)
+  uint16_t* S;     // digit planes in the tiled layout (fp16 or bf16 encoding)
   int* erow;       // [R] row exponents
   double* diag;    // [R] FP64 sum_Q B^2
   float* sc;       // [R] 2^(e_r - e_ref)
@@ -52,13 +54,17 @@ struct SliceWork {
   double* scale;   // [2] {global energy factor 2^(4 e_ref), 1/L}
 };
 // Slice schemes (split.cu).  0: three BF16 digits, six products per K step
-// (levels 0..2).  1: two FP16 digits, three Karatsuba products.
+// (levels 0..2).  1: two FP16 digits, four products per K step into three
+// accumulators (s0.s0', s0.s1' + s1.s0', s1.s1').
 constexpr int kSchemeDigits3 = 0;
-constexpr int kSchemeKara = 1;
-inline int scheme_for_precision(int precision) {
-  return precision == 1 /* CORR_PREC_SPLIT_FP16 */ ? kSchemeKara : kSchemeDigits3;
+constexpr int kSchemeDigits2 = 1;
+__host__ __device__ constexpr int planes_for_scheme(int scheme) {
+  return scheme == kSchemeDigits2 ? 2 : 3;
 }
-inline int format_for_scheme(int scheme) { return scheme == kSchemeKara ? 0 : 1; }  // 0 FP16
+inline int scheme_for_precision(int precision) {
+  return precision == 1 /* CORR_PREC_SPLIT_FP16 */ ? kSchemeDigits2 : kSchemeDigits3;
+}
+inline int format_for_scheme(int scheme) { return scheme == kSchemeDigits2 ? 0 : 1; }  // 0 FP16
 int slice_bits_for(int Qp);
 cudaError_t launch_slices(const double* b, int naux, int nocc, int nvir, int Qp, int scheme,
                           int fmt, int p, SliceWork w, cudaStream_t s);

@@ -15,34 +15,42 @@
 // ~2^-21 of the row maximum, round-to-nearest and unbiased.
 //
 // The diagonal elements (ia|ia) = sum_Q (B^Q_ia)^2 are all-positive sums that
-// dominate the bias of any truncated scheme; they are formed here in FP64 and
-// substituted by the energy kernel.
+// dominate the bias of any truncated scheme; they are formed here to FP64
+// accuracy and substituted by the energy kernel.
 //
-// Scheme 1 (FP16 slices, Karatsuba): two digits per element,
+// Scheme 1 (FP16 slices): two digits per element,
 //
 //   B^Q_r = 2^(e_r) (s0 + s1/L),   s0 = round(x), s1 = round(L (x - s0)),
-//   x = B^Q_r 2^(-e_r),  u = s0 + s1,
+//   x = B^Q_r 2^(-e_r),
 //
-// and three products per pair of rows (Karatsuba's identity for the cross term),
+// and four products per pair of rows into three accumulators,
 //
-//   P0 = s0.s0',  Pm = u.u',  P2 = s1.s1',
-//   x.x' = P0 + (Pm - P0 - P2)/L + P2/L^2   (exact for the two-digit values).
+//   acc_0 = s0.s0',  acc_1 = s0.s1' + s1.s0',  acc_2 = s1.s1',
+//   x.x' = acc_0 + acc_1/L + acc_2/L^2   (exact for the two-digit values).
 //
 // Dropping the s1.s1' product (plain two-term hi/lo splitting) loses every
-// product of two sub-digit elements and biases molecular energies; the
-// Karatsuba form keeps it at the cost of three products, not four.  Each of
-// P0, Pm, P2 is a tensor-core sum of integer products, exact in FP32 when
-// every partial sum stays below 2^24; by Cauchy-Schwarz that holds when
-// ||s0||, ||u||, ||s1|| <= 2^12 for every row, which the pre-pass enforces:
-//   e_r: ||x|| <= 2^11.5 - sqrt(naux)/2 - 1 and max|x| <= 2^11 - 2^9 - 1;
+// product of two sub-digit elements and biases molecular energies, so it is
+// kept.  (Karatsuba's identity would need three products, but a third plane
+// s0 + s1 per operand: more operand bytes per product, and the operand stream
+// is what bounds the kernel.)  Each accumulator is a tensor-core sum of
+// integer products, exact in FP32 when every partial sum stays within 2^24;
+// by Cauchy-Schwarz that holds when ||s0||, ||s1|| <= 2^11.5 for every row
+// (acc_1 <= 2 2^11.5 2^11.5), which the pre-pass enforces:
+//   e_r: ||x|| <= 2^11.5 - sqrt(naux)/2 - 1 and max|x| <= 2^11 - 2^9 - 1
+//        (so ||s0|| <= 2^11.5 - 1 and |s0| <= 2^11: exact in FP16);
 //   L = 2^k, the largest k <= 10 such that for every row
-//     ||s0 + L r|| + (1/2 + 2^-10) sqrt(naux) <= 2^12   (bounds ||u||),
-//     L ||r|| + (1/2 + 2^-10) sqrt(naux) <= 2^12        (bounds ||s1||),
-//     max|s0| + L/2 <= 2^11                            (u exact in FP16),
-//   with r = x - s0 and the row sums a = ||s0||^2, b = s0.r, c = ||r||^2 taken
-//   in a second pass over the row (a exact, b and c with a 2^-10 margin).
+//     L ||r|| + (1/2 + 2^-10) sqrt(naux) <= 2^11.5     (bounds ||s1||),
+//   with r = x - s0 and c = ||r||^2 taken in a second pass over the row (FP32,
+//   with a 2^-10 margin); |s1| <= L/2 <= 2^9.
+// Digits come from the 20-bit fixed-point value X20 = round(x 2^20) (32-bit
+// integer arithmetic on the IEEE fields): s0 = round(X20 / 2^20), r = X20 2^-20
+// - s0, s1 = round(L r).  The diagonal sum_Q B^2 is the exact integer sum of
+// floor(X20^2 / 2^10) (relative error ~1e-10).  Per element the pre-pass uses
+// no FP64 instruction: GB300's FP64 pipe is ~2 operations per clock per SM.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+
+#include <atomic>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -56,46 +64,6 @@ __device__ __forceinline__ unsigned long long abs_bits(double x) {
   return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
 }
 
-// round(b * 2^k) to nearest (ties away from zero) by integer arithmetic on the
-// IEEE-754 fields; exact for every |result| < 2^31.  Zero and subnormal b map
-// to 0 (their contribution lies far below the row scale).
-__device__ __forceinline__ int round_scaled(double b, int k) {
-  const long long bits = __double_as_longlong(b);
-  const int E = (int)((bits >> 52) & 0x7ff);
-  if (E == 0) return 0;
-  const long long m = (bits & 0xfffffffffffffll) | (1ll << 52);
-  const int sh = 1075 - E - k;  // value = m * 2^-sh
-  long long X;
-  if (sh <= 0) X = m << (-sh > 10 ? 10 : -sh);  // not reached for |b| <= row max
-  else if (sh > 62) X = 0;
-  else X = (m + (1ll << (sh - 1))) >> sh;
-  return bits < 0 ? -(int)X : (int)X;
-}
-
-// round(b * 2^k) as a 64-bit integer (same rounding as round_scaled); exact
-// for |result| < 2^62.
-__device__ __forceinline__ long long round_scaled64(double b, int k) {
-  const long long bits = __double_as_longlong(b);
-  const int E = (int)((bits >> 52) & 0x7ff);
-  if (E == 0) return 0;
-  const long long m = (bits & 0xfffffffffffffll) | (1ll << 52);
-  const int sh = 1075 - E - k;
-  long long X;
-  if (sh <= 0) X = m << (-sh > 9 ? 9 : -sh);  // not reached for |x| < 2^11
-  else if (sh > 62) X = 0;
-  else X = (m + (1ll << (sh - 1))) >> sh;
-  return bits < 0 ? -X : X;
-}
-
-// Scheme-1 digits of one element from its 24-bit fixed-point value
-// X24 = round(x 2^24): s0 = round(x) (ties up), r24 = X24 - s0 2^24.
-__device__ __forceinline__ void kara_digits(long long X24, int k, int* s0, int* s1) {
-  const long long h = (X24 + (1ll << 23)) >> 24;
-  const int r24 = (int)(X24 - (h << 24));
-  *s0 = (int)h;
-  *s1 = (r24 + (1 << (23 - k))) >> (24 - k);
-}
-
 // smallest e with y 2^-e <= 1 (y > 0)
 __device__ __forceinline__ int ceil_log2(double y) {
   int k;
@@ -103,7 +71,95 @@ __device__ __forceinline__ int ceil_log2(double y) {
   return f == 0.5 ? k - 1 : k;
 }
 
-constexpr int kKaraMaxK = 10;
+constexpr int kMaxLevelExp = 10;
+
+// round(b * 2^c) to nearest (ties away from zero) by 32-bit integer
+// arithmetic on the IEEE-754 fields; exact whenever |b 2^c| < 2^31 (callers
+// guarantee |b 2^c| < 2^31 - 1).  Zero and subnormal b map to 0 (their
+// contribution lies far below the row scale).  With m the 53-bit significand,
+// b 2^c = m 2^-(sh) and round = ((m >> (sh - 1)) + 1) >> 1, where
+// m >> (sh - 1) < 2^32 because sh - 1 >= 21.
+__device__ __forceinline__ int round_scaled32(double b, int c) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(b);
+  const unsigned hi = (unsigned)(bits >> 32), lo = (unsigned)bits;
+  const int E = (int)((hi >> 20) & 0x7ffu);
+  const unsigned m21 = __funnelshift_l(lo, (hi & 0xfffffu) | 0x100000u, 11);  // m >> 21
+  const unsigned sh = (unsigned)(1074 - E - c - 21);  // (sh - 1) - 21; "negative" = huge
+  const unsigned t = sh < 32u ? (m21 >> sh) : 0u;
+  const int X = (int)((t + 1u) >> 1);
+  return E == 0 ? 0 : ((int)hi < 0 ? -X : X);
+}
+
+// Small integer (|v| < 2^22) to FP32 on the integer and FP32 pipes.
+__device__ __forceinline__ float small_int_to_float(int v) {
+  return __int_as_float(0x4b400000 + v) - 12582912.0f;
+}
+
+// Scheme-1 digits of one element from its 20-bit fixed-point value
+// X20 = round(x 2^20) (|x| < 2^11): s0 = round(x) (ties up),
+// r20 = X20 - s0 2^20, s1 = round(r20 2^(k - 20)) (ties up), k <= 10.
+__device__ __forceinline__ void digits2(int X20, int k, int* s0, int* s1) {
+  const int h = (X20 + (1 << 19)) >> 20;
+  const int r20 = X20 - (h << 20);
+  *s0 = h;
+  *s1 = (r20 + (1 << (19 - k))) >> (20 - k);
+}
+
+// Pass-1 contribution of one element: the high word of |x| (the maximum of
+// these bounds max |x| from above) and |x| truncated to FP32 from that word
+// (20 significand bits: low by less than 2^-20 relative; 0 below 2^-126,
+// FLT_MAX above).
+__device__ __forceinline__ void pass1_elem(double x, unsigned* mhi, float* sf) {
+  const unsigned h = (unsigned)((unsigned long long)__double_as_longlong(x) >> 32) & 0x7fffffffu;
+  *mhi = h > *mhi ? h : *mhi;
+  int t = (int)h - (896 << 20);
+  t = t < 0 ? 0 : (t > 0x0fefffff ? 0x0fefffff : t);
+  const float f = __int_as_float(t << 3);
+  *sf = fmaf(f, f, *sf);
+}
+
+// Pass-2 statistics of a row at scale e (scheme 1): c = sum r20^2 (FP32)
+// and the diagonal as the exact integer sum of floor(X20^2 / 2^10) (< 2^53 for
+// any row the scale admits: ||x|| <= 2^11.5).
+struct RowStats2 {
+  float c = 0.f;
+  unsigned long long d = 0;
+};
+
+__device__ __forceinline__ void pass2_elem(double x, int e, RowStats2& st) {
+  const int X = round_scaled32(x, 20 - e);
+  const int s0 = (X + (1 << 19)) >> 20;
+  const float fr = small_int_to_float(X - (s0 << 20));
+  st.c = fmaf(fr, fr, st.c);
+  st.d += (unsigned long long)((long long)X * X) >> 10;
+}
+
+// Row scale e_r of scheme 1 from the pass-1 results: ||x|| <= 2^11.5 -
+// sqrt(naux)/2 - 1 (from the FP32 estimate with its error margin) and
+// max|x| <= 2^11 - 2^9 - 1 (from the upper bound mhi + 1).  INT_MIN/4 for a
+// row without normal elements.
+__device__ __forceinline__ int row_scale2(unsigned mhi, float sfl, int naux) {
+  if ((mhi >> 20) == 0) return INT_MIN / 4;
+  // the FP32 estimate is low by at most ~2^-19 + (naux + 32) 2^-24 relative
+  const double sest = (double)sfl * (1.0 + 0x1p-16 + (double)(naux + 32) * 0x1p-23);
+  const double mx = __longlong_as_double((long long)((unsigned long long)(mhi + 1u) << 32));
+  const double t0 = 2896.309375740099 - 0.5 * sqrt((double)naux) - 1.0;
+  const int en = ceil_log2(sqrt(sest) / t0);
+  const int ec = ceil_log2(mx / (2048.0 - 512.0 - 1.0));
+  return en > ec ? en : ec;
+}
+
+// Largest level exponent k (L = 2^k, 0 <= k <= 10) that keeps ||s1|| <= 2^11.5
+// for a row with pass-2 statistics st; also writes the row's diagonal
+// sum_Q B^2.  The FP32 sum c is low by at most ~2^-19 relative: margin 2^-10.
+__device__ __forceinline__ int row_level2(const RowStats2& st, int e, int naux, double* diag) {
+  *diag = ldexp((double)st.d, 2 * e - 30);
+  const double C = (double)st.c * 0x1p-40 * (1.0 + 0x1p-10);
+  const double slack = (0.5 + 0x1p-10) * sqrt((double)naux);
+  int k = kMaxLevelExp;
+  while (k > 0 && ldexp(sqrt(C), k) + slack > 2896.309375740099) --k;  // 2^11.5
+  return k;
+}
 
 // Row statistics are taken by blocks of 32 rows x QG Q-groups: for a fixed
 // Q the 32 threads of a warp read 32 consecutive rows (coalesced), and every
@@ -146,23 +202,10 @@ __device__ __forceinline__ void row_pass1(const double* __restrict__ b, int naux
   *so = ss;
 }
 
-// |x| truncated to FP32 from its IEEE fields (integer operations only; GB300's
-// FP64 pipe is the slow one): relative error below 2^-23, always low; 0 for
-// |x| < 2^-126 and 2^127 for |x| >= 2^128.
-__device__ __forceinline__ float abs_to_float_trunc(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
-  const int E = (int)(b >> 52) - 1023;
-  if (E < -126) return 0.0f;
-  if (E > 127) return 1.7014118346046923e38f;
-  return __uint_as_float((unsigned)((E + 127) << 23) | (unsigned)((b >> 29) & 0x7fffffu));
-}
-
-// Pass 1 of scheme 1 over one row slice: max |B| (IEEE bits) and an FP32
-// estimate of sum B^2 (only used to pick the row scale, with a margin).
+// Pass 1 of scheme 1 over one row slice (strided by QG in Q).
 __device__ __forceinline__ void row_pass1_est(const double* __restrict__ b, int naux, long long R,
-                                              long long r, int ty, unsigned long long* mo,
-                                              float* so) {
-  unsigned long long m[kUnroll] = {};
+                                              long long r, int ty, unsigned* mo, float* so) {
+  unsigned m[kUnroll] = {};
   float s[kUnroll] = {};
   int q = ty;
   for (; q + (kUnroll - 1) * QG < naux; q += kUnroll * QG) {
@@ -170,21 +213,10 @@ __device__ __forceinline__ void row_pass1_est(const double* __restrict__ b, int 
 #pragma unroll
     for (int u = 0; u < kUnroll; ++u) x[u] = b[(long long)(q + u * QG) * R + r];
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) {
-      const unsigned long long ax = abs_bits(x[u]);
-      m[u] = ax > m[u] ? ax : m[u];
-      const float f = abs_to_float_trunc(x[u]);
-      s[u] = fmaf(f, f, s[u]);
-    }
+    for (int u = 0; u < kUnroll; ++u) pass1_elem(x[u], &m[u], &s[u]);
   }
-  for (; q < naux; q += QG) {
-    const double x = b[(long long)q * R + r];
-    const unsigned long long ax = abs_bits(x);
-    m[0] = ax > m[0] ? ax : m[0];
-    const float f = abs_to_float_trunc(x);
-    s[0] = fmaf(f, f, s[0]);
-  }
-  unsigned long long mm = m[0];
+  for (; q < naux; q += QG) pass1_elem(b[(long long)q * R + r], &m[0], &s[0]);
+  unsigned mm = m[0];
   float ss = s[0];
 #pragma unroll
   for (int u = 1; u < kUnroll; ++u) {
@@ -195,33 +227,28 @@ __device__ __forceinline__ void row_pass1_est(const double* __restrict__ b, int 
   *so = ss;
 }
 
-// Scheme 1: per row r, e_r from the row maximum and an FP32 norm estimate
-// (first pass), then, in a second pass (a re-read that the L2 serves: a
-// block's rows were read just before), the digit statistics, the largest
-// admissible level exponent k_r (min-reduced into kglob) and the diagonal
-// sum_Q B^2 from the exact 128-bit integer sum of the fixed-point squares
-// X24^2 (|x - X24 2^-24| <= 2^-25 with ||x|| ~ 2^11.5: relative error below
-// 1e-9).  Block = 32 rows x QG Q-groups.
-__global__ void __launch_bounds__(32 * QG) rowstat_kara_kernel(const double* __restrict__ b,
-                                                               int naux, long long R,
-                                                               int* __restrict__ erow,
-                                                               double* __restrict__ diag,
-                                                               int* eref, int* kglob) {
-  __shared__ unsigned long long smax[QG][32];
+// Scheme 1 row statistics, two passes over global memory (the form for naux
+// too large to stage a block's rows in shared memory): per row r, e_r from the
+// first pass (row_scale2), then the pass-2 statistics (pass2_elem), the level
+// exponent k_r (min-reduced into kglob) and the diagonal.  Block = 32 rows x QG
+// Q-groups; partial results summed over the Q-groups in order.
+__global__ void __launch_bounds__(32 * QG) rowstat2_kernel(const double* __restrict__ b,
+                                                           int naux, long long R,
+                                                           int* __restrict__ erow,
+                                                           double* __restrict__ diag, int* eref,
+                                                           int* kglob) {
+  __shared__ unsigned smax[QG][32];
   __shared__ float ssum[QG][32];
-  __shared__ float sb[QG][32], scc[QG][32];
-  __shared__ int sa[QG][32], sm0[QG][32];
-  __shared__ unsigned long long sdl[QG][32], sdh[QG][32];
+  __shared__ unsigned long long sd[QG][32];
   __shared__ int se[32];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const long long r = (long long)blockIdx.x * 32 + tx;
-  unsigned long long m = 0;
+  unsigned m = 0;
   float sf = 0.f;
   if (r < R) row_pass1_est(b, naux, R, r, ty, &m, &sf);
   smax[ty][tx] = m;
   ssum[ty][tx] = sf;
   __syncthreads();
-  const double hs = 0.5 * sqrt((double)naux);
   if (ty == 0) {
     int e = INT_MIN / 4;
     if (r < R) {
@@ -230,80 +257,137 @@ __global__ void __launch_bounds__(32 * QG) rowstat_kara_kernel(const double* __r
         m = smax[k][tx] > m ? smax[k][tx] : m;
         sfl += ssum[k][tx];
       }
-      // the FP32 estimate is low by at most ~2^-22 + (naux + 32) 2^-24 relative
-      const double s = (double)sfl * (1.0 + 0x1p-16 + (double)(naux + 32) * 0x1p-23);
-      const bool live = m != 0 && (m >> 52) != 0;
-      if (live) {
-        const double mx = __longlong_as_double((long long)m);
-        const double t0 = 2896.309375740099 - hs - 1.0;  // 2^11.5 - sqrt(naux)/2 - 1
-        const int en = ceil_log2(sqrt(s) / t0);
-        const int ec = ceil_log2(mx / (2048.0 - 512.0 - 1.0));
-        e = en > ec ? en : ec;
-        atomicMax(eref, e);
-      }
+      e = row_scale2(m, sfl, naux);
+      if (e > INT_MIN / 8) atomicMax(eref, e);
       erow[r] = e;
-      if (!live) diag[r] = 0.0;
+      if (e <= INT_MIN / 8) diag[r] = 0.0;
     }
     se[tx] = e;
   }
   __syncthreads();
   const int e = se[tx];
   const bool live = r < R && e > INT_MIN / 8;
-  int a = 0, m0 = 0;
-  float bb = 0.f, cc = 0.f;
-  unsigned __int128 dsq = 0;  // exact sum of X24^2 (< 2^72 each)
+  RowStats2 st;
   if (live) {
 #pragma unroll 4
-    for (int q = ty; q < naux; q += QG) {
-      const long long X24 = round_scaled64(b[(long long)q * R + r], 24 - e);
-      const long long h = (X24 + (1ll << 23)) >> 24;
-      const float rf = (float)(int)(X24 - (h << 24));
-      const int s0 = (int)h;
-      const unsigned long long ax = (unsigned long long)(X24 < 0 ? -X24 : X24);
-      dsq += (unsigned __int128)ax * ax;
-      a += s0 * s0;
-      m0 = max(m0, abs(s0));
-      bb = fmaf((float)s0, rf, bb);
-      cc = fmaf(rf, rf, cc);
-    }
+    for (int q = ty; q < naux; q += QG) pass2_elem(b[(long long)q * R + r], e, st);
   }
-  sa[ty][tx] = a;
-  sm0[ty][tx] = m0;
-  sb[ty][tx] = bb;
-  scc[ty][tx] = cc;
-  sdl[ty][tx] = (unsigned long long)dsq;
-  sdh[ty][tx] = (unsigned long long)(dsq >> 64);
+  ssum[ty][tx] = st.c;
+  sd[ty][tx] = st.d;
   __syncthreads();
   if (ty == 0 && live) {
-    // FP32 sums of the FP32 partials: their error (< 2^-19 relative) sits
-    // far inside the 2^-10 margins of the bounds below
-    float bsf = 0.f, csf = 0.f;
-    unsigned __int128 dt = 0;
-    for (int k = 0; k < QG; ++k) {
-      if (k) {
-        a += sa[k][tx];
-        m0 = max(m0, sm0[k][tx]);
-      }
-      bsf += sb[k][tx];
-      csf += scc[k][tx];
-      dt += ((unsigned __int128)sdh[k][tx] << 64) | sdl[k][tx];
+    for (int k = 1; k < QG; ++k) {
+      st.c += ssum[k][tx];
+      st.d += sd[k][tx];
     }
-    const double bsum = (double)bsf, csum = (double)csf;
-    // diag = sum X24^2 2^(2e - 48)
-    const double dhi = (double)(unsigned long long)(dt >> 64), dlo = (double)(unsigned long long)dt;
-    diag[r] = ldexp(fma(dhi, 0x1p64, dlo), 2 * e - 48);
-    const double A = (double)a, Bx = bsum * 0x1p-24, C = csum * 0x1p-48;
-    const double marg = 1.0 + 0x1p-10;
-    const double slack = (0.5 + 0x1p-10) * sqrt((double)naux);
-    const double bpos = Bx + 0x1p-10 * sqrt(A * C * marg);  // upper bound on s0.r
-    int k = kKaraMaxK;
-    for (; k > 0; --k) {
-      const double L = (double)(1 << k);
-      const double nu2 = A + 2.0 * L * bpos + L * L * C * marg;
-      const bool ok = sqrt(nu2 > 0.0 ? nu2 : 0.0) + slack <= 4096.0 &&
-                      L * sqrt(C * marg) + slack <= 4096.0 && m0 + (1 << (k - 1)) <= 2048;
-      if (ok) break;
+    double dg;
+    const int k = row_level2(st, e, naux, &dg);
+    diag[r] = dg;
+    atomicMin(kglob, k);
+  }
+}
+
+// 8-byte asynchronous global -> shared copy (zero-filled when !valid).
+__device__ __forceinline__ void cp_async8(void* dst, const void* src, bool valid) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(smem_u32(dst)), "l"(src),
+               "r"(valid ? 8 : 0)
+               : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n" "cp.async.wait_group 0;\n" ::: "memory");
+}
+
+// Scheme 1 row statistics with each block's rows staged in shared memory:
+// the same e_r, k_r and diagonal as rowstat2_kernel (the same per-element
+// helpers), but B is read from HBM once (8-byte asynchronous copies, every
+// element of the block in flight at once) and both passes run from shared
+// memory.  Block = 512 threads on RB consecutive rows x all naux Q; shared
+// image s[q * RB + row] = B^q_(r0 + row), thread t handles elements t + 512 k
+// (row t % RB).  Sums over the threads of a row: lanes by shuffles in a fixed
+// tree, then the 16 warps in order (deterministic).
+constexpr int kStatThreads = 512;
+
+template <int RB>
+__global__ void __launch_bounds__(kStatThreads) rowstat2_smem_kernel(
+    const double* __restrict__ b, int naux, long long R, int* __restrict__ erow,
+    double* __restrict__ diag, int* eref, int* kglob) {
+  constexpr int NW = kStatThreads / 32;
+  extern __shared__ __align__(16) double stage[];
+  __shared__ unsigned long long w_d[NW][RB];
+  __shared__ unsigned w_u[NW][RB];
+  __shared__ float w_f[NW][RB];
+  __shared__ int se[RB];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5, row = t & (RB - 1);
+  const long long r0 = (long long)blockIdx.x * RB;
+  const int n = naux * RB;
+  for (int k = t; k < n; k += kStatThreads) {
+    const int q = k / RB, rr = k & (RB - 1);
+    const bool valid = r0 + rr < R;
+    cp_async8(stage + k, valid ? b + (long long)q * R + r0 + rr : b, valid);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+
+  // pass 1
+  unsigned m = 0;
+  float sf = 0.f;
+  for (int k = t; k < n; k += kStatThreads) pass1_elem(stage[k], &m, &sf);
+#pragma unroll
+  for (int o = RB; o < 32; o <<= 1) {
+    const unsigned mo = __shfl_xor_sync(0xffffffffu, m, o);
+    m = mo > m ? mo : m;
+    sf += __shfl_xor_sync(0xffffffffu, sf, o);
+  }
+  if (lane < RB) {
+    w_u[warp][lane] = m;
+    w_f[warp][lane] = sf;
+  }
+  __syncthreads();
+  if (t < RB) {
+    const long long r = r0 + t;
+    m = 0;
+    float sfl = 0.f;
+    for (int w = 0; w < NW; ++w) {
+      m = w_u[w][t] > m ? w_u[w][t] : m;
+      sfl += w_f[w][t];
     }
+    int e = INT_MIN / 4;
+    if (r < R) {
+      e = row_scale2(m, sfl, naux);
+      if (e > INT_MIN / 8) atomicMax(eref, e);
+      erow[r] = e;
+      if (e <= INT_MIN / 8) diag[r] = 0.0;
+    }
+    se[t] = e;
+  }
+  __syncthreads();
+
+  // pass 2 at the row's scale
+  const int e = se[row];
+  const bool live = r0 + row < R && e > INT_MIN / 8;
+  RowStats2 st;
+  if (live)
+    for (int k = t; k < n; k += kStatThreads) pass2_elem(stage[k], e, st);
+#pragma unroll
+  for (int o = RB; o < 32; o <<= 1) {
+    st.c += __shfl_xor_sync(0xffffffffu, st.c, o);
+    st.d += __shfl_xor_sync(0xffffffffu, st.d, o);
+  }
+  if (lane < RB) {  // (the row threads' reads of w_f precede the barrier above)
+    w_f[warp][lane] = st.c;
+    w_d[warp][lane] = st.d;
+  }
+  __syncthreads();
+  if (t < RB && r0 + t < R && se[t] > INT_MIN / 8) {
+    RowStats2 tot;
+    for (int w = 0; w < NW; ++w) {
+      tot.c += w_f[w][t];
+      tot.d += w_d[w][t];
+    }
+    double dg;
+    const int k = row_level2(tot, se[t], naux, &dg);
+    diag[r0 + t] = dg;
     atomicMin(kglob, k);
   }
 }
@@ -340,10 +424,17 @@ __global__ void __launch_bounds__(32 * QG) rowstat_kernel(const double* __restri
   }
 }
 
+// Two small integers (exact in the format) as a packed FP16 (FMT 0) or BF16
+// (FMT 1) pair, low half = v0.
 template <int FMT>
-__device__ __forceinline__ uint16_t to16i(int v) {
-  if (FMT == 0) return __half_as_ushort(__int2half_rn(v));
-  return __bfloat16_as_ushort(__int2bfloat16_rn(v));
+__device__ __forceinline__ uint32_t pack16(int v0, int v1) {
+  const float f0 = small_int_to_float(v0), f1 = small_int_to_float(v1);
+  if (FMT == 0) {
+    const __half2 h = __floats2half2_rn(f0, f1);
+    return *reinterpret_cast<const uint32_t*>(&h);
+  }
+  const __nv_bfloat162 h = __floats2bfloat162_rn(f0, f1);
+  return *reinterpret_cast<const uint32_t*>(&h);
 }
 
 // B[Q][r] -> digit planes in the tiled layout of the energy kernels
@@ -353,87 +444,90 @@ __device__ __forceinline__ uint16_t to16i(int v) {
 // tile with one linear bulk copy.  Rows a >= nvir of the last tile and
 // Q >= naux are zero.
 //
-// Block = 256 threads on a 64 (padded row) x 64 (Q) tile: reads coalesced
-// along r, then each thread converts 16 consecutive Q of one row and stores
-// two 16-byte chunks per plane.  Digits by integer arithmetic on the IEEE
-// fields: scheme 0 (levels) X = round(B 2^(2(p+1) - e_r)), s0 = round(X/L^2),
-// s1 = round((X - s0 L^2)/L), s2 = remainder; scheme 1 (Karatsuba) as
-// kara_digits, planes s0, s0 + s1, s1.
+// Block = 256 threads on a 64 (padded row) x 64 (Q) tile: 8-byte asynchronous
+// copies coalesced along r (all 16 of a thread in flight at once), then each
+// thread converts 16 consecutive Q of its row to the fixed-point integer of
+// the row scale (round_scaled32) and to digits (a warp: 32 consecutive rows,
+// conflict-free shared reads) and stores one 32-byte sector per plane.  Scheme 0 (levels):
+// X = round(B 2^(2(p+1) - e_r)), s0 = round(X/L^2), s1 = round((X - s0 L^2)/L),
+// s2 = remainder; scheme 1: X20 = round(B 2^(20 - e_r)) and digits2, planes
+// s0, s1.
 template <int SCHEME, int FMT>
 __global__ void __launch_bounds__(256) slice_kernel(const double* __restrict__ b, int naux,
                                                     int nocc, int nvir, int Qp, int p,
                                                     const int* __restrict__ erow,
                                                     const int* __restrict__ kglob,
                                                     uint16_t* __restrict__ S) {
-  __shared__ double tile[64][65];
+  __shared__ __align__(16) double tile[64][65];
   const int t = threadIdx.x;
   const int ntiles = (nvir + 127) / 128, vp = ntiles * 128;
   const long long R = (long long)nocc * nvir, Rp = (long long)nocc * vp;
-  const long long r0 = (long long)blockIdx.x * 64;
-  const int q0 = blockIdx.y * 64;
-  {
-    const int c = t & 63;
-    const long long rp = r0 + c;
-    const int i = (int)(rp / vp), a = (int)(rp % vp);
-    const bool real = rp < Rp && a < nvir;
-    const long long r = (long long)i * nvir + a;
-#pragma unroll 4
-    for (int k = t >> 6; k < 64; k += 4) {
-      const int q = q0 + k;
-      tile[k][c] = (q < naux && real) ? b[(long long)q * R + r] : 0.0;
-    }
-  }
-  __syncthreads();
-  const int rl = t >> 2, qc = (t & 3) * 16;
+  // Blocks walk the rows from the last to the first, all Q of a row tile
+  // together: the row-statistics pass just streamed B in ascending row order,
+  // so the L2 still holds its last rows, and they are read first here.
+  const long long lin = (long long)blockIdx.y * gridDim.x + blockIdx.x;
+  const long long r0 = (long long)(gridDim.x - 1 - lin / gridDim.y) * 64;
+  const int q0 = (int)(lin % gridDim.y) * 64;
+  // thread's row (the same in both phases): padded row r0 + (t % 64)
+  const int rl = t & 63;
   const long long rp = r0 + rl;
-  if (rp >= Rp || q0 + qc >= Qp) return;
   const int i = (int)(rp / vp), a = (int)(rp % vp);
-  const int e = a < nvir ? erow[(long long)i * nvir + a] : INT_MIN / 4;
-  const bool live = e > INT_MIN / 8;
-  __align__(16) uint16_t h0[16];
-  __align__(16) uint16_t h1[16];
-  __align__(16) uint16_t h2[16];
-  if (SCHEME == kSchemeKara) {
-    const int k = live ? *kglob : 0;
+  const bool real = rp < Rp && a < nvir;
+  const long long r = (long long)i * nvir + a;
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      int s0 = 0, s1 = 0;
-      if (live) kara_digits(round_scaled64(tile[qc + j][rl], 24 - e), k, &s0, &s1);
-      h0[j] = to16i<FMT>(s0);
-      h1[j] = to16i<FMT>(s0 + s1);
-      h2[j] = to16i<FMT>(s1);
-    }
-  } else {
-    const int lb = p + 1;       // bits per level
-    const int k2 = 2 * lb - e;  // X = B 2^k2
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      const int X = live ? round_scaled(tile[qc + j][rl], k2) : 0;
-      const int s0 = (X + (1 << (2 * lb - 1))) >> (2 * lb);
-      const int rem = X - (s0 << (2 * lb));
-      const int s1 = (rem + (1 << (lb - 1))) >> lb;
-      const int s2 = rem - (s1 << lb);
-      h0[j] = to16i<FMT>(s0);
-      h1[j] = to16i<FMT>(s1);
-      h2[j] = to16i<FMT>(s2);
-    }
+  for (int k = t >> 6; k < 64; k += 4) {  // 16 asynchronous 8-byte copies, all in flight
+    const int q = q0 + k;
+    const bool valid = real && q < naux;
+    cp_async8(&tile[k][rl], valid ? b + (long long)q * R + r : b, valid);
   }
+  cp_async_wait_all();
+  __syncthreads();
+  const int qc = (t >> 6) * 16;
+  if (rp >= Rp || q0 + qc >= Qp) return;
+  const int e = real ? erow[r] : INT_MIN / 4;
+  const bool live = e > INT_MIN / 8;
+  const int cs = (SCHEME == kSchemeDigits2 ? 20 : 2 * (p + 1)) - e;
   const int q = q0 + qc;
-  const int nkb = Qp / 32, kb = q / 32, c0 = (q % 32) / 8;
-  const size_t plane = 4096;  // the three planes of a tile are adjacent
-  const size_t base = slice_tile_offset(0, i, kb, a / 128, nocc, nkb, ntiles);
+  constexpr int NPL = planes_for_scheme(SCHEME);
+  const int nkb = Qp / kSliceQ, kb = q / kSliceQ, c0 = (q % kSliceQ) / 8;
+  const size_t plane = kSliceTileElems;  // the planes of a tile are adjacent
+  const size_t base = slice_tile_offset(0, i, kb, a / 128, nkb, ntiles, NPL);
   const int row = a % 128;
-  const size_t at0 = base + slice_chunk_offset(row, c0);
-  const size_t at1 = base + slice_chunk_offset(row, c0 + 1);
-  const uint4* v0 = reinterpret_cast<const uint4*>(h0);
-  const uint4* v1 = reinterpret_cast<const uint4*>(h1);
-  const uint4* v2 = reinterpret_cast<const uint4*>(h2);
-  *reinterpret_cast<uint4*>(S + at0) = v0[0];
-  *reinterpret_cast<uint4*>(S + at1) = v0[1];
-  *reinterpret_cast<uint4*>(S + plane + at0) = v1[0];
-  *reinterpret_cast<uint4*>(S + plane + at1) = v1[1];
-  *reinterpret_cast<uint4*>(S + 2 * plane + at0) = v2[0];
-  *reinterpret_cast<uint4*>(S + 2 * plane + at1) = v2[1];
+  int k = 0;
+  if (SCHEME == kSchemeDigits2) {
+    k = *kglob;  // no live row at all: every X is 0, any level works
+    k = k < 0 ? 0 : (k > kMaxLevelExp ? kMaxLevelExp : k);
+  }
+  const int lb = p + 1;  // scheme 0: bits per level
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {  // two 16-byte chunks (8 Q each) per plane
+    uint32_t w0[4], w1[4], w2[4];
+#pragma unroll
+    for (int j = 0; j < 8; j += 2) {
+      int d0[2], d1[2], d2[2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int X = live ? round_scaled32(tile[qc + 8 * h + j + u][rl], cs) : 0;
+        if (SCHEME == kSchemeDigits2) {
+          digits2(X, k, &d0[u], &d1[u]);
+          d2[u] = 0;
+        } else {
+          d0[u] = (X + (1 << (2 * lb - 1))) >> (2 * lb);
+          const int rem = X - (d0[u] << (2 * lb));
+          d1[u] = (rem + (1 << (lb - 1))) >> lb;
+          d2[u] = rem - (d1[u] << lb);
+        }
+      }
+      w0[j / 2] = pack16<FMT>(d0[0], d0[1]);
+      w1[j / 2] = pack16<FMT>(d1[0], d1[1]);
+      w2[j / 2] = pack16<FMT>(d2[0], d2[1]);
+    }
+    const size_t at = base + slice_chunk_offset(row, c0 + h);
+    *reinterpret_cast<uint4*>(S + at) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
+    *reinterpret_cast<uint4*>(S + plane + at) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+    if (NPL == 3)
+      *reinterpret_cast<uint4*>(S + 2 * plane + at) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+  }
 }
 
 // Per-row FP32 factors for the energy kernel: sc_r = 2^(e_r - e_ref) and the
@@ -503,6 +597,26 @@ int slice_bits_for(int Qp) {
   return p;
 }
 
+// Dynamic shared memory of the staged row-statistics kernel: at most this
+// many bytes per block (naux <= 3200 for 4 rows per block).
+constexpr size_t kStatSmemMax = 100 * 1024;
+
+// Raise the kernel's dynamic shared memory limit once per device (safe under
+// stream capture: not a stream operation).
+template <int RB>
+cudaError_t set_stat_smem() {
+  static std::atomic<unsigned long long> done{0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (done.load() & bit) return cudaSuccess;
+  e = cudaFuncSetAttribute(rowstat2_smem_kernel<RB>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStatSmemMax);
+  if (e == cudaSuccess) done.fetch_or(bit);
+  return e;
+}
+
 cudaError_t launch_slices(const double* b, int naux, int nocc, int nvir, int Qp, int scheme,
                           int fmt, int p, SliceWork w, cudaStream_t s) {
   const long long R = (long long)nocc * nvir;
@@ -512,11 +626,20 @@ cudaError_t launch_slices(const double* b, int naux, int nocc, int nvir, int Qp,
   if (e != cudaSuccess) return e;
   const long long Rp = (long long)nocc * ((nvir + 127) / 128) * 128;
   dim3 grid((unsigned)((Rp + 63) / 64), (unsigned)((Qp + 63) / 64));
-  if (scheme == kSchemeKara) {
-    rowstat_kara_kernel<<<(unsigned)((R + 31) / 32), dim3(32, QG), 0, s>>>(b, naux, R, w.erow,
-                                                                          w.diag, w.eref,
-                                                                          w.eref + 1);
-    slice_kernel<kSchemeKara, 0><<<grid, 256, 0, s>>>(b, naux, nocc, nvir, Qp, p, w.erow,
+  if (scheme == kSchemeDigits2) {
+    // rows staged in shared memory, 4 rows per block (four blocks per SM up to
+    // naux ~ 1700), else the two-pass global form
+    const size_t img = (size_t)naux * 4 * 8;
+    if (img <= kStatSmemMax) {
+      e = set_stat_smem<4>();
+      if (e != cudaSuccess) return e;
+      rowstat2_smem_kernel<4><<<(unsigned)((R + 3) / 4), kStatThreads, img, s>>>(
+          b, naux, R, w.erow, w.diag, w.eref, w.eref + 1);
+    } else {
+      rowstat2_kernel<<<(unsigned)((R + 31) / 32), dim3(32, QG), 0, s>>>(
+          b, naux, R, w.erow, w.diag, w.eref, w.eref + 1);
+    }
+    slice_kernel<kSchemeDigits2, 0><<<grid, 256, 0, s>>>(b, naux, nocc, nvir, Qp, p, w.erow,
                                                       w.eref + 1, w.S);
   } else {
     rowstat_kernel<<<(unsigned)((R + 31) / 32), dim3(32, QG), 0, s>>>(b, naux, R, p, w.erow,
@@ -529,7 +652,7 @@ cudaError_t launch_slices(const double* b, int naux, int nocc, int nvir, int Qp,
                                                            w.eref + 1, w.S);
   }
   rowfactor_kernel<<<(unsigned)((R + 255) / 256 < 1024 ? (R + 255) / 256 : 1024), 256, 0, s>>>(
-      w.erow, w.diag, R, w.eref, scheme == kSchemeKara ? -1 : p + 1, w.sc, w.dg, w.scale);
+      w.erow, w.diag, R, w.eref, scheme == kSchemeDigits2 ? -1 : p + 1, w.sc, w.dg, w.scale);
   return cudaGetLastError();
 }
 

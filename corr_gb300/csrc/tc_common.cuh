@@ -43,10 +43,9 @@ __device__ __forceinline__ void tc_wait_st() {
 }
 
 // 32 columns [c, c+32) of one phase's result in scaled FP32 units, from the
-// three exact integer accumulators at columns tb, tb+128, tb+256.
-//   scheme 0 (levels):    d = acc0 + acc1/L + acc2/L^2
-//   scheme 1 (Karatsuba): d = P0 + (Pm - P0 - P2)/L + P2/L^2
-// Every step rounds to nearest (CUDA cores), so no bias enters here.
+// three exact integer accumulators at columns tb, tb+128, tb+256 (levels 0, 1,
+// 2 of either scheme): d = acc0 + acc1/L + acc2/L^2.  Every step rounds to
+// nearest (CUDA cores), so no bias enters here.
 template <int SCHEME>
 __device__ __forceinline__ void load_level_sum(uint32_t tb, int c, float inv_l, float inv_l2,
                                                float sca, const float* scb, float* d) {
@@ -57,8 +56,7 @@ __device__ __forceinline__ void load_level_sum(uint32_t tb, int c, float inv_l, 
   tc_wait_ld();
 #pragma unroll
   for (int k = 0; k < 32; ++k) {
-    const float l1 = SCHEME == 1 ? (a1[k] - a0[k]) - a2[k] : a1[k];
-    const float t = fmaf(a2[k], inv_l2, fmaf(l1, inv_l, a0[k]));
+    const float t = fmaf(a2[k], inv_l2, fmaf(a1[k], inv_l, a0[k]));
     d[k] = t * (sca * scb[c + k]);
   }
 }
@@ -74,31 +72,32 @@ __device__ __forceinline__ void load_level_sum16(uint32_t tb, int c, float inv_l
   tc_wait_ld();
 #pragma unroll
   for (int k = 0; k < 16; ++k) {
-    const float l1 = SCHEME == 1 ? (a1[k] - a0[k]) - a2[k] : a1[k];
-    const float t = fmaf(a2[k], inv_l2, fmaf(l1, inv_l, a0[k]));
+    const float t = fmaf(a2[k], inv_l2, fmaf(a1[k], inv_l, a0[k]));
     d[k] = t * (sca * scb[c + k]);
   }
 }
 
 // The MMAs of one K=16 step: r[l], q[l] are the row/column descriptors of
-// digit plane l; c0..c2 the three accumulators.
+// digit plane l; c0..c2 the three accumulators.  MMAs sharing a row operand
+// run back to back and keep it in the tensor core's A collector buffer (one
+// shared-memory read of each row plane per K step).
 template <int SCHEME>
 __device__ __forceinline__ void issue_digit_mmas(uint32_t c0, uint32_t c1, uint32_t c2,
                                                  const uint64_t* r, const uint64_t* q,
                                                  uint32_t idesc, uint32_t acc) {
   if (SCHEME == 1) {
-    tc_mma_f16(c0, r[0], q[0], idesc, acc);  // s0.s0'
-    tc_mma_f16(c1, r[1], q[1], idesc, acc);  // u.u'
-    tc_mma_f16(c2, r[2], q[2], idesc, acc);  // s1.s1'
+    tc_mma_f16_ca<0>(c0, r[0], q[0], idesc, acc);  // s0.s0'
+    tc_mma_f16_ca<2>(c1, r[0], q[1], idesc, acc);  // s0.s1'
+    tc_mma_f16_ca<0>(c1, r[1], q[0], idesc, 1u);   // + s1.s0'
+    tc_mma_f16_ca<2>(c2, r[1], q[1], idesc, acc);  // s1.s1'
   } else {
-    tc_mma_f16(c0, r[0], q[0], idesc, acc);
-    tc_mma_f16(c1, r[0], q[1], idesc, acc);
-    tc_mma_f16(c1, r[1], q[0], idesc, 1u);
-    tc_mma_f16(c2, r[0], q[2], idesc, acc);
-    tc_mma_f16(c2, r[1], q[1], idesc, 1u);
+    tc_mma_f16_ca<0>(c0, r[0], q[0], idesc, acc);
+    tc_mma_f16_ca<1>(c1, r[0], q[1], idesc, acc);
+    tc_mma_f16_ca<2>(c2, r[0], q[2], idesc, acc);
+    tc_mma_f16_ca<0>(c1, r[1], q[0], idesc, 1u);
+    tc_mma_f16_ca<2>(c2, r[1], q[1], idesc, 1u);
     tc_mma_f16(c2, r[2], q[0], idesc, 1u);
   }
 }
-
 
 }  // namespace corr

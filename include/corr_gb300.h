@@ -47,10 +47,11 @@ enum corr_precision {
   CORR_PREC_FP64 = 0,       /* FP64 end to end (FP64 mma.sync)                   */
   CORR_PREC_SPLIT_FP16 = 1, /* each row (i,a) of B scaled by a power of two and
                                split into two integer digits s0 + s1/L stored as
-                               FP16 (|digit| <= 2048); three Karatsuba products
-                               s0.s0', (s0+s1).(s0'+s1'), s1.s1' on tcgen05 with
-                               exact FP32 integer accumulation in TMEM; (ia|ia)
-                               in FP64; FP64 pair-energy sums.  The fast form.  */
+                               FP16 (|digit| <= 2048); the products s0.s0',
+                               s0.s1' + s1.s0', s1.s1' on tcgen05 with exact
+                               FP32 integer accumulation in TMEM; (ia|ia) to
+                               FP64 accuracy; FP64 pair-energy sums.  The fast
+                               form.                                             */
   CORR_PREC_SPLIT_BF16 = 2  /* three 7-bit integer digits per element stored as
                                BF16; the six digit products of orders 0-2 on
                                tcgen05, exact accumulation, (ia|ia) in FP64     */
@@ -169,7 +170,8 @@ int corr_selftest_wait_timeout(corr_context* ctx, int limit_ms);
 int corr_set_energy_policy(corr_context* ctx, int cluster);
 
 /* Launch variant of the batched kernel: unit order (0 = input order,
- * 1 = costliest instance first) and shared-memory pipeline depth (3 or 4). */
+ * 1 = costliest instance first) and shared-memory pipeline depth in stages of
+ * one 64-wide Q block (2 or 3; the three-digit form always runs 2). */
 int corr_set_batch_policy(corr_context* ctx, int order, int stages);
 
 /* Time every launch variant on this batch (median of three runs after a

@@ -45,7 +45,7 @@ def test_batched_policies_agree_and_autotune(ctx, tmp_path):
     for prec in ("split_fp16", "split_bf16"):
         base = None
         for order in (0, 1):
-            for stages in (3, 4):
+            for stages in (2, 3):
                 ctx.set_batch_policy(order, stages)
                 got = [g.e_total for g in ctx.rimp2_energy_batched(items, prec)]
                 if base is None:

@@ -53,6 +53,19 @@ def test_split_matches_oracle(ctx, o, v, X, seed, prec, rel):
     assert abs(got.e_ss - ref[0]) <= rel * abs(ref[2]), (prec, got, ref)
 
 
+@pytest.mark.parametrize("o,v,X,seed", [
+    (5, 7, 1600, 21),   # row statistics staged in shared memory, 4 rows per block
+    (3, 41, 3200, 22),  # staged, at its size limit
+    (2, 30, 3300, 23),  # beyond the staged form: two-pass global form
+])
+def test_split_fp16_row_statistics_forms(ctx, o, v, X, seed):
+    B, eps = O.synth_rimp2(o, v, X, seed)
+    ref = O.rimp2_energy(B, eps, o, v)
+    got = ctx.rimp2_energy(B, eps, o, v, X, "split_fp16")
+    assert abs(got.e_total - ref[2]) <= 1e-6 * abs(ref[2]), (got, ref)
+    assert abs(got.e_ss - ref[0]) <= 1e-6 * abs(ref[2]), (got, ref)
+
+
 def test_config2_full_size(ctx):
     """nocc=40, nvir=360, naux=1200 (decaying aux spectrum)."""
     o, v, X = 40, 360, 1200
