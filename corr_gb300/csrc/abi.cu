@@ -301,7 +301,7 @@ namespace corr {
 
 // Scratch of the energy stage for device-resident B and eps.
 static void energy_carve(Carver& w, int nocc, int nvir, int Qp, bool tc, int grid, SliceWork* sw,
-                         double** partials) {
+                         double** partials, unsigned long long** queue = nullptr) {
   const long long R = (long long)nocc * nvir;
   if (tc) {
     sw->S = static_cast<uint16_t*>(w.take(slice_bytes(nocc, nvir, Qp)));
@@ -313,6 +313,8 @@ static void energy_carve(Carver& w, int nocc, int nvir, int Qp, bool tc, int gri
     sw->scale = static_cast<double*>(w.take(16));
   }
   *partials = static_cast<double*>(w.take((size_t)grid * 16));
+  unsigned long long* qp = static_cast<unsigned long long*>(w.take(16));  // work-queue counter
+  if (queue) *queue = qp;
 }
 
 static int energy_grid(corr_context* c, const EnergyShape& sh, bool tc) {
@@ -344,7 +346,8 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
   const int grid = energy_grid(c, sh, tc);
   SliceWork sw{};
   double* partials;
-  energy_carve(w, nocc, nvir, Qp, tc, 2 * c->sms, &sw, &partials);
+  unsigned long long* queue;
+  energy_carve(w, nocc, nvir, Qp, tc, 2 * c->sms, &sw, &partials, &queue);
   if (!tc) {
     mark(c, 1);
     CORR_CUDA(launch_energy_fp64(d_b, d_e, sh, partials, grid, c->stream));
@@ -369,7 +372,7 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
       cluster ? kTcCluster * (int)std::min<long long>(c->tc_clusters, cwork) : grid;
   mark(c, 1);
   CORR_CUDA(launch_energy_tc(sw.S, d_e, sw.sc, sw.dg, sw.scale, sh, Qp, fmt, scheme, cluster,
-                             partials, lgrid, &c->dres->status, c->stream));
+                             partials, lgrid, &c->dres->status, queue, c->stream));
   mark(c, 2);
   CORR_CUDA(launch_energy_reduce(partials, lgrid, sw.scale, out_e, c->stream));
   c->launches += 5;  // rowstat, slice, rowfactor, energy, reduce

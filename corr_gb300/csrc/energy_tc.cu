@@ -75,9 +75,15 @@ constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t COL_STASH = 384;           // parked D1
 constexpr uint32_t SW128 = 2;                 // descriptor layout type: 128B swizzle
 
+constexpr int RING = 4;                       // unit numbers in flight (one-CTA form)
+
 struct Ctl {
   uint64_t full[MAX_STAGES];
   uint64_t empty[MAX_STAGES];
+  uint64_t ufull[RING];   // unit ring: producer -> MMA thread and epilogue
+  uint64_t uempty[RING];
+  long long uring[RING];
+  int wu[2][4];           // per-warp outcome of the epilogue's unit wait
   uint64_t afull;
   uint64_t aempty;
   uint64_t fin;
@@ -133,7 +139,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     energy_tc_kernel(const uint16_t* __restrict__ S, const double* __restrict__ eps,
                      const float* __restrict__ sc, const float* __restrict__ dg,
                      const double* __restrict__ scale, EnergyShape sh, int nkb, uint32_t idesc,
-                     double* __restrict__ partials, int* status) {
+                     double* __restrict__ partials, int* status,
+                     unsigned long long* __restrict__ queue) {
   using G = Geo<SCHEME>;
   constexpr int STAGES = G::STAGES, STAGE_BYTES = G::STAGE_BYTES, NPL = G::NPL;
   extern __shared__ uint8_t smem_raw[];
@@ -155,6 +162,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(&ctl->full[s], 1);
       mbar_init(&ctl->empty[s], CL ? 3 : 1);
+    }
+    for (int s = 0; s < RING; ++s) {
+      mbar_init(&ctl->ufull[s], 1);
+      mbar_init(&ctl->uempty[s], 2);
     }
     mbar_init(&ctl->afull, 1);
     mbar_init(&ctl->aempty, 4);
@@ -184,14 +195,32 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       for (int s = 0; s < STAGES; ++s) has[s] = false;
       bool ok = true;
       // Shared-memory slots of a stage: [row operand planes][column operand
-      // planes] per 32-wide Q block.  One-CTA form: lane 2 kbo + colop copies
-      // the NPL adjacent planes of its operand.  Cluster form: lane
-      // 2 NPL kbo + 2 l + colop copies its 64-row half of one plane tile.
-      const int kbo = CL ? lane / (2 * NPL) : lane >> 1;
-      const int l = CL ? (lane % (2 * NPL)) >> 1 : 0;
+      // planes] per Q block.  Lane 2 NPL kbo + 2 l + colop copies plane l of
+      // its operand (one-CTA form: the whole 16 KB tile; cluster form: its
+      // 64-row half).
+      const int kbo = lane / (2 * NPL);
+      const int l = (lane % (2 * NPL)) >> 1;
       const bool colop = (lane & 1) != 0;
-      const int ncopy = CL ? G::NTILES : 2 * KBS;
-      for (long long k = first; k < nwork && ok; k += stride) {
+      const int ncopy = G::NTILES;
+      for (long long t = 0; ok; ++t) {
+        // next unit: the static sequence (cluster form) or the device queue
+        long long k = first + t * stride;
+        if (!CL) {
+          const int slot = (int)(t % RING);
+          const uint32_t use = (uint32_t)(t / RING);
+          long long u = -2;  // -2: wait failed, -1: queue drained
+          if (lane == 0 && mbar_wait(&ctl->uempty[slot], (use & 1) ^ 1, abort, status)) {
+            u = (long long)atomicAdd(queue, 1ull);
+            if (u >= nwork) u = -1;
+            ctl->uring[slot] = u;
+            mbar_arrive(&ctl->ufull[slot]);
+          }
+          k = __shfl_sync(0xffffffffu, u, 0);
+          if (k == -2) ok = false;
+          if (k < 0) break;
+        } else if (k >= nwork) {
+          break;
+        }
         const Unit w = unit_at<CL>(k, sh, cr, cc);
         for (int phs = 0; phs < w.nph && ok; ++phs) {
           const int x = phs == 0 ? w.i : w.j;  // row operand slab
@@ -224,7 +253,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 bulk_load_mc(sb + half * HALF_BYTES, src + half * (HALF_BYTES / 2), HALF_BYTES,
                              bar, mask);
               else
-                bulk_load(sb, src, NPL * TILE_BYTES, bar);
+                bulk_load(sb, src, TILE_BYTES, bar);
             }
             has[st] = true;
             last_ph[st] = ph;
@@ -259,7 +288,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       // shared-memory descriptor of tile 0 of stage 0 (every tile address is
       // below 2^18, so offsets added to the 14-bit start field never carry out)
       const uint64_t dbase = smem_desc(smem_u32(tiles), 16, 1024, SW128);
-      for (long long k = first; k < nwork && ok; k += stride) {
+      for (long long t = 0; ok; ++t) {
+        long long k = first + t * stride;
+        if (!CL) {
+          const int slot = (int)(t % RING);
+          const uint32_t use = (uint32_t)(t / RING);
+          if (!mbar_wait(&ctl->ufull[slot], use & 1, abort, status)) break;
+          k = ctl->uring[slot];
+          mbar_arrive(&ctl->uempty[slot]);
+          if (k < 0) break;
+        } else if (k >= nwork) {
+          break;
+        }
         const Unit w = unit_at<CL>(k, sh, cr, cc);
         for (int phs = 0; phs < w.nph && ok; ++phs) {
           if (!mbar_wait(&ctl->aempty, (nuse & 1) ^ 1, abort, status)) {
@@ -319,7 +359,28 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     double tot_os = 0.0, tot_ss = 0.0;
     bool dead = false;
     uint32_t nuse = 0;
-    for (long long k = first; k < nwork; k += stride) {
+    for (long long t = 0;; ++t) {
+      long long k = first + t * stride;
+      if (!CL) {
+        // unit number: every epilogue thread waits and reads, then one
+        // thread releases the slot (after the barrier that ends the reads)
+        if (dead) break;
+        const int slot = (int)(t % RING);
+        const uint32_t use = (uint32_t)(t / RING);
+        const bool gotu =
+            __all_sync(0xffffffffu, mbar_wait(&ctl->ufull[slot], use & 1, abort, status));
+        if (lane == 0) ctl->wu[t & 1][q] = gotu ? 1 : 0;
+        k = gotu ? ctl->uring[slot] : -1;
+        named_bar(1, 128);
+        const bool all = ctl->wu[t & 1][0] & ctl->wu[t & 1][1] & ctl->wu[t & 1][2] &
+                         ctl->wu[t & 1][3];
+        named_bar(1, 128);
+        if (et == 0 && all) mbar_arrive(&ctl->uempty[slot]);
+        if (!all) dead = true;
+        if (!all || k < 0) break;  // uniform: every thread read the same slot
+      } else if (k >= nwork) {
+        break;
+      }
       const Unit w = unit_at<CL>(k, sh, cr, cc);
       const int i = w.i, j = w.j, A = w.A, B = w.B;
       const bool two = w.nph == 2;
@@ -500,7 +561,7 @@ template <int SCHEME, bool CL>
 static cudaError_t launch_variant(int grid, cudaStream_t s, const uint16_t* S, const double* eps,
                                   const float* sc, const float* dg, const double* scale,
                                   const EnergyShape& sh, int nkb, uint32_t idesc,
-                                  double* partials, int* status) {
+                                  double* partials, int* status, unsigned long long* queue) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3(NTHREADS);
@@ -514,7 +575,7 @@ static cudaError_t launch_variant(int grid, cudaStream_t s, const uint16_t* S, c
   cfg.attrs = attr;
   cfg.numAttrs = CL ? 1 : 0;
   return cudaLaunchKernelEx(&cfg, energy_tc_kernel<SCHEME, CL>, S, eps, sc, dg, scale, sh, nkb,
-                            idesc, partials, status);
+                            idesc, partials, status, queue);
 }
 
 cudaError_t prepare_energy_tc(int* max_clusters) {
@@ -553,18 +614,22 @@ long long energy_tc_cluster_work(const EnergyShape& sh) {
 cudaError_t launch_energy_tc(const uint16_t* S, const double* eps, const float* sc,
                              const float* dg, const double* scale, const EnergyShape& sh, int Qp,
                              int fmt, int scheme, bool cluster, double* partials, int grid,
-                             int* status, cudaStream_t s) {
+                             int* status, unsigned long long* queue, cudaStream_t s) {
   const uint32_t idesc = idesc_f16((uint32_t)fmt, TILE, TILE);
   const int nkb = Qp / KB;
+  if (!cluster) {
+    cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+  }
   if (scheme == kSchemeDigits2)
     return cluster ? launch_variant<kSchemeDigits2, true>(grid, s, S, eps, sc, dg, scale, sh, nkb,
-                                                       idesc, partials, status)
-                   : launch_variant<kSchemeDigits2, false>(grid, s, S, eps, sc, dg, scale, sh, nkb,
-                                                        idesc, partials, status);
+                                                          idesc, partials, status, queue)
+                   : launch_variant<kSchemeDigits2, false>(grid, s, S, eps, sc, dg, scale, sh,
+                                                           nkb, idesc, partials, status, queue);
   return cluster ? launch_variant<kSchemeDigits3, true>(grid, s, S, eps, sc, dg, scale, sh, nkb,
-                                                        idesc, partials, status)
+                                                        idesc, partials, status, queue)
                  : launch_variant<kSchemeDigits3, false>(grid, s, S, eps, sc, dg, scale, sh, nkb,
-                                                         idesc, partials, status);
+                                                         idesc, partials, status, queue);
 }
 
 }  // namespace corr

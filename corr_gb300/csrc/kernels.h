@@ -77,13 +77,14 @@ cudaError_t launch_energy_reduce(const double* partials, int n, const double* sc
 // tcgen05 precision form (energy_tc.cu) over the tiled digit planes S.
 // scale: the SliceWork scale pair (the kernel reads 1/L from scale[1]).
 // cluster: the 2 x 2 multicast form (grid = a multiple of kTcCluster, at most
-// kTcCluster x the max_clusters of prepare_energy_tc); else one CTA per unit
-// stream.  partials: grid pairs {os, ss}.
+// kTcCluster x the max_clusters of prepare_energy_tc); else one CTA per SM
+// taking units from the device counter `queue` (8 bytes, zeroed here on the
+// stream before the launch).  partials: grid pairs {os, ss}.
 constexpr int kTcCluster = 4;
 cudaError_t launch_energy_tc(const uint16_t* S, const double* eps, const float* sc,
                              const float* dg, const double* scale, const EnergyShape& sh, int Qp,
                              int fmt, int scheme, bool cluster, double* partials, int grid,
-                             int* status, cudaStream_t s);
+                             int* status, unsigned long long* queue, cudaStream_t s);
 // One-time attributes (dynamic smem size) and the number of 4-CTA clusters
 // that fit at once (0: no cluster form).
 cudaError_t prepare_energy_tc(int* max_clusters);

@@ -121,9 +121,11 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
   if ((long long)grid > sh.nunits) grid = (int)sh.nunits;
 
   // carve the static scratch (same order for the size check and the real pass)
-  auto carve = [&](Carver& w, Header** hdr, double** partials, SliceWork* sw) {
+  auto carve = [&](Carver& w, Header** hdr, double** partials, unsigned long long** queue,
+                   SliceWork* sw) {
     *hdr = static_cast<Header*>(w.take(256));
     *partials = static_cast<double*>(w.take((size_t)kMaxGrid * 16));
+    *queue = static_cast<unsigned long long*>(w.take(16));
     if (tc) {
       sw->erow = static_cast<int*>(w.take((size_t)R * 4));
       sw->diag = static_cast<double*>(w.take((size_t)R * 8));
@@ -136,9 +138,10 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
   };
   Header* hdr;
   double* partials;
+  unsigned long long* queue;
   SliceWork sw{};
   Carver size_pass{nullptr, 0};
-  carve(size_pass, &hdr, &partials, &sw);
+  carve(size_pass, &hdr, &partials, &queue, &sw);
   if (size_pass.used > kScratchBytes) {
     set_error(
         "corr_rimp2_energy_noalloc: nocc=%d nvir=%d naux=%d needs %zu bytes of scratch; the "
@@ -148,7 +151,7 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
     return CORR_ERR_BAD_ARG;
   }
   Carver w{ds.ptr, 0};
-  carve(w, &hdr, &partials, &sw);
+  carve(w, &hdr, &partials, &queue, &sw);
 
   CORR_CUDA(cudaMemsetAsync(hdr, 0, sizeof(Header), s));  // status and results start at zero
   if (!tc) {
@@ -160,7 +163,7 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
     const int p = slice_bits_for(Qp);
     CORR_CUDA(launch_slices(bia, naux, nocc, nvir, Qp, scheme, fmt, p, sw, s));
     CORR_CUDA(launch_energy_tc(sw.S, eps, sw.sc, sw.dg, sw.scale, sh, Qp, fmt, scheme, false,
-                               partials, grid, &hdr->status, s));
+                               partials, grid, &hdr->status, queue, s));
     CORR_CUDA(launch_energy_reduce(partials, grid, sw.scale, hdr->e, s));
   }
   Header h;
