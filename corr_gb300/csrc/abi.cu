@@ -330,7 +330,8 @@ size_t energy_scratch_bytes(corr_context* c, int nocc, int nvir, int naux, int p
   SliceWork sw{};
   double* part;
   Carver cv{nullptr, 0};
-  energy_carve(cv, nocc, nvir, Qp, tc, 2 * c->sms, &sw, &part);  // partials of any grid
+  energy_carve(cv, nocc, nvir, Qp, tc, (int)std::max<long long>(2 * c->sms, sh.nunits), &sw,
+               &part);  // partials of any grid or one per unit
   return cv.used + 256;
 }
 
@@ -347,7 +348,8 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
   SliceWork sw{};
   double* partials;
   unsigned long long* queue;
-  energy_carve(w, nocc, nvir, Qp, tc, 2 * c->sms, &sw, &partials, &queue);
+  energy_carve(w, nocc, nvir, Qp, tc, (int)std::max<long long>(2 * c->sms, sh.nunits), &sw,
+               &partials, &queue);
   if (!tc) {
     mark(c, 1);
     CORR_CUDA(launch_energy_fp64(d_b, d_e, sh, partials, grid, c->stream));
@@ -374,7 +376,8 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
   CORR_CUDA(launch_energy_tc(sw.S, d_e, sw.sc, sw.dg, sw.scale, sh, Qp, fmt, scheme, cluster,
                              partials, lgrid, &c->dres->status, queue, c->stream));
   mark(c, 2);
-  CORR_CUDA(launch_energy_reduce(partials, lgrid, sw.scale, out_e, c->stream));
+  CORR_CUDA(launch_energy_reduce(partials, cluster ? lgrid : (int)sh.nunits, sw.scale, out_e,
+                                 c->stream));
   c->launches += 5;  // rowstat, slice, rowfactor, energy, reduce
   return CORR_OK;
 }

@@ -29,7 +29,7 @@ constexpr int KB = kSliceQ;
 constexpr int TILE_BYTES = TILE * KB * 2;
 // a stage = the NPL digit planes of the row and of the column operand
 template <int SCHEME>
-constexpr int stage_bytes() {
+__host__ __device__ constexpr int stage_bytes() {
   return 2 * planes_for_scheme(SCHEME) * TILE_BYTES;
 }
 constexpr int NTHREADS = 192;

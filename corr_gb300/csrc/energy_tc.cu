@@ -308,8 +308,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           }
           tc_fence_after();
           const uint32_t c0 = tmem, c1 = tmem + 128u, c2 = tmem + 256u;
+          bool ready = false;  // the next stage's barrier, probed ahead of time
           for (int ks = 0; ks < nkb; ks += KBS) {
-            if (!mbar_wait(&ctl->full[st], ph, abort, status)) {
+            if (!ready && !mbar_wait(&ctl->full[st], ph, abort, status)) {
               ok = false;
               break;
             }
@@ -318,6 +319,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             // descriptor of this stage: the base descriptor plus the stage's
             // address offset in the 16-byte units of the start-address field
             const uint64_t ds = dbase + (uint64_t)(((uint32_t)st * STAGE_BYTES) >> 4);
+            const int nst = st + 1 == STAGES ? 0 : st + 1;
+            const uint32_t nph = st + 1 == STAGES ? ph ^ 1 : ph;
+            ready = false;
 #pragma unroll
             for (int j = 0; j < KBS * (KB / 16); ++j) {
               const int kbo = j / (KB / 16), kk = j % (KB / 16);
@@ -327,6 +331,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 r[l] = ds + (uint64_t)(((2 * NPL * kbo + l) * TILE_BYTES + kk * 32) >> 4);
                 q[l] = ds + (uint64_t)(((2 * NPL * kbo + NPL + l) * TILE_BYTES + kk * 32) >> 4);
               }
+              // while the MMAs queued so far run, probe the next stage
+              // (non-blocking), so the stage boundary costs no barrier latency
+              if (j == KBS * (KB / 16) - 1 && ks + KBS < nkb)
+                ready = mbar_test_wait(&ctl->full[nst], nph);
               const uint32_t acc = (ks | j) ? 1u : 0u;
               issue_digit_mmas<SCHEME>(c0, c1, c2, r, q, idesc, acc);
             }
@@ -521,22 +529,41 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         ++nuse;
       }
       const double fw = w.valid ? (A < B ? 2.0 : 1.0) * (same ? 0.5 : 1.0) : 0.0;
-      tot_os -= fw * uos;
-      tot_ss -= fw * uss;
-      named_bar(1, 128);  // smem db/scb are rewritten by the next unit
+      if (CL) {
+        tot_os -= fw * uos;
+        tot_ss -= fw * uss;
+      } else {
+        // queue form: which CTA takes a unit varies from run to run, so each
+        // unit writes its own partial (reduced over the 128 epilogue threads
+        // in a fixed order) and the host-side reduction sums them in unit order
+        const double pos = warp_sum(-fw * uos), pss = warp_sum(-fw * uss);
+        if (lane == 0) {
+          ctl->red[0][q] = pos;
+          ctl->red[1][q] = pss;
+        }
+        named_bar(1, 128);
+        if (et == 0) {
+          partials[2 * k] = (ctl->red[0][0] + ctl->red[0][1]) + (ctl->red[0][2] + ctl->red[0][3]);
+          partials[2 * k + 1] =
+              (ctl->red[1][0] + ctl->red[1][1]) + (ctl->red[1][2] + ctl->red[1][3]);
+        }
+      }
+      named_bar(1, 128);  // smem db/scb/red are rewritten by the next unit
     }
-    tot_os = warp_sum(tot_os);
-    tot_ss = warp_sum(tot_ss);
-    if (lane == 0) {
-      ctl->red[0][warp - 2] = tot_os;
-      ctl->red[1][warp - 2] = tot_ss;
-    }
-    named_bar(1, 128);
-    if (et == 0) {
-      partials[2 * blockIdx.x] =
-          (ctl->red[0][0] + ctl->red[0][1]) + (ctl->red[0][2] + ctl->red[0][3]);
-      partials[2 * blockIdx.x + 1] =
-          (ctl->red[1][0] + ctl->red[1][1]) + (ctl->red[1][2] + ctl->red[1][3]);
+    if (CL) {  // static assignment: one partial per CTA
+      tot_os = warp_sum(tot_os);
+      tot_ss = warp_sum(tot_ss);
+      if (lane == 0) {
+        ctl->red[0][warp - 2] = tot_os;
+        ctl->red[1][warp - 2] = tot_ss;
+      }
+      named_bar(1, 128);
+      if (et == 0) {
+        partials[2 * blockIdx.x] =
+            (ctl->red[0][0] + ctl->red[0][1]) + (ctl->red[0][2] + ctl->red[0][3]);
+        partials[2 * blockIdx.x + 1] =
+            (ctl->red[1][0] + ctl->red[1][1]) + (ctl->red[1][2] + ctl->red[1][3]);
+      }
     }
   }
 

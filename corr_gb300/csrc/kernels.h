@@ -79,7 +79,8 @@ cudaError_t launch_energy_reduce(const double* partials, int n, const double* sc
 // cluster: the 2 x 2 multicast form (grid = a multiple of kTcCluster, at most
 // kTcCluster x the max_clusters of prepare_energy_tc); else one CTA per SM
 // taking units from the device counter `queue` (8 bytes, zeroed here on the
-// stream before the launch).  partials: grid pairs {os, ss}.
+// stream before the launch).  partials: pairs {os, ss}, one per unit
+// (sh.nunits) in the queue form, one per CTA (grid) in the cluster form.
 constexpr int kTcCluster = 4;
 cudaError_t launch_energy_tc(const uint16_t* S, const double* eps, const float* sc,
                              const float* dg, const double* scale, const EnergyShape& sh, int Qp,

@@ -19,6 +19,7 @@
 // the same call first.  Calls whose GPU work overlaps (different streams or
 // threads on one device) race on the array and must be serialised by the
 // caller.
+#include <algorithm>
 #include <cmath>
 #include <mutex>
 
@@ -124,7 +125,8 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
   auto carve = [&](Carver& w, Header** hdr, double** partials, unsigned long long** queue,
                    SliceWork* sw) {
     *hdr = static_cast<Header*>(w.take(256));
-    *partials = static_cast<double*>(w.take((size_t)kMaxGrid * 16));
+    *partials = static_cast<double*>(
+        w.take((size_t)std::max<long long>(kMaxGrid, sh.nunits) * 16));  // per CTA or per unit
     *queue = static_cast<unsigned long long*>(w.take(16));
     if (tc) {
       sw->erow = static_cast<int*>(w.take((size_t)R * 4));
@@ -164,7 +166,7 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
     CORR_CUDA(launch_slices(bia, naux, nocc, nvir, Qp, scheme, fmt, p, sw, s));
     CORR_CUDA(launch_energy_tc(sw.S, eps, sw.sc, sw.dg, sw.scale, sh, Qp, fmt, scheme, false,
                                partials, grid, &hdr->status, queue, s));
-    CORR_CUDA(launch_energy_reduce(partials, grid, sw.scale, hdr->e, s));
+    CORR_CUDA(launch_energy_reduce(partials, (int)sh.nunits, sw.scale, hdr->e, s));
   }
   Header h;
   CORR_CUDA(cudaMemcpyAsync(&h, hdr, sizeof(Header), cudaMemcpyDeviceToHost, s));

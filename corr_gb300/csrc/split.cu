@@ -294,6 +294,14 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src, bool valid
                : "memory");
 }
 
+// 16-byte asynchronous global -> shared copy of `bytes` (0, 8 or 16) source
+// bytes, zero-filling the rest; both addresses 16-byte aligned.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, int bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_u32(dst)), "l"(src),
+               "r"(bytes)
+               : "memory");
+}
+
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\n" "cp.async.wait_group 0;\n" ::: "memory");
 }
@@ -321,10 +329,20 @@ __global__ void __launch_bounds__(kStatThreads) rowstat2_smem_kernel(
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5, row = t & (RB - 1);
   const long long r0 = (long long)blockIdx.x * RB;
   const int n = naux * RB;
-  for (int k = t; k < n; k += kStatThreads) {
-    const int q = k / RB, rr = k & (RB - 1);
-    const bool valid = r0 + rr < R;
-    cp_async8(stage + k, valid ? b + (long long)q * R + r0 + rr : b, valid);
+  if ((R & 1) == 0 && ((uintptr_t)b & 15) == 0) {
+    // rows in pairs: 16-byte copies (every row pair's address is 16-byte aligned)
+    for (int k2 = t; 2 * k2 < n; k2 += kStatThreads) {
+      const int k = 2 * k2, q = k / RB, rr = k & (RB - 1);
+      const long long left = R - (r0 + rr);  // rows left from this pair on
+      const int bytes = left >= 2 ? 16 : (left == 1 ? 8 : 0);
+      cp_async16(stage + k, bytes ? b + (long long)q * R + r0 + rr : b, bytes);
+    }
+  } else {
+    for (int k = t; k < n; k += kStatThreads) {
+      const int q = k / RB, rr = k & (RB - 1);
+      const bool valid = r0 + rr < R;
+      cp_async8(stage + k, valid ? b + (long long)q * R + r0 + rr : b, valid);
+    }
   }
   cp_async_wait_all();
   __syncthreads();
@@ -598,7 +616,7 @@ int slice_bits_for(int Qp) {
 }
 
 // Dynamic shared memory of the staged row-statistics kernel: at most this
-// many bytes per block (naux <= 3200 for 4 rows per block).
+// many bytes per block (naux <= 1600 for 8 rows per block, 3200 for 4).
 constexpr size_t kStatSmemMax = 100 * 1024;
 
 // Raise the kernel's dynamic shared memory limit once per device (safe under
@@ -627,13 +645,18 @@ cudaError_t launch_slices(const double* b, int naux, int nocc, int nvir, int Qp,
   const long long Rp = (long long)nocc * ((nvir + 127) / 128) * 128;
   dim3 grid((unsigned)((Rp + 63) / 64), (unsigned)((Qp + 63) / 64));
   if (scheme == kSchemeDigits2) {
-    // rows staged in shared memory, 4 rows per block (four blocks per SM up to
-    // naux ~ 1700), else the two-pass global form
-    const size_t img = (size_t)naux * 4 * 8;
-    if (img <= kStatSmemMax) {
+    // rows staged in shared memory: 8 rows per block (two blocks per SM) up to
+    // naux = 1600, 4 rows per block up to 3200, else the two-pass global form
+    const size_t img8 = (size_t)naux * 8 * 8, img4 = (size_t)naux * 4 * 8;
+    if (img8 <= kStatSmemMax) {
+      e = set_stat_smem<8>();
+      if (e != cudaSuccess) return e;
+      rowstat2_smem_kernel<8><<<(unsigned)((R + 7) / 8), kStatThreads, img8, s>>>(
+          b, naux, R, w.erow, w.diag, w.eref, w.eref + 1);
+    } else if (img4 <= kStatSmemMax) {
       e = set_stat_smem<4>();
       if (e != cudaSuccess) return e;
-      rowstat2_smem_kernel<4><<<(unsigned)((R + 3) / 4), kStatThreads, img, s>>>(
+      rowstat2_smem_kernel<4><<<(unsigned)((R + 3) / 4), kStatThreads, img4, s>>>(
           b, naux, R, w.erow, w.diag, w.eref, w.eref + 1);
     } else {
       rowstat2_kernel<<<(unsigned)((R + 31) / 32), dim3(32, QG), 0, s>>>(

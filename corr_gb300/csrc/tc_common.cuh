@@ -80,7 +80,9 @@ __device__ __forceinline__ void load_level_sum16(uint32_t tb, int c, float inv_l
 // The MMAs of one K=16 step: r[l], q[l] are the row/column descriptors of
 // digit plane l; c0..c2 the three accumulators.  MMAs sharing a row operand
 // run back to back and keep it in the tensor core's A collector buffer (one
-// shared-memory read of each row plane per K step).
+// shared-memory read of each row plane per K step), and no two consecutive
+// MMAs (within or across K steps) write the same accumulator.  The first MMA
+// into each accumulator carries `acc` (0: overwrite at the start of a phase).
 template <int SCHEME>
 __device__ __forceinline__ void issue_digit_mmas(uint32_t c0, uint32_t c1, uint32_t c2,
                                                  const uint64_t* r, const uint64_t* q,
@@ -88,14 +90,14 @@ __device__ __forceinline__ void issue_digit_mmas(uint32_t c0, uint32_t c1, uint3
   if (SCHEME == 1) {
     tc_mma_f16_ca<0>(c0, r[0], q[0], idesc, acc);  // s0.s0'
     tc_mma_f16_ca<2>(c1, r[0], q[1], idesc, acc);  // s0.s1'
-    tc_mma_f16_ca<0>(c1, r[1], q[0], idesc, 1u);   // + s1.s0'
-    tc_mma_f16_ca<2>(c2, r[1], q[1], idesc, acc);  // s1.s1'
+    tc_mma_f16_ca<0>(c2, r[1], q[1], idesc, acc);  // s1.s1'
+    tc_mma_f16_ca<2>(c1, r[1], q[0], idesc, 1u);   // + s1.s0'
   } else {
-    tc_mma_f16_ca<0>(c0, r[0], q[0], idesc, acc);
-    tc_mma_f16_ca<1>(c1, r[0], q[1], idesc, acc);
-    tc_mma_f16_ca<2>(c2, r[0], q[2], idesc, acc);
-    tc_mma_f16_ca<0>(c1, r[1], q[0], idesc, 1u);
-    tc_mma_f16_ca<2>(c2, r[1], q[1], idesc, 1u);
+    tc_mma_f16_ca<0>(c1, r[0], q[1], idesc, acc);
+    tc_mma_f16_ca<1>(c2, r[0], q[2], idesc, acc);
+    tc_mma_f16_ca<2>(c0, r[0], q[0], idesc, acc);
+    tc_mma_f16_ca<0>(c2, r[1], q[1], idesc, 1u);
+    tc_mma_f16_ca<2>(c1, r[1], q[0], idesc, 1u);
     tc_mma_f16(c2, r[2], q[0], idesc, 1u);
   }
 }

@@ -54,8 +54,8 @@ def test_split_matches_oracle(ctx, o, v, X, seed, prec, rel):
 
 
 @pytest.mark.parametrize("o,v,X,seed", [
-    (5, 7, 1600, 21),   # row statistics staged in shared memory, 4 rows per block
-    (3, 41, 3200, 22),  # staged, at its size limit
+    (5, 7, 1600, 21),   # row statistics staged in shared memory, 8 rows per block (limit)
+    (3, 41, 3200, 22),  # staged, 4 rows per block, at its size limit
     (2, 30, 3300, 23),  # beyond the staged form: two-pass global form
 ])
 def test_split_fp16_row_statistics_forms(ctx, o, v, X, seed):
