@@ -104,18 +104,41 @@ struct Unit {
   bool valid;      // contributes to the energy
 };
 
-// Work item k of this CTA's sequence.  Plain: unit k = (pair, tile pair).
-// Cluster: super-unit k = (block pair, tile pair), this CTA's (r, c) member.
+// Work item k.  Queue form: unit k in cost order -- first the units with two
+// MMA phases (i < j and A < B), then those with one (i == j, or A == B), so
+// the last units handed out are the cheap ones.  Cluster form: super-unit
+// k = (block pair, tile pair), this CTA's (r, c) member.
 template <bool CL>
 __device__ __forceinline__ Unit unit_at(long long k, const EnergyShape& sh, int r, int c) {
   Unit u;
-  const int tp = (int)(k % sh.ntpairs);
-  tpair_decode(tp, sh.ntiles, &u.A, &u.B);
   if (!CL) {
-    pair_decode((int)(k / sh.ntpairs), sh.nocc, &u.i, &u.j);
-    u.nph = (u.i == u.j || u.A == u.B) ? 1 : 2;
+    const int o = sh.nocc, nt = sh.ntiles;
+    const long long ps = (long long)o * (o - 1) / 2;      // pairs i < j
+    const long long ts = (long long)nt * (nt - 1) / 2;    // tile pairs A < B
+    int jj, bb;
+    if (k < ps * ts) {
+      pair_decode((int)(k / ts), o - 1, &u.i, &jj);
+      tpair_decode((int)(k % ts), nt - 1, &u.A, &bb);
+      u.j = jj + 1;
+      u.B = bb + 1;
+      u.nph = 2;
+    } else {
+      const long long v = k - ps * ts;
+      if (v < (long long)o * sh.ntpairs) {  // i == j, any tile pair
+        u.i = u.j = (int)(v / sh.ntpairs);
+        tpair_decode((int)(v % sh.ntpairs), nt, &u.A, &u.B);
+      } else {  // i < j, A == B
+        const long long w = v - (long long)o * sh.ntpairs;
+        pair_decode((int)(w / nt), o - 1, &u.i, &jj);
+        u.j = jj + 1;
+        u.A = u.B = (int)(w % nt);
+      }
+      u.nph = 1;
+    }
     u.valid = true;
   } else {
+    const int tp = (int)(k % sh.ntpairs);
+    tpair_decode(tp, sh.ntiles, &u.A, &u.B);
     int a, b;
     pair_decode((int)(k / sh.ntpairs), (sh.nocc + 1) / 2, &a, &b);
     const int i = 2 * a + r, j = 2 * b + c;

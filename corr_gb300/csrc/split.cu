@@ -622,7 +622,7 @@ constexpr size_t kStatSmemMax = 100 * 1024;
 // Raise the kernel's dynamic shared memory limit once per device (safe under
 // stream capture: not a stream operation).
 template <int RB>
-cudaError_t set_stat_smem() {
+static cudaError_t set_stat_smem() {
   static std::atomic<unsigned long long> done{0};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
