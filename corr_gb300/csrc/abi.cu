@@ -301,7 +301,8 @@ namespace corr {
 
 // Scratch of the energy stage for device-resident B and eps.
 static void energy_carve(Carver& w, int nocc, int nvir, int Qp, bool tc, int grid, SliceWork* sw,
-                         double** partials, unsigned long long** queue = nullptr) {
+                         double** partials, unsigned long long** queue = nullptr,
+                         double** red_scratch = nullptr) {
   const long long R = (long long)nocc * nvir;
   if (tc) {
     sw->S = static_cast<uint16_t*>(w.take(slice_bytes(nocc, nvir, Qp)));
@@ -315,6 +316,8 @@ static void energy_carve(Carver& w, int nocc, int nvir, int Qp, bool tc, int gri
   *partials = static_cast<double*>(w.take((size_t)grid * 16));
   unsigned long long* qp = static_cast<unsigned long long*>(w.take(16));  // work-queue counter
   if (queue) *queue = qp;
+  double* rs = static_cast<double*>(w.take((size_t)kReduceBlocks * 16));  // reduction stage 1
+  if (red_scratch) *red_scratch = rs;
 }
 
 static int energy_grid(corr_context* c, const EnergyShape& sh, bool tc) {
@@ -348,8 +351,9 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
   SliceWork sw{};
   double* partials;
   unsigned long long* queue;
+  double* red_scratch;
   energy_carve(w, nocc, nvir, Qp, tc, (int)std::max<long long>(2 * c->sms, sh.nunits), &sw,
-               &partials, &queue);
+               &partials, &queue, &red_scratch);
   if (!tc) {
     mark(c, 1);
     CORR_CUDA(launch_energy_fp64(d_b, d_e, sh, partials, grid, c->stream));
@@ -376,9 +380,17 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
   CORR_CUDA(launch_energy_tc(sw.S, d_e, sw.sc, sw.dg, sw.scale, sh, Qp, fmt, scheme, cluster,
                              partials, lgrid, &c->dres->status, queue, c->stream));
   mark(c, 2);
-  CORR_CUDA(launch_energy_reduce(partials, cluster ? lgrid : (int)sh.nunits, sw.scale, out_e,
-                                 c->stream));
-  c->launches += 5;  // rowstat, slice, rowfactor, energy, reduce
+  int nred = 1;
+  if (cluster) {
+    CORR_CUDA(launch_energy_reduce(partials, lgrid, sw.scale, out_e, c->stream));
+  } else {
+    nred = launch_unit_reduce(partials, (int)sh.nunits, sw.scale, out_e, red_scratch, c->stream);
+    if (nred < 0) {
+      set_error("energy reduction launch failed");
+      return CORR_ERR_CUDA;
+    }
+  }
+  c->launches += 4 + nred;  // rowstat, slice, rowfactor, energy, reduction
   return CORR_OK;
 }
 

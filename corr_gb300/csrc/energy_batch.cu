@@ -81,10 +81,7 @@ __device__ __forceinline__ UnitInfo unit_info(const BatchInst* __restrict__ in, 
   UnitInfo r;
   r.inst = find_instance(in, n, u);
   const BatchInst& b = in[r.inst];
-  const long long lu = u - b.unit_begin;
-  const int p = (int)(lu / b.ntpairs), tp = (int)(lu % b.ntpairs);
-  pair_decode(p, b.o, &r.i, &r.j);
-  tpair_decode(tp, b.ntiles, &r.A, &r.B);
+  unit_decode_cost(u - b.unit_begin, b.o, b.ntiles, b.ntpairs, &r.i, &r.j, &r.A, &r.B);
   return r;
 }
 

@@ -112,29 +112,7 @@ template <bool CL>
 __device__ __forceinline__ Unit unit_at(long long k, const EnergyShape& sh, int r, int c) {
   Unit u;
   if (!CL) {
-    const int o = sh.nocc, nt = sh.ntiles;
-    const long long ps = (long long)o * (o - 1) / 2;      // pairs i < j
-    const long long ts = (long long)nt * (nt - 1) / 2;    // tile pairs A < B
-    int jj, bb;
-    if (k < ps * ts) {
-      pair_decode((int)(k / ts), o - 1, &u.i, &jj);
-      tpair_decode((int)(k % ts), nt - 1, &u.A, &bb);
-      u.j = jj + 1;
-      u.B = bb + 1;
-      u.nph = 2;
-    } else {
-      const long long v = k - ps * ts;
-      if (v < (long long)o * sh.ntpairs) {  // i == j, any tile pair
-        u.i = u.j = (int)(v / sh.ntpairs);
-        tpair_decode((int)(v % sh.ntpairs), nt, &u.A, &u.B);
-      } else {  // i < j, A == B
-        const long long w = v - (long long)o * sh.ntpairs;
-        pair_decode((int)(w / nt), o - 1, &u.i, &jj);
-        u.j = jj + 1;
-        u.A = u.B = (int)(w % nt);
-      }
-      u.nph = 1;
-    }
+    u.nph = unit_decode_cost(k, sh.nocc, sh.ntiles, sh.ntpairs, &u.i, &u.j, &u.A, &u.B);
     u.valid = true;
   } else {
     const int tp = (int)(k % sh.ntpairs);

@@ -123,11 +123,12 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
 
   // carve the static scratch (same order for the size check and the real pass)
   auto carve = [&](Carver& w, Header** hdr, double** partials, unsigned long long** queue,
-                   SliceWork* sw) {
+                   double** red_scratch, SliceWork* sw) {
     *hdr = static_cast<Header*>(w.take(256));
     *partials = static_cast<double*>(
         w.take((size_t)std::max<long long>(kMaxGrid, sh.nunits) * 16));  // per CTA or per unit
     *queue = static_cast<unsigned long long*>(w.take(16));
+    *red_scratch = static_cast<double*>(w.take((size_t)kReduceBlocks * 16));
     if (tc) {
       sw->erow = static_cast<int*>(w.take((size_t)R * 4));
       sw->diag = static_cast<double*>(w.take((size_t)R * 8));
@@ -141,9 +142,10 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
   Header* hdr;
   double* partials;
   unsigned long long* queue;
+  double* red_scratch;
   SliceWork sw{};
   Carver size_pass{nullptr, 0};
-  carve(size_pass, &hdr, &partials, &queue, &sw);
+  carve(size_pass, &hdr, &partials, &queue, &red_scratch, &sw);
   if (size_pass.used > kScratchBytes) {
     set_error(
         "corr_rimp2_energy_noalloc: nocc=%d nvir=%d naux=%d needs %zu bytes of scratch; the "
@@ -153,7 +155,7 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
     return CORR_ERR_BAD_ARG;
   }
   Carver w{ds.ptr, 0};
-  carve(w, &hdr, &partials, &queue, &sw);
+  carve(w, &hdr, &partials, &queue, &red_scratch, &sw);
 
   CORR_CUDA(cudaMemsetAsync(hdr, 0, sizeof(Header), s));  // status and results start at zero
   if (!tc) {
@@ -166,7 +168,10 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
     CORR_CUDA(launch_slices(bia, naux, nocc, nvir, Qp, scheme, fmt, p, sw, s));
     CORR_CUDA(launch_energy_tc(sw.S, eps, sw.sc, sw.dg, sw.scale, sh, Qp, fmt, scheme, false,
                                partials, grid, &hdr->status, queue, s));
-    CORR_CUDA(launch_energy_reduce(partials, (int)sh.nunits, sw.scale, hdr->e, s));
+    if (launch_unit_reduce(partials, (int)sh.nunits, sw.scale, hdr->e, red_scratch, s) < 0) {
+      set_error("corr_rimp2_energy_noalloc: energy reduction launch failed");
+      return CORR_ERR_CUDA;
+    }
   }
   Header h;
   CORR_CUDA(cudaMemcpyAsync(&h, hdr, sizeof(Header), cudaMemcpyDeviceToHost, s));

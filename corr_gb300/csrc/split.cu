@@ -679,6 +679,52 @@ cudaError_t launch_slices(const double* b, int naux, int nocc, int nvir, int Qp,
   return cudaGetLastError();
 }
 
+// First stage of a fixed-order reduction of n {os, ss} pairs: block b sums the
+// contiguous chunk [b chunk, (b+1) chunk) (compensated per thread, then a
+// shared-memory tree) into scratch[2b], scratch[2b+1].
+__global__ void reduce_chunks_kernel(const double* __restrict__ part, int n, int chunk,
+                                     double* __restrict__ scratch) {
+  __shared__ double s_os[256], s_ss[256];
+  const int lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
+  double os = 0.0, ss = 0.0, cos_ = 0.0, css = 0.0;
+  for (int k = lo + threadIdx.x; k < hi; k += 256) {
+    double y = part[2 * k] - cos_;
+    double t = os + y;
+    cos_ = (t - os) - y;
+    os = t;
+    y = part[2 * k + 1] - css;
+    t = ss + y;
+    css = (t - ss) - y;
+    ss = t;
+  }
+  s_os[threadIdx.x] = os;
+  s_ss[threadIdx.x] = ss;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      s_os[threadIdx.x] += s_os[threadIdx.x + w];
+      s_ss[threadIdx.x] += s_ss[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    scratch[2 * blockIdx.x] = s_os[0];
+    scratch[2 * blockIdx.x + 1] = s_ss[0];
+  }
+}
+
+int launch_unit_reduce(const double* partials, int n, const double* scale, double* out,
+                       double* scratch, cudaStream_t s) {
+  if (n <= 2048) {
+    energy_reduce_kernel<<<1, 256, 0, s>>>(partials, n, scale, out);
+    return cudaGetLastError() == cudaSuccess ? 1 : -1;
+  }
+  const int nb = kReduceBlocks, chunk = (n + nb - 1) / nb;
+  reduce_chunks_kernel<<<nb, 256, 0, s>>>(partials, n, chunk, scratch);
+  energy_reduce_kernel<<<1, 256, 0, s>>>(scratch, nb, scale, out);
+  return cudaGetLastError() == cudaSuccess ? 2 : -1;
+}
+
 cudaError_t launch_energy_reduce(const double* partials, int n, const double* scale, double* out,
                                  cudaStream_t s) {
   energy_reduce_kernel<<<1, 256, 0, s>>>(partials, n, scale, out);

@@ -42,6 +42,35 @@ __device__ __forceinline__ void tc_wait_st() {
   asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
+// Unit k of an energy problem with o occupied orbitals and nt virtual tiles
+// (ntp = nt (nt + 1) / 2 tile pairs) in cost order: first the units with two
+// MMA phases (i < j and A < B), then those with one (i == j, or A == B), so a
+// work queue hands out the cheap units last.  Returns the number of phases.
+__device__ __forceinline__ int unit_decode_cost(long long k, int o, int nt, int ntp, int* i,
+                                                int* j, int* A, int* B) {
+  const long long ps = (long long)o * (o - 1) / 2;    // pairs i < j
+  const long long ts = (long long)nt * (nt - 1) / 2;  // tile pairs A < B
+  int jj, bb;
+  if (k < ps * ts) {
+    pair_decode((int)(k / ts), o - 1, i, &jj);
+    tpair_decode((int)(k % ts), nt - 1, A, &bb);
+    *j = jj + 1;
+    *B = bb + 1;
+    return 2;
+  }
+  const long long v = k - ps * ts;
+  if (v < (long long)o * ntp) {  // i == j, any tile pair
+    *i = *j = (int)(v / ntp);
+    tpair_decode((int)(v % ntp), nt, A, B);
+  } else {  // i < j, A == B
+    const long long w = v - (long long)o * ntp;
+    pair_decode((int)(w / nt), o - 1, i, &jj);
+    *j = jj + 1;
+    *A = *B = (int)(w % nt);
+  }
+  return 1;
+}
+
 // 32 columns [c, c+32) of one phase's result in scaled FP32 units, from the
 // three exact integer accumulators at columns tb, tb+128, tb+256 (levels 0, 1,
 // 2 of either scheme): d = acc0 + acc1/L + acc2/L^2.  Every step rounds to
