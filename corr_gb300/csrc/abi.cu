@@ -390,7 +390,7 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
       return CORR_ERR_CUDA;
     }
   }
-  c->launches += 4 + nred;  // rowstat, slice, rowfactor, energy, reduction
+  c->launches += 3 + nred;  // row statistics, slice (+ row factors), energy, reduction
   return CORR_OK;
 }
 

@@ -159,7 +159,7 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
     horder[k] = order[k];
     ub += s.sh.nunits;
   }
-  c->launches += 3LL * n;
+  c->launches += 2LL * n;  // row statistics and slice per instance
   CORR_CUDA(cudaMemcpyAsync(dtab, htab, sizeof(BatchInst) * n, cudaMemcpyHostToDevice, c->stream));
   CORR_CUDA(cudaMemcpyAsync(dorder, horder, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
   CORR_CUDA(cudaMemsetAsync(queue, 0, 8, c->stream));

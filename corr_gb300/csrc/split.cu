@@ -474,8 +474,12 @@ template <int SCHEME, int FMT>
 __global__ void __launch_bounds__(256) slice_kernel(const double* __restrict__ b, int naux,
                                                     int nocc, int nvir, int Qp, int p,
                                                     const int* __restrict__ erow,
-                                                    const int* __restrict__ kglob,
-                                                    uint16_t* __restrict__ S) {
+                                                    const int* __restrict__ eref,
+                                                    uint16_t* __restrict__ S,
+                                                    const double* __restrict__ diag,
+                                                    float* __restrict__ sc,
+                                                    float* __restrict__ dg, double* scale_out) {
+  const int* kglob = eref + 1;
   __shared__ __align__(16) double tile[64][65];
   const int t = threadIdx.x;
   const int ntiles = (nvir + 127) / 128, vp = ntiles * 128;
@@ -505,6 +509,21 @@ __global__ void __launch_bounds__(256) slice_kernel(const double* __restrict__ b
   const int e = real ? erow[r] : INT_MIN / 4;
   const bool live = e > INT_MIN / 8;
   const int cs = (SCHEME == kSchemeDigits2 ? 20 : 2 * (p + 1)) - e;
+  if (q0 == 0 && qc == 0) {
+    // per-row FP32 factors for the energy kernel (the Q-block-0 tiles cover
+    // every row once): sc_r = 2^(e_r - e_ref), dg_r = diag_r 2^(-2 e_ref), and
+    // the global factors 2^(4 e_ref) and 1/L
+    int er = *eref;
+    if (er < -4000) er = 0;  // every row zero
+    if (real) {
+      sc[r] = live ? (float)ldexp(1.0, e - er) : 0.0f;
+      dg[r] = (float)ldexp(diag[r], -2 * er);
+    }
+    if (lin == 0 && t == 0) {
+      scale_out[0] = ldexp(1.0, 4 * er);
+      scale_out[1] = ldexp(1.0, -(SCHEME == kSchemeDigits2 ? eref[1] : p + 1));
+    }
+  }
   const int q = q0 + qc;
   constexpr int NPL = planes_for_scheme(SCHEME);
   const int nkb = Qp / kSliceQ, kb = q / kSliceQ, c0 = (q % kSliceQ) / 8;
@@ -545,28 +564,6 @@ __global__ void __launch_bounds__(256) slice_kernel(const double* __restrict__ b
     *reinterpret_cast<uint4*>(S + plane + at) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
     if (NPL == 3)
       *reinterpret_cast<uint4*>(S + 2 * plane + at) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
-  }
-}
-
-// Per-row FP32 factors for the energy kernel: sc_r = 2^(e_r - e_ref) and the
-// diagonal sum in the same units, dg_r = diag_r 2^(-2 e_ref).  Also writes
-// the global energy factor 2^(4 e_ref) into scale_out[0] and the level
-// factor 1/L into scale_out[1] (scheme 1: L = 2^eref[1]; scheme 0: L = 2^(p+1)).
-__global__ void rowfactor_kernel(const int* __restrict__ erow, const double* __restrict__ diag,
-                                 long long R, const int* eref, int level_log2,
-                                 float* __restrict__ sc, float* __restrict__ dg,
-                                 double* scale_out) {
-  int er = *eref;
-  if (er < -4000) er = 0;  // every row zero
-  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < R;
-       r += (long long)gridDim.x * blockDim.x) {
-    int e = erow[r];
-    sc[r] = (e > INT_MIN / 8) ? (float)ldexp(1.0, e - er) : 0.0f;
-    dg[r] = (float)ldexp(diag[r], -2 * er);
-  }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    scale_out[0] = ldexp(1.0, 4 * er);
-    scale_out[1] = ldexp(1.0, -(level_log2 >= 0 ? level_log2 : eref[1]));
   }
 }
 
@@ -663,19 +660,20 @@ cudaError_t launch_slices(const double* b, int naux, int nocc, int nvir, int Qp,
           b, naux, R, w.erow, w.diag, w.eref, w.eref + 1);
     }
     slice_kernel<kSchemeDigits2, 0><<<grid, 256, 0, s>>>(b, naux, nocc, nvir, Qp, p, w.erow,
-                                                      w.eref + 1, w.S);
+                                                         w.eref, w.S, w.diag, w.sc, w.dg,
+                                                         w.scale);
   } else {
     rowstat_kernel<<<(unsigned)((R + 31) / 32), dim3(32, QG), 0, s>>>(b, naux, R, p, w.erow,
                                                                      w.diag, w.eref);
     if (fmt == 0)
       slice_kernel<kSchemeDigits3, 0><<<grid, 256, 0, s>>>(b, naux, nocc, nvir, Qp, p, w.erow,
-                                                           w.eref + 1, w.S);
+                                                           w.eref, w.S, w.diag, w.sc, w.dg,
+                                                           w.scale);
     else
       slice_kernel<kSchemeDigits3, 1><<<grid, 256, 0, s>>>(b, naux, nocc, nvir, Qp, p, w.erow,
-                                                           w.eref + 1, w.S);
+                                                           w.eref, w.S, w.diag, w.sc, w.dg,
+                                                           w.scale);
   }
-  rowfactor_kernel<<<(unsigned)((R + 255) / 256 < 1024 ? (R + 255) / 256 : 1024), 256, 0, s>>>(
-      w.erow, w.diag, R, w.eref, scheme == kSchemeDigits2 ? -1 : p + 1, w.sc, w.dg, w.scale);
   return cudaGetLastError();
 }
 

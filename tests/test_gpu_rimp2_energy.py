@@ -90,6 +90,25 @@ def test_device_resident_inputs(ctx):
     assert got.as_tuple() == ref.as_tuple()
 
 
+@pytest.mark.parametrize("prec", ["split_fp16", "split_bf16"])
+def test_unaligned_device_input(ctx, prec):
+    """B starting 8 bytes into an allocation (not 16-byte aligned): the
+    pre-pass takes its 8-byte copy path and gives the same energy."""
+    import torch
+
+    o, v, X = 6, 140, 300
+    B, eps = O.synth_rimp2(o, v, X, 123)
+    ed = torch.from_numpy(eps).cuda()
+    aligned = torch.from_numpy(B).cuda()
+    buf = torch.empty(B.size + 1, dtype=torch.float64, device="cuda")
+    shifted = buf[1:].view(B.shape)
+    shifted.copy_(aligned)
+    assert shifted.data_ptr() % 16 == 8
+    a = ctx.rimp2_energy(aligned, ed, o, v, X, prec)
+    b = ctx.rimp2_energy(shifted, ed, o, v, X, prec)
+    assert a.as_tuple() == b.as_tuple()
+
+
 def test_repeat_is_deterministic(ctx):
     o, v, X = 6, 150, 90
     B, eps = O.synth_rimp2(o, v, X, 5)
