@@ -207,6 +207,9 @@ int corr_destroy(corr_context* c) {
   if (c->hres) cudaFreeHost(c->hres);
   for (int k = 0; k < 4; ++k)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+  for (int k = 0; k < 5; ++k)
+    if (c->cev[k]) cudaEventDestroy(c->cev[k]);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   delete c;
   return CORR_OK;
 }
@@ -341,8 +344,39 @@ size_t energy_scratch_bytes(corr_context* c, int nocc, int nvir, int naux, int p
 // Enqueue the energy of device-resident B/eps, carving scratch from `w`
 // (which must already be backed by reserved workspace); results to `res`
 // (device, 4 doubles; NULL = the context's result block).
+// Upload B [naux][R] from host memory into d_b in row chunks on the copy
+// stream and run each chunk's row statistics on the context stream once it has
+// landed: the statistics pass runs under the transfer instead of after it.
+static int upload_with_row_stats(corr_context* c, const double* host_b, double* d_b, int naux,
+                                 int nocc, int nvir, int scheme, int p, SliceWork sw) {
+  constexpr int kChunks = 4;
+  if (!c->copy_stream) {
+    CORR_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    for (int k = 0; k < kChunks + 1; ++k)
+      CORR_CUDA(cudaEventCreateWithFlags(&c->cev[k], cudaEventDisableTiming));
+  }
+  const long long R = (long long)nocc * nvir;
+  const long long per = ((R + kChunks - 1) / kChunks + 31) / 32 * 32;  // rows, multiple of 32
+  CORR_CUDA(reset_row_stats(sw, c->stream));
+  // the slot may still be read by earlier work on the context stream
+  CORR_CUDA(cudaEventRecord(c->cev[kChunks], c->stream));
+  CORR_CUDA(cudaStreamWaitEvent(c->copy_stream, c->cev[kChunks], 0));
+  for (int k = 0; k < kChunks; ++k) {
+    const long long lo = k * per, hi = std::min(R, lo + per);
+    if (lo >= hi) break;
+    CORR_CUDA(cudaMemcpy2DAsync(d_b + lo, (size_t)R * 8, host_b + lo, (size_t)R * 8,
+                                (size_t)(hi - lo) * 8, (size_t)naux, cudaMemcpyHostToDevice,
+                                c->copy_stream));
+    CORR_CUDA(cudaEventRecord(c->cev[k], c->copy_stream));
+    CORR_CUDA(cudaStreamWaitEvent(c->stream, c->cev[k], 0));
+    CORR_CUDA(launch_row_stats(d_b, naux, nocc, nvir, scheme, p, sw, lo, hi, c->stream));
+    c->launches += 1;
+  }
+  return CORR_OK;
+}
+
 int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, const double* d_b,
-                      const double* d_e, int precision, double* res) {
+                      const double* d_e, int precision, double* res, const double* host_b) {
   double* out_e = res ? res : c->dres->e;
   const bool tc = precision != CORR_PREC_FP64;
   const int Qp = padded_naux(naux);
@@ -355,6 +389,10 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
   energy_carve(w, nocc, nvir, Qp, tc, (int)std::max<long long>(2 * c->sms, sh.nunits), &sw,
                &partials, &queue, &red_scratch);
   if (!tc) {
+    if (host_b)
+      CORR_CUDA(cudaMemcpyAsync(const_cast<double*>(d_b), host_b,
+                                (size_t)naux * nocc * nvir * 8, cudaMemcpyHostToDevice,
+                                c->stream));
     mark(c, 1);
     CORR_CUDA(launch_energy_fp64(d_b, d_e, sh, partials, grid, c->stream));
     mark(c, 2);
@@ -365,7 +403,15 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
   const int scheme = scheme_for_precision(precision);
   const int fmt = format_for_scheme(scheme);
   const int p = slice_bits_for(Qp);
-  CORR_CUDA(launch_slices(d_b, naux, nocc, nvir, Qp, scheme, fmt, p, sw, c->stream));
+  if (host_b) {
+    CORR_TRY(upload_with_row_stats(c, host_b, const_cast<double*>(d_b), naux, nocc, nvir, scheme,
+                                   p, sw));
+    CORR_CUDA(launch_slice_planes(d_b, naux, nocc, nvir, Qp, scheme, fmt, p, sw, c->stream));
+    c->launches += 1;
+  } else {
+    CORR_CUDA(launch_slices(d_b, naux, nocc, nvir, Qp, scheme, fmt, p, sw, c->stream));
+    c->launches += 2;
+  }
   if (!c->attrs_set) {
     CORR_CUDA(prepare_energy_tc(&c->tc_clusters));
     c->attrs_set = true;
@@ -390,7 +436,7 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
       return CORR_ERR_CUDA;
     }
   }
-  c->launches += 3 + nred;  // row statistics, slice (+ row factors), energy, reduction
+  c->launches += 1 + nred;  // energy, reduction
   return CORR_OK;
 }
 
@@ -411,13 +457,16 @@ int rimp2_energy_device(corr_context* c, int nocc, int nvir, int naux, const dou
   void* e_slot = e_dev ? nullptr : w.take(ne * 8);
   if (!res) CORR_CUDA(cudaMemsetAsync(c->dres, 0, sizeof(ResultBlock), c->stream));
   mark(c, 0);
-  const double* d_b = static_cast<const double*>(stage_in(c, bia, nb * 8, b_slot));
+  // B: device arrays are used in place; host arrays go to b_slot inside the
+  // energy stage (in row chunks for the precision forms)
+  const double* d_b = b_dev ? bia : static_cast<const double*>(b_slot);
   const double* d_e = static_cast<const double*>(stage_in(c, eps, ne * 8, e_slot));
-  if (!d_b || !d_e) {
+  if (!d_e) {
     set_error("host-to-device copy failed: %s", cudaGetErrorString(cudaGetLastError()));
     return CORR_ERR_CUDA;
   }
-  return rimp2_energy_core(c, w, nocc, nvir, naux, d_b, d_e, precision, res);
+  return rimp2_energy_core(c, w, nocc, nvir, naux, d_b, d_e, precision, res,
+                           b_dev ? nullptr : bia);
 }
 
 }  // namespace corr

@@ -56,6 +56,9 @@ struct corr_context {
   int batch_stages = 3;
   corr::Workspace batch_out;
   void* pinned = nullptr;
+  // chunked upload of host inputs (created on first use)
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t cev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   size_t pinned_cap = 0;
 };
 
@@ -72,6 +75,10 @@ int rimp2_energy_device(corr_context* c, int nocc, int nvir, int naux, const dou
 // Scratch bytes of the energy stage, and the stage itself on device-resident
 // inputs, carving from `w` (already backed by reserved workspace).
 size_t energy_scratch_bytes(corr_context* c, int nocc, int nvir, int naux, int precision);
+// host_b (optional): B still in host memory; the precision forms upload it
+// into d_b in row chunks on the context's copy stream, each chunk's row
+// statistics starting as soon as it has landed; the FP64 form copies it first.
 int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, const double* d_b,
-                      const double* d_e, int precision, double* res);
+                      const double* d_e, int precision, double* res,
+                      const double* host_b = nullptr);
 }  // namespace corr

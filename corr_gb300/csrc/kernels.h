@@ -68,6 +68,14 @@ inline int format_for_scheme(int scheme) { return scheme == kSchemeDigits2 ? 0 :
 int slice_bits_for(int Qp);
 cudaError_t launch_slices(const double* b, int naux, int nocc, int nvir, int Qp, int scheme,
                           int fmt, int p, SliceWork w, cudaStream_t s);
+// The same in parts (for row statistics that follow rows arriving in chunks):
+// reset the reductions, row statistics of rows [rbeg, rend) (rbeg a multiple
+// of 32), then the digit planes once every row is done.
+cudaError_t reset_row_stats(SliceWork w, cudaStream_t s);
+cudaError_t launch_row_stats(const double* b, int naux, int nocc, int nvir, int scheme, int p,
+                             SliceWork w, long long rbeg, long long rend, cudaStream_t s);
+cudaError_t launch_slice_planes(const double* b, int naux, int nocc, int nvir, int Qp,
+                                int scheme, int fmt, int p, SliceWork w, cudaStream_t s);
 // Sum per-CTA partial pairs {os, ss} in fixed order, times `scale` (device),
 // into out[4] = {E_SS, E_OS, E, E_SCS}.
 // The same for many pairs (one per unit): up to kReduceBlocks blocks sum fixed

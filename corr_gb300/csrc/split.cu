@@ -234,6 +234,7 @@ __device__ __forceinline__ void row_pass1_est(const double* __restrict__ b, int 
 // Q-groups; partial results summed over the Q-groups in order.
 __global__ void __launch_bounds__(32 * QG) rowstat2_kernel(const double* __restrict__ b,
                                                            int naux, long long R,
+                                                           long long rbeg, long long rend,
                                                            int* __restrict__ erow,
                                                            double* __restrict__ diag, int* eref,
                                                            int* kglob) {
@@ -242,16 +243,16 @@ __global__ void __launch_bounds__(32 * QG) rowstat2_kernel(const double* __restr
   __shared__ unsigned long long sd[QG][32];
   __shared__ int se[32];
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const long long r = (long long)blockIdx.x * 32 + tx;
+  const long long r = rbeg + (long long)blockIdx.x * 32 + tx;
   unsigned m = 0;
   float sf = 0.f;
-  if (r < R) row_pass1_est(b, naux, R, r, ty, &m, &sf);
+  if (r < rend) row_pass1_est(b, naux, R, r, ty, &m, &sf);
   smax[ty][tx] = m;
   ssum[ty][tx] = sf;
   __syncthreads();
   if (ty == 0) {
     int e = INT_MIN / 4;
-    if (r < R) {
+    if (r < rend) {
       float sfl = sf;
       for (int k = 1; k < QG; ++k) {
         m = smax[k][tx] > m ? smax[k][tx] : m;
@@ -266,7 +267,7 @@ __global__ void __launch_bounds__(32 * QG) rowstat2_kernel(const double* __restr
   }
   __syncthreads();
   const int e = se[tx];
-  const bool live = r < R && e > INT_MIN / 8;
+  const bool live = r < rend && e > INT_MIN / 8;
   RowStats2 st;
   if (live) {
 #pragma unroll 4
@@ -318,7 +319,8 @@ constexpr int kStatThreads = 512;
 
 template <int RB>
 __global__ void __launch_bounds__(kStatThreads) rowstat2_smem_kernel(
-    const double* __restrict__ b, int naux, long long R, int* __restrict__ erow,
+    const double* __restrict__ b, int naux, long long R, long long rbeg, long long rend,
+    int* __restrict__ erow,
     double* __restrict__ diag, int* eref, int* kglob) {
   constexpr int NW = kStatThreads / 32;
   extern __shared__ __align__(16) double stage[];
@@ -327,20 +329,20 @@ __global__ void __launch_bounds__(kStatThreads) rowstat2_smem_kernel(
   __shared__ float w_f[NW][RB];
   __shared__ int se[RB];
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5, row = t & (RB - 1);
-  const long long r0 = (long long)blockIdx.x * RB;
+  const long long r0 = rbeg + (long long)blockIdx.x * RB;
   const int n = naux * RB;
-  if ((R & 1) == 0 && ((uintptr_t)b & 15) == 0) {
+  if ((R & 1) == 0 && (rbeg & 1) == 0 && ((uintptr_t)b & 15) == 0) {
     // rows in pairs: 16-byte copies (every row pair's address is 16-byte aligned)
     for (int k2 = t; 2 * k2 < n; k2 += kStatThreads) {
       const int k = 2 * k2, q = k / RB, rr = k & (RB - 1);
-      const long long left = R - (r0 + rr);  // rows left from this pair on
+      const long long left = rend - (r0 + rr);  // rows left from this pair on
       const int bytes = left >= 2 ? 16 : (left == 1 ? 8 : 0);
       cp_async16(stage + k, bytes ? b + (long long)q * R + r0 + rr : b, bytes);
     }
   } else {
     for (int k = t; k < n; k += kStatThreads) {
       const int q = k / RB, rr = k & (RB - 1);
-      const bool valid = r0 + rr < R;
+      const bool valid = r0 + rr < rend;
       cp_async8(stage + k, valid ? b + (long long)q * R + r0 + rr : b, valid);
     }
   }
@@ -371,7 +373,7 @@ __global__ void __launch_bounds__(kStatThreads) rowstat2_smem_kernel(
       sfl += w_f[w][t];
     }
     int e = INT_MIN / 4;
-    if (r < R) {
+    if (r < rend) {
       e = row_scale2(m, sfl, naux);
       if (e > INT_MIN / 8) atomicMax(eref, e);
       erow[r] = e;
@@ -383,7 +385,7 @@ __global__ void __launch_bounds__(kStatThreads) rowstat2_smem_kernel(
 
   // pass 2 at the row's scale
   const int e = se[row];
-  const bool live = r0 + row < R && e > INT_MIN / 8;
+  const bool live = r0 + row < rend && e > INT_MIN / 8;
   RowStats2 st;
   if (live)
     for (int k = t; k < n; k += kStatThreads) pass2_elem(stage[k], e, st);
@@ -397,7 +399,7 @@ __global__ void __launch_bounds__(kStatThreads) rowstat2_smem_kernel(
     w_d[warp][lane] = st.d;
   }
   __syncthreads();
-  if (t < RB && r0 + t < R && se[t] > INT_MIN / 8) {
+  if (t < RB && r0 + t < rend && se[t] > INT_MIN / 8) {
     RowStats2 tot;
     for (int w = 0; w < NW; ++w) {
       tot.c += w_f[w][t];
@@ -415,20 +417,21 @@ __global__ void __launch_bounds__(kStatThreads) rowstat2_smem_kernel(
 // taken on the integer bit patterns (no FP64 compare); the diagonal needs one
 // FP64 FMA per element.
 __global__ void __launch_bounds__(32 * QG) rowstat_kernel(const double* __restrict__ b, int naux,
-                                                          long long R, int p,
+                                                          long long R, long long rbeg,
+                                                          long long rend, int p,
                                                           int* __restrict__ erow,
                                                           double* __restrict__ diag, int* eref) {
   __shared__ unsigned long long smax[QG][32];
   __shared__ double ssum[QG][32];
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const long long r = (long long)blockIdx.x * 32 + tx;
+  const long long r = rbeg + (long long)blockIdx.x * 32 + tx;
   unsigned long long m = 0;
   double s = 0.0;
-  if (r < R) row_pass1(b, naux, R, r, ty, &m, &s);
+  if (r < rend) row_pass1(b, naux, R, r, ty, &m, &s);
   smax[ty][tx] = m;
   ssum[ty][tx] = s;
   __syncthreads();
-  if (ty == 0 && r < R) {
+  if (ty == 0 && r < rend) {
     for (int k = 1; k < QG; ++k) {
       m = smax[k][tx] > m ? smax[k][tx] : m;
       s += ssum[k][tx];
@@ -632,15 +635,17 @@ static cudaError_t set_stat_smem() {
   return e;
 }
 
-cudaError_t launch_slices(const double* b, int naux, int nocc, int nvir, int Qp, int scheme,
-                          int fmt, int p, SliceWork w, cudaStream_t s) {
-  const long long R = (long long)nocc * nvir;
+cudaError_t reset_row_stats(SliceWork w, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(w.eref, 0x80, sizeof(int), s);  // very negative start
   if (e != cudaSuccess) return e;
-  e = cudaMemsetAsync(w.eref + 1, 0x7f, sizeof(int), s);  // level exponent: min-reduced
-  if (e != cudaSuccess) return e;
-  const long long Rp = (long long)nocc * ((nvir + 127) / 128) * 128;
-  dim3 grid((unsigned)((Rp + 63) / 64), (unsigned)((Qp + 63) / 64));
+  return cudaMemsetAsync(w.eref + 1, 0x7f, sizeof(int), s);  // level exponent: min-reduced
+}
+
+cudaError_t launch_row_stats(const double* b, int naux, int nocc, int nvir, int scheme, int p,
+                             SliceWork w, long long rbeg, long long rend, cudaStream_t s) {
+  const long long R = (long long)nocc * nvir, n = rend - rbeg;
+  if (n <= 0) return cudaSuccess;
+  cudaError_t e = cudaSuccess;
   if (scheme == kSchemeDigits2) {
     // rows staged in shared memory: 8 rows per block (two blocks per SM) up to
     // naux = 1600, 4 rows per block up to 3200, else the two-pass global form
@@ -648,33 +653,50 @@ cudaError_t launch_slices(const double* b, int naux, int nocc, int nvir, int Qp,
     if (img8 <= kStatSmemMax) {
       e = set_stat_smem<8>();
       if (e != cudaSuccess) return e;
-      rowstat2_smem_kernel<8><<<(unsigned)((R + 7) / 8), kStatThreads, img8, s>>>(
-          b, naux, R, w.erow, w.diag, w.eref, w.eref + 1);
+      rowstat2_smem_kernel<8><<<(unsigned)((n + 7) / 8), kStatThreads, img8, s>>>(
+          b, naux, R, rbeg, rend, w.erow, w.diag, w.eref, w.eref + 1);
     } else if (img4 <= kStatSmemMax) {
       e = set_stat_smem<4>();
       if (e != cudaSuccess) return e;
-      rowstat2_smem_kernel<4><<<(unsigned)((R + 3) / 4), kStatThreads, img4, s>>>(
-          b, naux, R, w.erow, w.diag, w.eref, w.eref + 1);
+      rowstat2_smem_kernel<4><<<(unsigned)((n + 3) / 4), kStatThreads, img4, s>>>(
+          b, naux, R, rbeg, rend, w.erow, w.diag, w.eref, w.eref + 1);
     } else {
-      rowstat2_kernel<<<(unsigned)((R + 31) / 32), dim3(32, QG), 0, s>>>(
-          b, naux, R, w.erow, w.diag, w.eref, w.eref + 1);
+      rowstat2_kernel<<<(unsigned)((n + 31) / 32), dim3(32, QG), 0, s>>>(
+          b, naux, R, rbeg, rend, w.erow, w.diag, w.eref, w.eref + 1);
     }
+  } else {
+    rowstat_kernel<<<(unsigned)((n + 31) / 32), dim3(32, QG), 0, s>>>(b, naux, R, rbeg, rend, p,
+                                                                     w.erow, w.diag, w.eref);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_slice_planes(const double* b, int naux, int nocc, int nvir, int Qp,
+                                int scheme, int fmt, int p, SliceWork w, cudaStream_t s) {
+  const long long Rp = (long long)nocc * ((nvir + 127) / 128) * 128;
+  dim3 grid((unsigned)((Rp + 63) / 64), (unsigned)((Qp + 63) / 64));
+  if (scheme == kSchemeDigits2)
     slice_kernel<kSchemeDigits2, 0><<<grid, 256, 0, s>>>(b, naux, nocc, nvir, Qp, p, w.erow,
                                                          w.eref, w.S, w.diag, w.sc, w.dg,
                                                          w.scale);
-  } else {
-    rowstat_kernel<<<(unsigned)((R + 31) / 32), dim3(32, QG), 0, s>>>(b, naux, R, p, w.erow,
-                                                                     w.diag, w.eref);
-    if (fmt == 0)
-      slice_kernel<kSchemeDigits3, 0><<<grid, 256, 0, s>>>(b, naux, nocc, nvir, Qp, p, w.erow,
-                                                           w.eref, w.S, w.diag, w.sc, w.dg,
-                                                           w.scale);
-    else
-      slice_kernel<kSchemeDigits3, 1><<<grid, 256, 0, s>>>(b, naux, nocc, nvir, Qp, p, w.erow,
-                                                           w.eref, w.S, w.diag, w.sc, w.dg,
-                                                           w.scale);
-  }
+  else if (fmt == 0)
+    slice_kernel<kSchemeDigits3, 0><<<grid, 256, 0, s>>>(b, naux, nocc, nvir, Qp, p, w.erow,
+                                                         w.eref, w.S, w.diag, w.sc, w.dg,
+                                                         w.scale);
+  else
+    slice_kernel<kSchemeDigits3, 1><<<grid, 256, 0, s>>>(b, naux, nocc, nvir, Qp, p, w.erow,
+                                                         w.eref, w.S, w.diag, w.sc, w.dg,
+                                                         w.scale);
   return cudaGetLastError();
+}
+
+cudaError_t launch_slices(const double* b, int naux, int nocc, int nvir, int Qp, int scheme,
+                          int fmt, int p, SliceWork w, cudaStream_t s) {
+  cudaError_t e = reset_row_stats(w, s);
+  if (e == cudaSuccess)
+    e = launch_row_stats(b, naux, nocc, nvir, scheme, p, w, 0, (long long)nocc * nvir, s);
+  if (e == cudaSuccess) e = launch_slice_planes(b, naux, nocc, nvir, Qp, scheme, fmt, p, w, s);
+  return e;
 }
 
 // First stage of a fixed-order reduction of n {os, ss} pairs: block b sums the
