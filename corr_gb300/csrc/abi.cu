@@ -200,6 +200,7 @@ int corr_destroy(corr_context* c) {
   if (!c) return CORR_OK;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);  // uploads into the workspace
   if (c->ws.ptr) cudaFree(c->ws.ptr);
   if (c->batch_out.ptr) cudaFree(c->batch_out.ptr);
   if (c->pinned) cudaFreeHost(c->pinned);
