@@ -99,6 +99,16 @@ class Context:
                                         _ptr(eps), _prec(precision), ctypes.byref(out)))
         return out
 
+    def rimp2_energy_estimate(self, bia, eps, nocc, nvir, naux, precision="split_fp16"):
+        """RI-MP2 energy and an estimate (one standard deviation) of its
+        deviation from the FP64 energy of the same inputs.  Returns
+        (MP2Energy, err)."""
+        out = MP2Energy()
+        err = ctypes.c_double(0.0)
+        check(self._L.corr_rimp2_energy_estimate(self._h, int(nocc), int(nvir), int(naux),
+                                                 _ptr(bia), _ptr(eps), _prec(precision),
+                                                 ctypes.byref(out), ctypes.byref(err)))
+        return out, err.value
 
     def rimp2_energy_async(self, bia, eps, nocc, nvir, naux, precision, out):
         """Enqueue only (device tensors; out = device float64[4] receiving

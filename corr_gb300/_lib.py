@@ -68,6 +68,8 @@ SIGNATURES = {
     "corr_get_timing": [_vp, ctypes.POINTER(Timing)],
     "corr_rimp2_energy": [_vp, _i, _i, _i, _vp, _vp, _i, ctypes.POINTER(MP2Energy)],
     "corr_rimp2_energy_async": [_vp, _i, _i, _i, _vp, _vp, _i, _vp],
+    "corr_rimp2_energy_estimate": [_vp, _i, _i, _i, _vp, _vp, _i, ctypes.POINTER(MP2Energy),
+                                   ctypes.POINTER(_d)],
     "corr_sync": [_vp],
     "corr_rimp2_gradient": [_vp, _i, _i, _i, _vp, _vp, _vp, _vp, ctypes.POINTER(MP2Energy)],
     "corr_rimp2_energy_noalloc": [_i, _vp, _i, _i, _i, _vp, _vp, _i, ctypes.POINTER(MP2Energy)],

@@ -276,6 +276,62 @@ int corr_get_timing(const corr_context* c, corr_timing* out) {
   return CORR_OK;
 }
 
+int corr_rimp2_energy_estimate(corr_context* c, int nocc, int nvir, int naux, const double* bia,
+                               const double* eps, int precision, corr_mp2_energy* out,
+                               double* err) {
+  CORR_CHECK_ARG(c != nullptr, "null context");
+  CORR_CHECK_ARG(out != nullptr && err != nullptr && bia != nullptr && eps != nullptr,
+                 "corr_rimp2_energy_estimate: null pointer argument");
+  CORR_CHECK_ARG(nocc >= 1 && nvir >= 1 && naux >= 1,
+                 "corr_rimp2_energy_estimate: sizes must be positive");
+  CORR_CHECK_ARG(precision >= CORR_PREC_FP64 && precision <= CORR_PREC_SPLIT_BF16,
+                 "corr_rimp2_energy_estimate: unknown precision %d", precision);
+  CORR_CHECK_ARG((long long)nocc * nvir <= (1ll << 31) && nocc <= 46000,
+                 "corr_rimp2_energy_estimate: nocc*nvir too large");
+  CORR_CUDA(cudaSetDevice(c->device));
+  if (precision == CORR_PREC_FP64) {  // the reference's own arithmetic: no estimate
+    CORR_TRY(corr_rimp2_energy(c, nocc, nvir, naux, bia, eps, precision, out));
+    *err = 0.0;
+    return CORR_OK;
+  }
+  const size_t nb = (size_t)naux * nocc * nvir, ne = (size_t)nocc + nvir;
+  const bool b_dev = is_device_ptr(bia), e_dev = is_device_ptr(eps);
+  Carver cv{nullptr, 0};
+  if (!b_dev) cv.take(nb * 8);
+  if (!e_dev) cv.take(ne * 8);
+  const size_t head = cv.used;
+  CORR_TRY(c->ws.reserve(head + energy_scratch_bytes(c, nocc, nvir, naux, precision)));
+  Carver w{c->ws.ptr, 0};
+  void* b_slot = b_dev ? nullptr : w.take(nb * 8);
+  void* e_slot = e_dev ? nullptr : w.take(ne * 8);
+  CORR_CUDA(cudaMemsetAsync(c->dres, 0, sizeof(ResultBlock), c->stream));
+  mark(c, 0);
+  const double* d_b = b_dev ? bia : static_cast<const double*>(b_slot);
+  const double* d_e = static_cast<const double*>(stage_in(c, eps, ne * 8, e_slot));
+  if (!d_e) {
+    set_error("host-to-device copy failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return CORR_ERR_CUDA;
+  }
+  // the energy, then the same evaluation one bit coarser per digit (B already
+  // on the device; the scratch carved again from the same offset)
+  Carver w2 = w;
+  CORR_TRY(rimp2_energy_core(c, w, nocc, nvir, naux, d_b, d_e, precision, c->dres->e,
+                             b_dev ? nullptr : bia, 0));
+  CORR_TRY(rimp2_energy_core(c, w2, nocc, nvir, naux, d_b, d_e, precision, c->dres->e + 4,
+                             nullptr, 1));
+  CORR_TRY(finish_results(c, 8));
+  out->e_ss = c->hres->e[0];
+  out->e_os = c->hres->e[1];
+  out->e_total = c->hres->e[2];
+  out->e_scs = c->hres->e[3];
+  // two digits: the difference of the two grids' representations has 6 times
+  // the variance of the fine grid's rounding error; three digits, one bit
+  // coarser each: 8 times the error, nearly independent (1 + 64)
+  const double ratio = precision == CORR_PREC_SPLIT_FP16 ? 6.0 : 65.0;
+  *err = fabs(c->hres->e[6] - c->hres->e[2]) / sqrt(ratio);
+  return CORR_OK;
+}
+
 int corr_rimp2_energy(corr_context* c, int nocc, int nvir, int naux, const double* bia,
                       const double* eps, int precision, corr_mp2_energy* out) {
   CORR_CHECK_ARG(c != nullptr, "null context");
@@ -377,7 +433,8 @@ static int upload_with_row_stats(corr_context* c, const double* host_b, double* 
 }
 
 int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, const double* d_b,
-                      const double* d_e, int precision, double* res, const double* host_b) {
+                      const double* d_e, int precision, double* res, const double* host_b,
+                      int coarse) {
   double* out_e = res ? res : c->dres->e;
   const bool tc = precision != CORR_PREC_FP64;
   const int Qp = padded_naux(naux);
@@ -403,16 +460,24 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
   }
   const int scheme = scheme_for_precision(precision);
   const int fmt = format_for_scheme(scheme);
-  const int p = slice_bits_for(Qp);
+  // coarse: the same evaluation on a grid one bit coarser per digit (the
+  // error estimate of corr_rimp2_energy_estimate)
+  const int p = std::max(1, slice_bits_for(Qp) - (scheme == kSchemeDigits3 ? coarse : 0));
   if (host_b) {
     CORR_TRY(upload_with_row_stats(c, host_b, const_cast<double*>(d_b), naux, nocc, nvir, scheme,
                                    p, sw));
-    CORR_CUDA(launch_slice_planes(d_b, naux, nocc, nvir, Qp, scheme, fmt, p, sw, c->stream));
-    c->launches += 1;
   } else {
-    CORR_CUDA(launch_slices(d_b, naux, nocc, nvir, Qp, scheme, fmt, p, sw, c->stream));
-    c->launches += 2;
+    CORR_CUDA(reset_row_stats(sw, c->stream));
+    CORR_CUDA(launch_row_stats(d_b, naux, nocc, nvir, scheme, p, sw, 0, (long long)nocc * nvir,
+                               c->stream));
+    c->launches += 1;
   }
+  if (coarse && scheme == kSchemeDigits2) {
+    CORR_CUDA(coarsen_level(sw, c->stream));
+    c->launches += 1;
+  }
+  CORR_CUDA(launch_slice_planes(d_b, naux, nocc, nvir, Qp, scheme, fmt, p, sw, c->stream));
+  c->launches += 1;
   if (!c->attrs_set) {
     CORR_CUDA(prepare_energy_tc(&c->tc_clusters));
     c->attrs_set = true;

@@ -80,5 +80,5 @@ size_t energy_scratch_bytes(corr_context* c, int nocc, int nvir, int naux, int p
 // statistics starting as soon as it has landed; the FP64 form copies it first.
 int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, const double* d_b,
                       const double* d_e, int precision, double* res,
-                      const double* host_b = nullptr);
+                      const double* host_b = nullptr, int coarse = 0);
 }  // namespace corr

@@ -72,6 +72,8 @@ cudaError_t launch_slices(const double* b, int naux, int nocc, int nvir, int Qp,
 // reset the reductions, row statistics of rows [rbeg, rend) (rbeg a multiple
 // of 32), then the digit planes once every row is done.
 cudaError_t reset_row_stats(SliceWork w, cudaStream_t s);
+// After the row statistics of the two-digit scheme: halve L (error estimate).
+cudaError_t coarsen_level(SliceWork w, cudaStream_t s);
 cudaError_t launch_row_stats(const double* b, int naux, int nocc, int nvir, int scheme, int p,
                              SliceWork w, long long rbeg, long long rend, cudaStream_t s);
 cudaError_t launch_slice_planes(const double* b, int naux, int nocc, int nvir, int Qp,

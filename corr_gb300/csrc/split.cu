@@ -635,6 +635,18 @@ static cudaError_t set_stat_smem() {
   return e;
 }
 
+// One bit coarser two-digit grid (L/2) for the error estimate of the
+// precision form: k = max(k - 1, 0).
+__global__ void coarsen_level_kernel(int* kglob) {
+  const int k = *kglob;
+  if (k > 0 && k <= kMaxLevelExp) *kglob = k - 1;
+}
+
+cudaError_t coarsen_level(SliceWork w, cudaStream_t s) {
+  coarsen_level_kernel<<<1, 1, 0, s>>>(w.eref + 1);
+  return cudaGetLastError();
+}
+
 cudaError_t reset_row_stats(SliceWork w, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(w.eref, 0x80, sizeof(int), s);  // very negative start
   if (e != cudaSuccess) return e;

@@ -116,6 +116,19 @@ int corr_get_timing(const corr_context* ctx, corr_timing* out);
 int corr_rimp2_energy(corr_context* ctx, int nocc, int nvir, int naux, const double* bia,
                       const double* eps, int precision, corr_mp2_energy* out);
 
+/* corr_rimp2_energy plus an error estimate for the precision forms (no
+ * reference counterpart: the reference computes in FP64): *err estimates the
+ * deviation of E from the FP64 energy of the same inputs (one standard
+ * deviation).  The deviation of a precision form is the rounding of B to its
+ * digit grid, to first order sum_r delta_r . dE/dB_r; the call evaluates the
+ * energy a second time on a grid one bit coarser per digit and scales the
+ * difference by the variance ratio of the two roundings (sqrt 6 for
+ * CORR_PREC_SPLIT_FP16, sqrt 65 for CORR_PREC_SPLIT_BF16).  Twice the cost of
+ * corr_rimp2_energy.  CORR_PREC_FP64: *err = 0. */
+int corr_rimp2_energy_estimate(corr_context* ctx, int nocc, int nvir, int naux, const double* bia,
+                               const double* eps, int precision, corr_mp2_energy* out,
+                               double* err);
+
 /* Asynchronous form of corr_rimp2_energy for device-resident data (no
  * reference counterpart): bia and eps must be device pointers; the call only
  * enqueues work on the context stream and writes {E_SS, E_OS, E, E_SCS} to

@@ -70,3 +70,15 @@ def test_dense_helpers_reject_bad_args_without_gpu():
     p = ctypes.c_void_p(a.ctypes.data)
     assert L.corr_dgemm(None, 0, 0, 2, 2, 2, 1.0, p, 2, p, 2, 0.0, p, 2) == 1
     assert L.corr_syev(None, 2, p, p, p) == 1
+
+
+def test_energy_estimate_rejects_bad_args_without_gpu():
+    import ctypes
+
+    from corr_gb300 import _lib
+
+    L = _lib.load()
+    out = _lib.MP2Energy()
+    err = ctypes.c_double()
+    assert L.corr_rimp2_energy_estimate(None, 1, 1, 1, None, None, 1, ctypes.byref(out),
+                                        ctypes.byref(err)) == 1

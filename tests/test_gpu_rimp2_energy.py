@@ -153,3 +153,30 @@ def test_cluster_form_matches_one_cta_form(ctx, o, v, X, prec):
     if o * v * X <= 13 * 360 * 300:
         ref = O.rimp2_energy(B, eps, o, v)
         assert abs(clu.e_total - ref[2]) <= 2e-7 * abs(ref[2]), (prec, clu, ref)
+
+
+@pytest.mark.parametrize("prec", ["split_fp16", "split_bf16"])
+def test_error_estimate(ctx, prec):
+    """corr_rimp2_energy_estimate: the energy equals corr_rimp2_energy's, and
+    the estimate (one standard deviation of the digit rounding's effect) is of
+    the size of the actual deviation from the FP64 energy: over several
+    workloads the geometric mean of deviation / estimate lies within a factor
+    of 4 of 1 (single cases may be a few sigma out)."""
+    import math
+
+    ratios = []
+    for (o, v, X, seed) in [(8, 128, 300, 31), (12, 200, 400, 32), (16, 256, 512, 33),
+                            (24, 300, 800, 34), (40, 360, 1200, 2024)]:
+        B, eps = O.synth_rimp2(o, v, X, seed)
+        e64 = ctx.rimp2_energy(B, eps, o, v, X, "fp64").e_total
+        e1 = ctx.rimp2_energy(B, eps, o, v, X, prec)
+        e2, est = ctx.rimp2_energy_estimate(B, eps, o, v, X, prec)
+        assert e2.as_tuple() == e1.as_tuple()
+        assert est > 0.0
+        ratios.append(abs(e1.e_total - e64) / est)
+    gm = math.exp(sum(math.log(max(r, 1e-3)) for r in ratios) / len(ratios))
+    print(f"{prec}: deviation / estimate per workload {[round(r, 2) for r in ratios]}, "
+          f"geometric mean {gm:.2f}")
+    assert 0.25 <= gm <= 4.0, ratios
+    e, est = ctx.rimp2_energy_estimate(*O.synth_rimp2(3, 20, 30, 35), 3, 20, 30, "fp64")
+    assert est == 0.0
