@@ -109,7 +109,7 @@ def test_syev_vs_reference_diag_mat(ctx, n):
         assert np.allclose(np.abs((V * G[pre + "vecs"]).sum(1)), 1.0, atol=1e-9)
 
 
-@pytest.mark.parametrize("n", [1, 2, 3, 64, 127, 300])
+@pytest.mark.parametrize("n", [1, 2, 3, 64, 127, 128, 300, 513])
 def test_syev_random_sizes(ctx, n):
     r = O.rng(900 + n)
     a = r.standard_normal((n, n))
@@ -134,6 +134,22 @@ def test_syev_degenerate_and_device(ctx):
     _check_eig(A, w.cpu().numpy(), V.cpu().numpy(), np.sort(lam))
     w, V = ctx.syev(np.eye(5) * 3.0)
     assert np.allclose(w, 3.0, atol=0, rtol=1e-15)
+
+
+def test_syev_clusters_mixed_path(ctx):
+    """n >= 128 runs FP32 sweeps first: clustered and exactly repeated
+    eigenvalues of both signs, and a matrix of tiny norm (the FP32 stage
+    works on A scaled by a power of two)."""
+    r = O.rng(77)
+    n = 260
+    Q, _ = np.linalg.qr(r.standard_normal((n, n)))
+    lam = np.concatenate([np.repeat([-3.0, 1.0], 60), 2.0 + 1e-9 * r.standard_normal(40),
+                          r.uniform(-1.0, 4.0, n - 160)])
+    A = (Q * lam) @ Q.T
+    A = 0.5 * (A + A.T)
+    for scale in (1.0, 2.0 ** -400, 2.0 ** 300):
+        w, V = ctx.syev(A * scale)
+        _check_eig(A * scale, w, V, np.sort(lam) * scale)
 
 
 def _f(fn, *argtypes):

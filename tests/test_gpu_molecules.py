@@ -51,17 +51,46 @@ def test_config1_h2o(ctx):
     assert abs(e3.e_total - g["ri_mp2"][2]) <= 1e-10
 
 
-def test_config3_water_cluster(ctx):
+@pytest.fixture(scope="module")
+def config3():
     g = GOLD.get("config3")
     if g is None:
         pytest.skip("config 3 fixture not generated")
     fx = np.load(os.path.join(HERE, "golden", "config3_cluster.npz"))
-    mos, eps = fx["mos"], fx["eps"]
     I = M.Integrals(M.water_cluster(20, box=g["box"], min_oo=g["min_oo"], seed=g["seed"]),
                     "def2-svp", "def2-svp-ri")
     J, P3 = I.metric(), I.three_center()
     for name, arr in (("J", J), ("P3", P3)):
         assert np.allclose([arr.sum(), (arr * arr).sum()], g["checksums"][name], rtol=1e-11), name
+    return g, J, P3, fx["mos"], fx["eps"]
+
+
+def test_config3_metric_inv_sqrt(ctx, config3):
+    """The full-size J^-1/2 (naux = 1520, condition number ~8e5) through the
+    eigendecomposition: against LAPACK's, and J^-1/2 J J^-1/2 = 1."""
+    import torch
+
+    g, J, _, _, _ = config3
+    ref, ncut_ref = O.ri_metric_inv_sqrt(J)
+    Jd = torch.from_numpy(J).cuda()
+    ctx.ri_metric_inv_sqrt(Jd)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    jm, ncut = ctx.ri_metric_inv_sqrt(Jd)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    jm = jm.cpu().numpy()
+    assert ncut == ncut_ref == g["ncut"]
+    err = np.abs(jm - ref).max() / np.abs(ref).max()
+    unit = np.abs(jm @ J @ jm - np.eye(J.shape[0])).max()
+    print(f"config3 J^-1/2: {dt * 1e3:.1f} ms, max rel diff vs LAPACK {err:.2e}, "
+          f"|J^-1/2 J J^-1/2 - 1| {unit:.2e}")
+    assert err <= 1e-9
+    assert unit <= 1e-9
+
+
+def test_config3_water_cluster(ctx, config3):
+    g, J, P3, mos, eps = config3
     import torch
 
     Jd = torch.from_numpy(J).cuda()

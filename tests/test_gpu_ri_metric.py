@@ -47,6 +47,26 @@ def test_inv_sqrt_vs_oracle(ctx, X):
     assert np.abs(got @ J @ got - np.eye(X)).max() <= 1e-11
 
 
+@pytest.mark.parametrize("X,decades", [(257, 6), (700, 7)])
+def test_inv_sqrt_ill_conditioned(ctx, X, decades):
+    """Orders from 128 on take the FP32 sweeps, the FP64 re-orthogonalisation
+    and the FP64 refinement sweeps; the result must still be the FP64
+    J^-1/2 (spectrum 1 .. 1e-decades, a degenerate block at the top)."""
+    r = O.rng(X + decades)
+    Q, _ = np.linalg.qr(r.standard_normal((X, X)))
+    lam = np.geomspace(1.0, 10.0 ** -decades, X)
+    lam[: X // 10] = lam[X // 10]
+    J = (Q * lam) @ Q.T
+    J = 0.5 * (J + J.T)
+    ref, ncut_ref = O.ri_metric_inv_sqrt(J)
+    got, ncut = ctx.ri_metric_inv_sqrt(J)
+    assert ncut == ncut_ref == 0
+    # LAPACK's own error here is ~ kappa^(1/2) eps relative to max|J^-1/2|
+    assert np.abs(got - ref).max() <= 1e-9 * np.abs(ref).max()
+    G = got @ J @ got
+    assert np.abs(G - np.eye(X)).max() <= 1e-9
+
+
 def test_inv_sqrt_with_cut_eigenvalues(ctx):
     """Rank-deficient metric: the 1e-10 relative cutoff removes X - rank
     eigenvalues; compare the metric-weighted product, which is unique."""
