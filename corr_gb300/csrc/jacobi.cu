@@ -60,7 +60,7 @@ constexpr double kRotTol = 1e-15;          // FP64 sweeps: relative threshold
 constexpr float kRotTol32 = 0x1p-20f;      // FP32 sweeps: relative threshold
 constexpr double kFloor32 = 0x1p-22;       // FP32 sweeps: absolute floor x n (||A||_F ~ 1)
 constexpr int kMaxSweeps = 40, kMaxSweeps32 = 30;
-constexpr int kStop32 = 16;                // FP32 sweeps end below 1/16 of the pairs rotated
+constexpr int kStop32 = 32;                // FP32 sweeps end below 1/32 of the inner rotations
 constexpr int kMixedMin = 128;             // padded order from which the FP32 sweeps run first
 
 template <typename T>
@@ -240,6 +240,217 @@ __global__ void jacobi_apply(T* __restrict__ A, T* __restrict__ V, int n, int r,
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 stage as a two-sided block Jacobi method (Golub & Van Loan, block
+// Jacobi with the same round-robin ordering, on blocks of kBlk indices): the
+// padded order np is a multiple of 2 kBlk, the m = np / kBlk index blocks are
+// paired as the scalar indices are, and a round
+//   1. diagonalises, for each block pair (I, J), the 2kBlk x 2kBlk matrix
+//      A[I+J, I+J] approximately by one cyclic Jacobi sweep in shared memory
+//      (same rotation formula and threshold as above), giving U_IJ;
+//   2. applies all U at once: A[I+J, K+L] <- U_IJ^T A[I+J, K+L] U_KL and
+//      V[:, K+L] <- V[:, K+L] U_KL, as 64 x 64 tile products.
+// A sweep is m-1 rounds instead of n-1, and the work of a round is a dense
+// product rather than n/2 dependent 2x2 rotations, so the FP32 stage is no
+// longer bound by the latency of 1500 rounds per sweep.
+// ---------------------------------------------------------------------------
+constexpr int kBlk = 32, kBlk2 = 64, kSLd = 65;
+
+__device__ __forceinline__ int block_row(int I, int J, int x) {
+  return x < kBlk ? I * kBlk + x : J * kBlk + (x - kBlk);
+}
+
+// CTA t (1024 threads): block pair t of round r.  U_t (64 x 64, row-major)
+// -> Ug + t 4096; *rotated += the rotations applied.  Thread x owns the 2x2
+// block (x / 32, x % 32) of S and the pairs x % 32 of rows x / 32 and
+// x / 32 + 32 of U, so an inner round is one dependent step per thread.  The
+// FP32 stage only has to come close: its rotations are formed with fast
+// division and reciprocal square root, and the FP64 steps after it restore
+// orthogonality.
+constexpr int kInnerThreads = 1024;
+
+__global__ void __launch_bounds__(kInnerThreads) block_inner(const float* __restrict__ Af, int np,
+                                                             int r, float tol, float floor_abs,
+                                                             float* __restrict__ Ug,
+                                                             int* __restrict__ rotated) {
+  __shared__ float S[kBlk2 * kSLd];
+  __shared__ float U[kBlk2 * kSLd];
+  __shared__ float2 cs[kBlk];
+  __shared__ unsigned char pt[kBlk2 - 1][kBlk][2];  // pair table of the 63 inner rounds
+  const int m = np / kBlk;
+  const int tid = threadIdx.x;
+  int I, J;
+  round_pair(m, r, blockIdx.x, &I, &J);
+  for (int e = tid; e < kBlk2 * kBlk2; e += kInnerThreads) {
+    const int x = e / kBlk2, y = e % kBlk2;
+    S[x * kSLd + y] = Af[(size_t)block_row(I, J, x) * np + block_row(I, J, y)];
+    U[x * kSLd + y] = (x == y) ? 1.0f : 0.0f;
+  }
+  for (int e = tid; e < (kBlk2 - 1) * kBlk; e += kInnerThreads) {
+    int p, q;
+    round_pair(kBlk2, e / kBlk, e % kBlk, &p, &q);
+    pt[e / kBlk][e % kBlk][0] = (unsigned char)p;
+    pt[e / kBlk][e % kBlk][1] = (unsigned char)q;
+  }
+  __syncthreads();
+  const float tol2 = tol * tol, floor2 = floor_abs * floor_abs;
+  const int k = tid / kBlk, l = tid % kBlk;  // S block (k, l); U rows k, k + 32, pair l
+  int rot = 0;
+  for (int rr = 0; rr < kBlk2 - 1; ++rr) {
+    if (tid < kBlk) {
+      const int p = pt[rr][tid][0], q = pt[rr][tid][1];
+      const float app = S[p * kSLd + p], aqq = S[q * kSLd + q], apq = S[p * kSLd + q];
+      float c = 1.0f, sn = 0.0f;
+      const float a2 = apq * apq;
+      if (a2 > tol2 * fabsf(app * aqq) && a2 > floor2) {
+        ++rot;
+        const float tau = __fdividef(aqq - app, 2.0f * apq);
+        const float t = __fdividef(copysignf(1.0f, tau), fabsf(tau) + sqrtf(1.0f + tau * tau));
+        c = rsqrtf(1.0f + t * t);
+        sn = t * c;
+        // one Newton step on c^2 + s^2 = 1: the approximate reciprocal square
+        // root is biased, and its error would compound over the ~10^4
+        // rotations that reach every index
+        const float f = 1.5f - 0.5f * (c * c + sn * sn);
+        c *= f;
+        sn *= f;
+      }
+      cs[tid] = make_float2(c, sn);
+    }
+    __syncthreads();
+    const float2 a = cs[k], b = cs[l];
+    const int p = pt[rr][k][0], q = pt[rr][k][1], u = pt[rr][l][0], w = pt[rr][l][1];
+    float* Sp = S + p * kSLd;
+    float* Sq = S + q * kSLd;
+    float* U0 = U + k * kSLd;
+    float* U1 = U + (k + kBlk) * kSLd;
+    const bool doS = !(a.y == 0.0f && b.y == 0.0f), doU = b.y != 0.0f;
+    float x00 = 0, x01 = 0, x10 = 0, x11 = 0, v0u = 0, v0w = 0, v1u = 0, v1w = 0;
+    if (doS) {
+      x00 = Sp[u];
+      x01 = Sp[w];
+      x10 = Sq[u];
+      x11 = Sq[w];
+    }
+    if (doU) {
+      v0u = U0[u];
+      v0w = U0[w];
+      v1u = U1[u];
+      v1w = U1[w];
+    }
+    if (doS) {
+      const float y00 = a.x * x00 - a.y * x10, y01 = a.x * x01 - a.y * x11;
+      const float y10 = a.y * x00 + a.x * x10, y11 = a.y * x01 + a.x * x11;
+      Sp[u] = y00 * b.x - y01 * b.y;
+      Sp[w] = y00 * b.y + y01 * b.x;
+      Sq[u] = y10 * b.x - y11 * b.y;
+      Sq[w] = y10 * b.y + y11 * b.x;
+    }
+    if (doU) {
+      U0[u] = b.x * v0u - b.y * v0w;
+      U0[w] = b.y * v0u + b.x * v0w;
+      U1[u] = b.x * v1u - b.y * v1w;
+      U1[w] = b.y * v1u + b.x * v1w;
+    }
+    __syncthreads();
+  }
+  float* Ut = Ug + (size_t)blockIdx.x * kBlk2 * kBlk2;
+  for (int e = tid; e < kBlk2 * kBlk2; e += kInnerThreads)
+    Ut[e] = U[(e / kBlk2) * kSLd + e % kBlk2];
+  if (tid < 32) {
+    for (int o = 16; o > 0; o >>= 1) rot += __shfl_xor_sync(0xffffffffu, rot, o);
+    if (tid == 0 && rot) atomicAdd(rotated, rot);
+  }
+}
+
+// acc[i][j] += sum_k L[k][ri + i] R[k][rj + j]  (L transposed)  or
+// acc[i][j] += sum_k L[ri + i][k] R[k][rj + j]  (L as is), 64 x 64 operands.
+template <bool LT>
+__device__ __forceinline__ void tile_mm(const float* __restrict__ L, const float* __restrict__ R,
+                                        int ri, int rj, float (&acc)[4][4]) {
+#pragma unroll 8
+  for (int k = 0; k < kBlk2; ++k) {
+    float l4[4];
+    if (LT) {
+      const float4 v = *reinterpret_cast<const float4*>(L + k * kBlk2 + ri);
+      l4[0] = v.x; l4[1] = v.y; l4[2] = v.z; l4[3] = v.w;
+    } else {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) l4[i] = L[(ri + i) * kBlk2 + k];
+    }
+    const float4 r4 = *reinterpret_cast<const float4*>(R + k * kBlk2 + rj);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      acc[i][0] = fmaf(l4[i], r4.x, acc[i][0]);
+      acc[i][1] = fmaf(l4[i], r4.y, acc[i][1]);
+      acc[i][2] = fmaf(l4[i], r4.z, acc[i][2]);
+      acc[i][3] = fmaf(l4[i], r4.w, acc[i][3]);
+    }
+  }
+}
+
+// CTAs [0, (m/2)^2): tile (s, t) of A <- U_s^T A[I_s+J_s, I_t+J_t] U_t;
+// CTAs [(m/2)^2, (m/2)^2 + (np/64)(m/2)): rows 64 rb .. of V[:, I_t+J_t] <- . U_t.
+// Each tile is owned by one CTA, so the update is in place.
+__global__ void __launch_bounds__(256) block_apply(float* __restrict__ Af, float* __restrict__ Vf,
+                                                   int np, int r,
+                                                   const float* __restrict__ Ug) {
+  __shared__ __align__(16) float X[kBlk2 * kBlk2];
+  __shared__ __align__(16) float Ls[kBlk2 * kBlk2];
+  __shared__ __align__(16) float Rs[kBlk2 * kBlk2];
+  const int m = np / kBlk, h = m / 2;
+  const int cta = blockIdx.x;
+  const bool onA = cta < h * h;
+  int s, t, rb = 0;
+  if (onA) {
+    s = cta / h;
+    t = cta % h;
+  } else {
+    const int j = cta - h * h;
+    rb = j / h;
+    t = j % h;
+    s = 0;
+  }
+  int It, Jt, Is = 0, Js = 0;
+  round_pair(m, r, t, &It, &Jt);
+  if (onA) round_pair(m, r, s, &Is, &Js);
+  float* M = onA ? Af : Vf;
+  const int ri = (threadIdx.x >> 4) * 4, rj = (threadIdx.x & 15) * 4;
+  // load the 64 x 64 tile (rows: I_s+J_s or 64 rb .., cols: I_t+J_t) and U_t (and U_s)
+  for (int e = threadIdx.x; e < kBlk2 * kBlk2 / 4; e += blockDim.x) {
+    const int x = e / (kBlk2 / 4), y4 = (e % (kBlk2 / 4)) * 4;
+    const int gx = onA ? block_row(Is, Js, x) : rb * kBlk2 + x;
+    const int gy = block_row(It, Jt, y4);
+    *reinterpret_cast<float4*>(X + x * kBlk2 + y4) =
+        *reinterpret_cast<const float4*>(M + (size_t)gx * np + gy);
+    *reinterpret_cast<float4*>(Rs + x * kBlk2 + y4) =
+        *reinterpret_cast<const float4*>(Ug + (size_t)t * kBlk2 * kBlk2 + x * kBlk2 + y4);
+    if (onA)
+      *reinterpret_cast<float4*>(Ls + x * kBlk2 + y4) =
+          *reinterpret_cast<const float4*>(Ug + (size_t)s * kBlk2 * kBlk2 + x * kBlk2 + y4);
+  }
+  __syncthreads();
+  float acc[4][4] = {};
+  if (onA) {
+    tile_mm<true>(Ls, X, ri, rj, acc);  // Y = U_s^T X
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      *reinterpret_cast<float4*>(X + (ri + i) * kBlk2 + rj) =
+          make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = 0.0f;
+  }
+  tile_mm<false>(X, Rs, ri, rj, acc);  // Z = Y U_t (or X U_t)
+  for (int i = 0; i < 4; ++i) {
+    const int gx = onA ? block_row(Is, Js, ri + i) : rb * kBlk2 + ri + i;
+    const int gy = block_row(It, Jt, rj);
+    *reinterpret_cast<float4*>(M + (size_t)gx * np + gy) =
+        make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+  }
+}
+
 // off = sum_{x != y} A^2, tot = sum A^2 (per block, FP64), then one block sums.
 __global__ void frob_kernel(const double* __restrict__ A, int n, double* __restrict__ part) {
   double off = 0.0, tot = 0.0;
@@ -302,21 +513,24 @@ __global__ void take_diag(const double* __restrict__ A, int n, int m, double* __
   if (x < m) d[x] = A[(size_t)x * n + x];
 }
 
-// Af = A * scale rounded to FP32, Vf = identity (n x n).
-__global__ void narrow_scaled(const double* __restrict__ A, int n, double scale,
+// Af = A * scale rounded to FP32 and zero-padded to np x np, Vf = identity.
+__global__ void narrow_scaled(const double* __restrict__ A, int n, int np, double scale,
                               float* __restrict__ Af, float* __restrict__ Vf) {
-  const long long nn = (long long)n * n;
+  const long long nn = (long long)np * np;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn;
        e += (long long)gridDim.x * blockDim.x) {
-    Af[e] = (float)(A[e] * scale);
-    Vf[e] = (e / n == e % n) ? 1.0f : 0.0f;
+    const int x = (int)(e / np), y = (int)(e % np);
+    Af[e] = (x < n && y < n) ? (float)(A[(size_t)x * n + y] * scale) : 0.0f;
+    Vf[e] = (x == y) ? 1.0f : 0.0f;
   }
 }
 
-__global__ void widen(const float* __restrict__ src, long long count, double* __restrict__ dst) {
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < count;
+// Q (n x n) = the leading n x n block of Vf (np x np), widened to FP64.
+__global__ void widen(const float* __restrict__ Vf, int np, int n, double* __restrict__ Q) {
+  const long long nn = (long long)n * n;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn;
        e += (long long)gridDim.x * blockDim.x)
-    dst[e] = (double)src[e];
+    Q[e] = (double)Vf[(size_t)(e / n) * np + e % n];
 }
 
 // A <- (A + A^T) / 2 (the thread of entry (x, y), x < y, writes both), V = I.
@@ -336,26 +550,18 @@ __global__ void symmetrize_and_identity(double* __restrict__ A, double* __restri
 
 }  // namespace
 
-// One sweep -- the flag reset and the n-1 rounds of two launches -- captured
-// as a CUDA graph on a private stream: a round is a few microseconds of work,
-// and launched one by one from the host the rounds would wait on the launches.
-template <typename T>
-static int capture_sweep(T* A, T* V, typename Pair2<T>::type* cs, int* rotated, int n, T tol,
-                         T floor_abs, cudaGraphExec_t* exec) {
-  const int h = n / 2;
-  const long long napply = (long long)(h + kRowsA - 1) / kRowsA * h +
-                           (long long)(n + kRowsV - 1) / kRowsV * h;
-  const int agrid = (int)((napply + 255) / 256);
+// A sweep -- the counter reset and its rounds -- is captured as a CUDA graph
+// on a private stream and replayed once per sweep: a round is a few
+// microseconds of work, and launched one by one from the host the rounds
+// would wait on the launches.
+template <typename F>
+static int capture_graph(F&& enqueue, cudaGraphExec_t* exec) {
   cudaStream_t cap = nullptr;
   CORR_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
   cudaGraph_t graph = nullptr;
   cudaError_t err = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
   if (err == cudaSuccess) {
-    cudaMemsetAsync(rotated, 0, sizeof(int), cap);
-    for (int r = 0; r < n - 1; ++r) {
-      jacobi_params<T><<<(h + 127) / 128, 128, 0, cap>>>(A, n, r, tol, floor_abs, cs, rotated);
-      jacobi_apply<T><<<agrid, 256, 0, cap>>>(A, V, n, r, cs);
-    }
+    enqueue(cap);
     err = cudaStreamEndCapture(cap, &graph);
   }
   (void)cudaGetLastError();
@@ -369,16 +575,11 @@ static int capture_sweep(T* A, T* V, typename Pair2<T>::type* cs, int* rotated, 
   return CORR_OK;
 }
 
-// Cyclic sweeps on the padded n x n work matrix A (in place -> eigenvalues on
-// the diagonal) accumulating the rotations into V (columns = eigenvectors),
-// until a sweep rotates fewer than stop_below pairs or max_sweeps sweeps ran.
-template <typename T>
-static int jacobi_sweeps(corr_context* c, T* A, T* V, typename Pair2<T>::type* cs, int* rotated,
-                         int n, T tol, T floor_abs, int max_sweeps, long long stop_below = 1) {
-  if (n < 2) return CORR_OK;
+// Replays the sweep graph until a sweep rotates fewer than stop_below pairs
+// (the count the sweep leaves in *rotated) or max_sweeps sweeps ran.
+static int run_sweeps(corr_context* c, cudaGraphExec_t exec, const int* rotated, int max_sweeps,
+                      long long stop_below, long long launches_per_sweep) {
   cudaStream_t s = c->stream;
-  cudaGraphExec_t exec = nullptr;
-  CORR_TRY(capture_sweep<T>(A, V, cs, rotated, n, tol, floor_abs, &exec));
   int status = CORR_OK;
   for (int sweeps = 0; sweeps < max_sweeps; ++sweeps) {
     int hrot = 0;
@@ -391,24 +592,78 @@ static int jacobi_sweeps(corr_context* c, T* A, T* V, typename Pair2<T>::type* c
       status = CORR_ERR_CUDA;
       break;
     }
-    c->launches += 2LL * (n - 1);
+    c->launches += launches_per_sweep;
     if (hrot < stop_below) break;
   }
   cudaGraphExecDestroy(exec);
   return status;
 }
 
-// The four n x n FP64 buffers and the small scratch of one eigendecomposition.
+// Cyclic sweeps on the padded n x n work matrix A (in place -> eigenvalues on
+// the diagonal) accumulating the rotations into V (columns = eigenvectors),
+// until a sweep rotates no pair or max_sweeps sweeps ran.
+template <typename T>
+static int jacobi_sweeps(corr_context* c, T* A, T* V, typename Pair2<T>::type* cs, int* rotated,
+                         int n, T tol, T floor_abs, int max_sweeps) {
+  if (n < 2) return CORR_OK;
+  const int h = n / 2;
+  const long long napply = (long long)(h + kRowsA - 1) / kRowsA * h +
+                           (long long)(n + kRowsV - 1) / kRowsV * h;
+  const int agrid = (int)((napply + 255) / 256);
+  cudaGraphExec_t exec = nullptr;
+  CORR_TRY(capture_graph(
+      [&](cudaStream_t cap) {
+        cudaMemsetAsync(rotated, 0, sizeof(int), cap);
+        for (int r = 0; r < n - 1; ++r) {
+          jacobi_params<T><<<(h + 127) / 128, 128, 0, cap>>>(A, n, r, tol, floor_abs, cs, rotated);
+          jacobi_apply<T><<<agrid, 256, 0, cap>>>(A, V, n, r, cs);
+        }
+      },
+      &exec));
+  return run_sweeps(c, exec, rotated, max_sweeps, 1, 2LL * (n - 1));
+}
+
+// FP32 block sweeps on the np x np matrices Af, Vf (np a multiple of 64),
+// ending when a sweep applies fewer than 1/kStop32 of its inner rotations.
+static int block_sweeps(corr_context* c, float* Af, float* Vf, float* Ug, int* rotated, int np,
+                        float tol, float floor_abs) {
+  const int m = np / kBlk, h = m / 2;
+  const int agrid = h * h + (np / kBlk2) * h;
+  cudaGraphExec_t exec = nullptr;
+  CORR_TRY(capture_graph(
+      [&](cudaStream_t cap) {
+        cudaMemsetAsync(rotated, 0, sizeof(int), cap);
+        for (int r = 0; r < m - 1; ++r) {
+          block_inner<<<h, kInnerThreads, 0, cap>>>(Af, np, r, tol, floor_abs, Ug, rotated);
+          block_apply<<<agrid, 256, 0, cap>>>(Af, Vf, np, r, Ug);
+        }
+      },
+      &exec));
+  const long long visits = (long long)(m - 1) * h * (kBlk2 - 1) * kBlk;
+  return run_sweeps(c, exec, rotated, kMaxSweeps32, visits / kStop32 + 1, 2LL * (m - 1));
+}
+
+// The four n x n FP64 buffers, the FP32 block-sweep matrices and the small
+// scratch of one eigendecomposition.
 struct EigWork {
   double* buf[4];
-  double2* cs;    // n pairs (also n FP32 pairs, and n doubles of host-bound scratch)
-  double* part;   // 2 * kFrobBlocks doubles; its head doubles as the sweep flag
+  float* f32;     // Af, Vf (np x np each) and the U of one round (np/64 x 64 x 64)
+  double2* cs;    // n pairs (also n doubles of host-bound scratch)
+  double* part;   // 2 * kFrobBlocks doubles; its head doubles as the sweep counter
 };
 constexpr int kFrobBlocks = 1024;
+
+static int padded64(int n) { return (n + kBlk2 - 1) / kBlk2 * kBlk2; }
+
+static size_t f32_floats(int n) {
+  const size_t np = (size_t)padded64(n);
+  return 2 * np * np + np * kBlk2;
+}
 
 static EigWork carve_eig(Carver& w, int n) {
   EigWork e;
   for (int b = 0; b < 4; ++b) e.buf[b] = static_cast<double*>(w.take((size_t)n * n * 8));
+  e.f32 = n >= kMixedMin ? static_cast<float*>(w.take(f32_floats(n) * 4)) : nullptr;
   e.cs = static_cast<double2*>(w.take((size_t)n * 16));
   e.part = static_cast<double*>(w.take((size_t)kFrobBlocks * 16));
   return e;
@@ -459,21 +714,23 @@ static int eig_work(corr_context* c, const EigWork& e, int n, double tot, double
     *spare = e.buf[2];
     return CORR_OK;
   }
-  // 1. FP32 sweeps on A / 2^e in buf[3] (Af, Vf: n^2 floats each)
+  // 1. FP32 block sweeps on A / 2^e, zero-padded to np (a multiple of 64)
   int ex = 0;
   std::frexp(std::sqrt(tot), &ex);
-  float* Af = reinterpret_cast<float*>(e.buf[3]);
-  float* Vf = Af + nn;
-  narrow_scaled<<<ig, 256, 0, s>>>(e.buf[0], n, std::ldexp(1.0, -ex), Af, Vf);
+  const int np = padded64(n);
+  const long long npp = (long long)np * np;
+  float* Af = e.f32;
+  float* Vf = Af + npp;
+  float* Ug = Vf + npp;
+  const int pg = (int)std::min<long long>((npp + 255) / 256, 4096);
+  narrow_scaled<<<pg, 256, 0, s>>>(e.buf[0], n, np, std::ldexp(1.0, -ex), Af, Vf);
   CORR_CUDA(cudaGetLastError());
   c->launches += 1;
-  CORR_TRY(jacobi_sweeps<float>(c, Af, Vf, reinterpret_cast<float2*>(e.cs), rotated, n,
-                                kRotTol32, (float)(kFloor32 / n), kMaxSweeps32,
-                                (long long)(n / 2) * (n - 1) / kStop32 + 1));
-  // 2. Q = Vf in FP64, two Newton-Schulz steps Q <- 1.5 Q - 0.5 Q (Q^T Q)
+  CORR_TRY(block_sweeps(c, Af, Vf, Ug, rotated, np, kRotTol32, (float)(kFloor32 / n)));
+  // 2. Q = Vf[:n, :n] in FP64, two Newton-Schulz steps Q <- 1.5 Q - 0.5 Q (Q^T Q)
   double* Q = e.buf[1];
   double* Qn = e.buf[3];
-  widen<<<ig, 256, 0, s>>>(Vf, nn, Q);
+  widen<<<ig, 256, 0, s>>>(Vf, np, n, Q);
   CORR_CUDA(cudaGetLastError());
   c->launches += 1;
   for (int it = 0; it < 2; ++it) {
@@ -550,7 +807,8 @@ int sym_eig_device(corr_context* c, void* ws, const double* Ain, int m, double* 
 // jacobi_workspace_bytes(m)).
 size_t jacobi_workspace_bytes(int m) {
   const int n = m + (m & 1);
-  return (size_t)4 * n * n * 8 + (size_t)n * 16 + (size_t)kFrobBlocks * 16 + (size_t)8 * 256;
+  return (size_t)4 * n * n * 8 + (n >= kMixedMin ? f32_floats(n) * 4 : 0) + (size_t)n * 16 +
+         (size_t)kFrobBlocks * 16 + (size_t)8 * 256;
 }
 
 int ri_inv_sqrt_device(corr_context* c, void* ws, const double* J, int m, double tol,
