@@ -56,6 +56,12 @@ __device__ __forceinline__ void round_pair(int n, int r, int k, int* p, int* q) 
   }
 }
 
+// Element (x, y) of the symmetric work matrix: the FP64 sweeps keep and
+// update its upper triangle only.
+__device__ __forceinline__ size_t sym_at(int x, int y, int n) {
+  return x < y ? (size_t)x * n + y : (size_t)y * n + x;
+}
+
 constexpr double kRotTol = 1e-15;          // FP64 sweeps: relative threshold
 constexpr float kRotTol32 = 0x1p-20f;      // FP32 sweeps: relative threshold
 constexpr double kFloor32 = 0x1p-22;       // FP32 sweeps: absolute floor x n (||A||_F ~ 1)
@@ -84,7 +90,7 @@ __global__ void jacobi_params(const T* __restrict__ A, int n, int r, T tol, T fl
   if (k < n / 2) {
     int p, q;
     round_pair(n, r, k, &p, &q);
-    const T app = A[(size_t)p * n + p], aqq = A[(size_t)q * n + q], apq = A[(size_t)p * n + q];
+    const T app = A[(size_t)p * n + p], aqq = A[(size_t)q * n + q], apq = A[sym_at(p, q, n)];
     T c = 1, s = 0;
     const T mag = fabs(apq);
     if (mag > tol * sqrt(fabs(app * aqq)) && mag > floor_abs) {
@@ -115,8 +121,11 @@ constexpr int kRowsA = 4;  // row pairs k per thread of the A update
 constexpr int kRowsV = 4;  // rows x per thread of the V update
 
 // Thread (kb, l) of the A update: the 2x2 blocks rows {p_k, q_k} x cols
-// {p_l, q_l} for the kRowsA row pairs k = kb kRowsA .. ; thread (xb, l) of the
-// V update: columns {p_l, q_l} of kRowsV rows.  Every load of a thread is
+// {p_l, q_l} for the row pairs k = kb kRowsA .. with k <= l -- A is symmetric,
+// block (l, k) is the transpose of block (k, l), and every element is kept
+// once, in the upper triangle (sym_at); the diagonal block k == l stores its
+// off-diagonal element twice, the same value from the same thread.  Thread
+// (xb, l) of the V update: columns {p_l, q_l} of kRowsV rows.  Every load of a thread is
 // issued before its first store, so each thread has 4 kRowsA (2 kRowsV)
 // independent loads in flight.  A block whose two rotations are both the
 // identity is left as it is (the product would reproduce it exactly).
@@ -148,7 +157,7 @@ __global__ void jacobi_apply(T* __restrict__ A, T* __restrict__ V, int n, int r,
         q[i] = q[i - 1];
         if (k < (int)h) next_pair(n, r, k - 1, &p[i], &q[i]);
       }
-      on[i] = k < (int)h;
+      on[i] = k < (int)h && k <= l;
       a[i] = on[i] ? cs[k] : b;
       on[i] = on[i] && !(a[i].y == T(0) && b.y == T(0));
     }
@@ -156,12 +165,10 @@ __global__ void jacobi_apply(T* __restrict__ A, T* __restrict__ V, int n, int r,
 #pragma unroll
     for (int i = 0; i < kRowsA; ++i) {
       if (on[i]) {
-        const T* Ap = A + (size_t)p[i] * n;
-        const T* Aq = A + (size_t)q[i] * n;
-        x[i][0] = Ap[u];
-        x[i][1] = Ap[w];
-        x[i][2] = Aq[u];
-        x[i][3] = Aq[w];
+        x[i][0] = A[sym_at(p[i], u, n)];
+        x[i][1] = A[sym_at(p[i], w, n)];
+        x[i][2] = A[sym_at(q[i], u, n)];
+        x[i][3] = A[sym_at(q[i], w, n)];
       }
     }
     // Rotations by angles below ~sqrt(eps) have c == 1 exactly (all of them
@@ -176,12 +183,10 @@ __global__ void jacobi_apply(T* __restrict__ A, T* __restrict__ V, int n, int r,
         if (on[i]) {
           const T y00 = fma(-a[i].y, x[i][2], x[i][0]), y01 = fma(-a[i].y, x[i][3], x[i][1]);
           const T y10 = fma(a[i].y, x[i][0], x[i][2]), y11 = fma(a[i].y, x[i][1], x[i][3]);
-          T* Ap = A + (size_t)p[i] * n;
-          T* Aq = A + (size_t)q[i] * n;
-          Ap[u] = fma(-b.y, y01, y00);
-          Ap[w] = fma(b.y, y00, y01);
-          Aq[u] = fma(-b.y, y11, y10);
-          Aq[w] = fma(b.y, y10, y11);
+          A[sym_at(p[i], u, n)] = fma(-b.y, y01, y00);
+          A[sym_at(p[i], w, n)] = fma(b.y, y00, y01);
+          A[sym_at(q[i], u, n)] = fma(-b.y, y11, y10);
+          A[sym_at(q[i], w, n)] = fma(b.y, y10, y11);
         }
       }
       return;
@@ -194,12 +199,10 @@ __global__ void jacobi_apply(T* __restrict__ A, T* __restrict__ V, int n, int r,
         const T y01 = a[i].x * x[i][1] - a[i].y * x[i][3];
         const T y10 = a[i].y * x[i][0] + a[i].x * x[i][2];
         const T y11 = a[i].y * x[i][1] + a[i].x * x[i][3];
-        T* Ap = A + (size_t)p[i] * n;
-        T* Aq = A + (size_t)q[i] * n;
-        Ap[u] = y00 * b.x - y01 * b.y;
-        Ap[w] = y00 * b.y + y01 * b.x;
-        Aq[u] = y10 * b.x - y11 * b.y;
-        Aq[w] = y10 * b.y + y11 * b.x;
+        A[sym_at(p[i], u, n)] = y00 * b.x - y01 * b.y;
+        A[sym_at(p[i], w, n)] = y00 * b.y + y01 * b.x;
+        A[sym_at(q[i], u, n)] = y10 * b.x - y11 * b.y;
+        A[sym_at(q[i], w, n)] = y10 * b.y + y11 * b.x;
       }
     }
   } else if (id < nA + nV) {
