@@ -20,16 +20,18 @@
 // FP64 arithmetic is scarce on this GPU (about 1/60 of its FP32 rate), and a
 // from-scratch Jacobi needs 15-20 sweeps.  From n = kMixedMin on, the sweeps
 // run in two precisions:
-//  1. A / 2^e (||A||_F in [2^(e-1), 2^e)) is rounded to FP32 and swept in FP32
-//     until no pair exceeds 2^-20 sqrt(|a_pp a_qq|) nor the absolute floor
-//     2^-22 / n (at most 30 sweeps); V0 is the product of those rotations.
+//  1. A / 2^e (||A||_F in [2^(e-1), 2^e)) is rounded to FP32, zero-padded to
+//     a multiple of 64 and swept by the FP32 block Jacobi method below (pairs
+//     rotated while above 2^-20 sqrt(|a_pp a_qq|) and the absolute floor
+//     2^-22 / n) until a sweep applies fewer than 1/32 of its inner rotations
+//     (at most 30 sweeps); V0 is the product of those rotations.
 //  2. V0 is widened to FP64 and made orthogonal to working accuracy by two
 //     Newton-Schulz steps of the polar factor, Q <- Q (3 I - Q^T Q) / 2
 //     (Higham, "Functions of Matrices", 8.3); ||Q^T Q - I|| goes from the
 //     FP32 level (~1e-5) to ~1e-10 and then to rounding level.
 //  3. A1 = Q^T A Q (FP64 GEMMs, then symmetrised) is diagonal up to the FP32
 //     residual, and the FP64 sweeps above diagonalise it: A1 = V1 L V1^T in
-//     typically two to four sweeps instead of fifteen or more.
+//     about six sweeps (two of them full) instead of fifteen or more.
 //  4. V = Q V1.
 // Every FP64 step is a similarity by an orthogonal matrix accurate to FP64
 // rounding, so the eigenvalues and vectors carry FP64 errors, as the plain
