@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--workload", default="rimp2", choices=["rimp2", "batch256", "ri_pipeline"],
                     help="batch256: 256 uneven RI-MP2 instances in one batched launch; "
                          "ri_pipeline: time-to-E_corr from the 3-index integrals")
+    ap.add_argument("--nbf", type=int, default=480, help="ri_pipeline: basis functions")
+    ap.add_argument("--nocc", type=int, default=100, help="ri_pipeline: occupied orbitals")
+    ap.add_argument("--naux", type=int, default=1520, help="ri_pipeline: auxiliary functions")
     return ap.parse_args()
 
 
@@ -141,6 +144,23 @@ def blas_threads():
     return os.cpu_count() or 1
 
 
+def cpu_energy_fn():
+    """The reference's RI-MP2 energy on the host: its own compiled code
+    (oracle/_ref) when present on this machine, else the oracle's restatement
+    (same BLAS calls).  Returns (fn(B, eps, nocc, nvir), kind)."""
+    from oracle import oracle as O
+
+    try:
+        from oracle import refwrap
+
+        if os.path.exists(refwrap.SO):
+            refwrap.lib()
+            return refwrap.rimp2_energy, "reference"
+    except Exception:
+        pass
+    return O.rimp2_energy, "port"
+
+
 def cpu_sample(B, eps, nocc_s, min_seconds=10.0, max_reps=50):
     """Time the reference's RI-MP2 loop on the first nocc_s occupied orbitals
     (nocc_s^2 of the workload's nocc^2 pair GEMMs, same nvir and naux).
@@ -151,21 +171,9 @@ def cpu_sample(B, eps, nocc_s, min_seconds=10.0, max_reps=50):
 
     from oracle import oracle as O
 
-    kind = "port"
-    fn = None
-    try:
-        from oracle import refwrap
-
-        if os.path.exists(refwrap.SO):
-            refwrap.lib()
-            fn = refwrap.rimp2_energy
-            kind = "reference"
-    except Exception:
-        fn = None
+    fn, kind = cpu_energy_fn()
     Bs = np.ascontiguousarray(B[:, :nocc_s, :])
     es = np.concatenate([eps[:nocc_s], eps[NOCC:]])
-    if fn is None:
-        fn = O.rimp2_energy
     fn(Bs, es, nocc_s, NVIR)  # warm
     t0 = time.perf_counter()
     reps = 0
@@ -488,6 +496,27 @@ def run_batch(args):
 
     e64 = np.array(e64)
     dE = np.abs(split - e64)
+    cpu = None
+    if not args.no_cpu_baseline:
+        # the reference's CPU energy on the instances in order until ~10 s of
+        # work, as a flop rate, scaled to the whole batch
+        fn, kind = cpu_energy_fn()
+        done = 0
+        fdone = 0.0
+        t0 = time.perf_counter()
+        for (B, e, o, v) in items:
+            fn(B.cpu().numpy(), e.cpu().numpy(), o, v)
+            done += 1
+            fdone += 2.0 * o * o * v * v * B.shape[0]
+            if time.perf_counter() - t0 >= 10.0:
+                break
+        dt = time.perf_counter() - t0
+        rate = fdone / dt
+        cpu = {"value": len(items) * rate / flops, "unit": "instances/s",
+               "cores": blas_threads(), "kind": kind,
+               "sample": f"the first {done} instances of the batch ({fdone / 1e12:.2f} TFLOP "
+                         f"in {dt:.1f} s, {rate / 1e12:.3f} TFLOP/s), scaled by flops to all "
+                         f"{len(items)}"}
     line = {
         "metric": f"batched RI-MP2 instances/s ({len(items)} uneven instances)",
         "value": len(items) / (ms * 1e-3), "unit": "instances/s", "n_gpus": 1,
@@ -504,13 +533,48 @@ def run_batch(args):
                       "split_speedup": f64_s / (ms * 1e-3)},
         "per_instance_abs_err_vs_fp64": {"max": float(dE.max()), "median": float(np.median(dE))},
         "per_instance_rel_err_vs_fp64_max": float((dE / np.abs(e64)).max()),
+        "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
 
 
+def cpu_pipeline(mos, eps, J, P, o):
+    """The same job on the host cores, as the reference computes it: the
+    transform_ri contractions (ri.cc:147-172, BLAS), J^-1/2 by LAPACK's
+    eigendecomposition with the cutoff (ri.cc:50-69), B = J^-1/2 (P|ia) and
+    the RI-MP2 energy (can_mp2.cc:53-132) on the first nocc_s occupied
+    orbitals, scaled by (nocc / nocc_s)^2.  Returns the cpu_baseline object
+    (time-to-E_corr in ms)."""
+    import numpy as np
+
+    from oracle import oracle as O
+
+    mos, eps, J, P = (t.cpu().numpy() for t in (mos, eps, J, P))
+    X, N = P.shape[0], P.shape[1]
+    v = N - o
+    t0 = time.perf_counter()
+    pia = O.transform_ri_np(o, mos, P)
+    t1 = time.perf_counter()
+    jm, _ = O.ri_metric_inv_sqrt(J)
+    B = np.ascontiguousarray((jm @ pia.reshape(X, -1)).reshape(X, o, v))
+    t2 = time.perf_counter()
+    fn, kind = cpu_energy_fn()
+    nocc_s = max(1, min(o, 30))
+    es = np.concatenate([eps[:nocc_s], eps[o:]])
+    te = time.perf_counter()
+    fn(np.ascontiguousarray(B[:, :nocc_s, :]), es, nocc_s, v)
+    t3 = time.perf_counter()
+    energy_ms = (t3 - te) * 1e3 * (o / nocc_s) ** 2
+    total = (t2 - t0) * 1e3 + energy_ms
+    return {"value": total, "unit": "ms", "cores": blas_threads(), "kind": kind,
+            "sample": f"transform {1e3 * (t1 - t0):.0f} ms + J^-1/2 and B {1e3 * (t2 - t1):.0f} ms "
+                      f"(numpy/LAPACK, all cores) + RI-MP2 energy on {nocc_s} of {o} occupied "
+                      f"orbitals scaled by (nocc/{nocc_s})^2: {energy_ms:.0f} ms"}
+
+
 def run_pipeline(args):
-    """RI-MP2 time-to-E_corr from the 3-index integrals at the water-cluster
-    sizes (nbf=480, nocc=100, naux=1520): (P|ia) transform, metric (Cholesky
+    """RI-MP2 time-to-E_corr from the 3-index integrals, by default at the
+    water-cluster sizes (nbf=480, nocc=100, naux=1520): (P|ia) transform, metric (Cholesky
     under the inertia certificate, else Jacobi), energy.  Inputs are seeded
     synthetic stand-ins resident on the GPU (corr_gb300.workloads); the
     tests run the same pipeline on the molecular integrals.  Split form vs
@@ -521,7 +585,7 @@ def run_pipeline(args):
     from corr_gb300 import workloads as W
 
     torch.cuda.set_device(0)
-    N, o, X = 480, 100, 1520
+    N, o, X = args.nbf, args.nocc, args.naux
     v = N - o
     mos, eps, J, P = W.synth_ri_pipeline(N, o, X, 303)
     ctx = corr_gb300.Context(0)
@@ -541,8 +605,12 @@ def run_pipeline(args):
     f64_ms = (time.perf_counter() - t0) * 1e3
     flops = (2.0 * X * N * N * o + 2.0 * X * o * v * N + 1.0 * X * X * o * v
              + 2.0 * o * o * v * v * X)
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_pipeline(mos, eps, J, P, o)
     line = {
-        "metric": "RI-MP2 time-to-E_corr from 3-index integrals (water-cluster sizes)",
+        "metric": "RI-MP2 time-to-E_corr from 3-index integrals"
+                  + (" (water-cluster sizes)" if (N, o, X) == (480, 100, 1520) else ""),
         "value": ms, "unit": "ms", "n_gpus": 1, "steps": steps, "warmup": max(3, args.warmup),
         "ms_per_step": ms, "higher_is_better": False,
         "dtype": "bf16" if prec == "split_bf16" else "f16", "data": "synthetic",
@@ -553,7 +621,7 @@ def run_pipeline(args):
         "fp64_form": {"ms": f64_ms, "split_speedup": f64_ms / ms},
         "energy": {"split": e_split.e_total, "fp64": e64.e_total,
                    "abs_err_vs_fp64": abs(e_split.e_total - e64.e_total)},
-        "cpu_baseline": None,
+        "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
 

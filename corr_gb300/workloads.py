@@ -53,8 +53,11 @@ def synth_ri_pipeline(nbf, nocc, naux, seed, device="cuda"):
     s = 0.1 * torch.exp(-torch.arange(naux, device=device, dtype=f64) / 600.0)
     P = torch.randn((naux, nbf, nbf), generator=g, device=device, dtype=f64) * s[:, None, None]
     P = 0.5 * (P + P.transpose(1, 2))
-    Q, _ = torch.linalg.qr(torch.randn((nbf, nbf), generator=g, device=device, dtype=f64))
-    mos = Q.T.contiguous()
+    # orthonormalised on the host: torch's lazily loaded GPU linear-algebra
+    # library is not always loadable (e.g. under a profiler)
+    R = torch.randn((nbf, nbf), generator=g, device=device, dtype=f64).cpu().numpy()
+    Q, _ = np.linalg.qr(R)
+    mos = torch.from_numpy(np.ascontiguousarray(Q.T)).to(device)
     eo = torch.sort(torch.rand(nocc, generator=g, device=device, dtype=f64) * 1.2 - 1.5)[0]
     ev = torch.sort(torch.rand(nbf - nocc, generator=g, device=device, dtype=f64) * 2.95 + 0.05)[0]
     return mos, torch.cat([eo, ev]).contiguous(), J.contiguous(), P.contiguous()
