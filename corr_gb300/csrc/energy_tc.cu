@@ -1,9 +1,9 @@
 // Precision-form fused RI-MP2 energy on the 5th-generation tensor cores.
 //
 // Input: the 16-bit integer digit planes of B (split.cu; three in scheme 0,
-// two in scheme 1) in the tiled layout of kernels.h: every 128 x 32 operand
-// tile is one contiguous, pre-swizzled 8 KB block fetched with a linear bulk
-// copy (whole 128-byte lines from L2).
+// two in scheme 1) in the tiled layout of kernels.h: every 128 x 64 operand
+// tile is one contiguous, pre-swizzled (128-byte swizzle) 16 KB block fetched
+// with a linear bulk copy (whole 128-byte lines from L2).
 // Work unit = (occupied pair i<=j, virtual tile pair A<=B), tiles of 128.
 //
 // Phase 1 forms D1[a][b] = (ia|jb) for a in A, b in B; phase 2 forms
@@ -12,10 +12,12 @@
 //   0: acc_m = sum_{k+l=m} s_k(row) . s_l(col)^T   (m = 0..2, six MMAs per K=16)
 //   1: acc_0 = s0.s0', acc_1 = s0.s1' + s1.s0', acc_2 = s1.s1'   (four MMAs per K=16)
 // Scheme 1 moves 4 KB of operands per 128x128x16 MMA (two planes of each
-// operand for four MMAs), half of what three planes for three products would:
-// the per-SM operand stream from L2, not the tensor core, bounds these kernels.
-// and the epilogue forms d = sc_row sc_col (value of the digits) in FP32 with
-// round-to-nearest (tc_common.cuh).
+// operand for four MMAs), half of what three planes for three products would.
+// The epilogue forms d = sc_row sc_col (value of the digits) in FP32 with
+// round-to-nearest (tc_common.cuh).  Measured at nocc=40, nvir=360,
+// naux=1200: the tensor pipe is active 73 % of the cycles while shared memory
+// (banks 28 % read, 19 % write; tensor-core path 55 %), L2 (53 %) and DRAM
+// (4 %) all have room: the gaps are the single issuing thread's hand-offs.
 // D1 is parked in TMEM columns 384-511 while D2 accumulates in 0-383.  For
 // i == j, D2 == D1 and phase 2 is skipped; for A == B, D2 = D1^T is obtained
 // by a 32x32-block exchange through shared memory instead of a second pass.  On the (i==j, A==B) diagonal the
@@ -38,8 +40,9 @@
 // outside i <= j < nocc load their share and contribute with weight 0.
 //
 // CTA = 6 warps, persistent, one CTA per SM:
-//   warp 0     bulk-copy producer (lane 0 paces; lanes 0-1 copy the row and column
-//              operand, the adjacent planes of 128x32 each), 4 (scheme 0) or 6 stages
+//   warp 0     bulk-copy producer (lane 0 paces; one lane per 16 KB operand tile:
+//              the digit planes of the row and of the column operand), 2 stages
+//              (scheme 0, 96 KB each) or 3 (scheme 1, 64 KB each)
 //   warp 1     TMEM owner + MMA issuer (one thread), tcgen05.mma kind::f16
 //   warps 2-5  epilogue, one TMEM lane quarter each
 // Every wait is bounded (common.cuh); on a timeout the CTA winds down and the
