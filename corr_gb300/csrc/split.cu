@@ -31,8 +31,8 @@
 // Dropping the s1.s1' product (plain two-term hi/lo splitting) loses every
 // product of two sub-digit elements and biases molecular energies, so it is
 // kept.  (Karatsuba's identity would need three products, but a third plane
-// s0 + s1 per operand: more operand bytes per product, and the operand stream
-// is what bounds the kernel.)  Each accumulator is a tensor-core sum of
+// s0 + s1 per operand: more operand bytes per product, and measured slower.)
+// Each accumulator is a tensor-core sum of
 // integer products, exact in FP32 when every partial sum stays within 2^24;
 // by Cauchy-Schwarz that holds when ||s0||, ||s1|| <= 2^11.5 for every row
 // (acc_1 <= 2 2^11.5 2^11.5), which the pre-pass enforces:
@@ -51,6 +51,7 @@
 #include <cuda_fp16.h>
 
 #include <atomic>
+#include <cmath>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -72,6 +73,29 @@ __device__ __forceinline__ int ceil_log2(double y) {
 }
 
 constexpr int kMaxLevelExp = 10;
+
+// Per-call constants of the scheme-1 row statistics, from naux on the host.
+// The reciprocals are inflated by 2^-40 relative (far above the few roundings
+// of their computation), so every bound they enter stays conservative.
+struct StatConsts {
+  double sest_factor;  // 1 + 2^-16 + (naux + 32) 2^-23: the FP32 estimate's error margin
+  double inv_t0sq;     // 1 / t0^2,  t0 = 2^11.5 - sqrt(naux)/2 - 1
+  double inv_xmax;     // 1 / (2^11 - 2^9 - 1)
+  double inv_tsq;      // 1 / T^2,   T = 2^11.5 - (1/2 + 2^-10) sqrt(naux)
+};
+
+StatConsts stat_consts(int naux) {
+  const double up = 1.0 + 0x1p-40;
+  const double sq = std::sqrt((double)naux);
+  const double t0 = 2896.309375740099 - 0.5 * sq - 1.0;
+  const double T = 2896.309375740099 - (0.5 + 0x1p-10) * sq;
+  StatConsts k;
+  k.sest_factor = 1.0 + 0x1p-16 + (double)(naux + 32) * 0x1p-23;
+  k.inv_t0sq = up / (t0 * t0);
+  k.inv_xmax = up / (2048.0 - 512.0 - 1.0);
+  k.inv_tsq = up / (T * T);
+  return k;
+}
 
 // round(b * 2^c) to nearest (ties away from zero) by 32-bit integer
 // arithmetic on the IEEE-754 fields; exact whenever |b 2^c| < 2^31 (callers
@@ -134,31 +158,52 @@ __device__ __forceinline__ void pass2_elem(double x, int e, RowStats2& st) {
   st.d += (unsigned long long)((long long)X * X) >> 10;
 }
 
+// ceil_log2 of y >= 0 from its IEEE fields (integer instructions only; the
+// FP64 pipe is ~1/64 rate here): y = 1.m 2^(E - 1023) <= 2^c for the smallest
+// c = E - 1023 (m == 0) or E - 1022; 0 for y == 0, as ceil_log2.
+__device__ __forceinline__ int ceil_log2_bits(double y) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(y);
+  const int E = (int)(u >> 52) & 0x7ff;
+  if (E == 0) return u == 0 ? 0 : ceil_log2(y);  // subnormal: the general path
+  return (u & 0xfffffffffffffull) == 0 ? E - 1023 : E - 1022;
+}
+
+// x 2^p for an integer-valued x >= 0 (exact by a power-of-two product when
+// 2^p is a normal double, else through ldexp).
+__device__ __forceinline__ double times_pow2(double x, int p) {
+  if (p < -1022 || p > 1023) return ldexp(x, p);
+  return x * __longlong_as_double((long long)(1023 + p) << 52);
+}
+
 // Row scale e_r of scheme 1 from the pass-1 results: ||x|| <= 2^11.5 -
 // sqrt(naux)/2 - 1 (from the FP32 estimate with its error margin) and
 // max|x| <= 2^11 - 2^9 - 1 (from the upper bound mhi + 1).  INT_MIN/4 for a
-// row without normal elements.
-__device__ __forceinline__ int row_scale2(unsigned mhi, float sfl, int naux) {
+// row without normal elements.  The bounds are compared squared against
+// reciprocals precomputed on the host and rounded up (StatConsts), so e_r is
+// never below the smallest admissible scale; two FP64 products per row.
+__device__ __forceinline__ int row_scale2(unsigned mhi, float sfl, const StatConsts& kc) {
   if ((mhi >> 20) == 0) return INT_MIN / 4;
-  // the FP32 estimate is low by at most ~2^-19 + (naux + 32) 2^-24 relative
-  const double sest = (double)sfl * (1.0 + 0x1p-16 + (double)(naux + 32) * 0x1p-23);
+  const double sest = (double)sfl * kc.sest_factor;
   const double mx = __longlong_as_double((long long)((unsigned long long)(mhi + 1u) << 32));
-  const double t0 = 2896.309375740099 - 0.5 * sqrt((double)naux) - 1.0;
-  const int en = ceil_log2(sqrt(sest) / t0);
-  const int ec = ceil_log2(mx / (2048.0 - 512.0 - 1.0));
+  const int c2 = ceil_log2_bits(sest * kc.inv_t0sq);  // sest / t0^2 <= 2^c2
+  const int en = (c2 + 1) >> 1;                       // sqrt(sest) / t0 <= 2^en
+  const int ec = ceil_log2_bits(mx * kc.inv_xmax);    // max|x| / (2^11 - 2^9 - 1) <= 2^ec
   return en > ec ? en : ec;
 }
 
 // Largest level exponent k (L = 2^k, 0 <= k <= 10) that keeps ||s1|| <= 2^11.5
-// for a row with pass-2 statistics st; also writes the row's diagonal
-// sum_Q B^2.  The FP32 sum c is low by at most ~2^-19 relative: margin 2^-10.
-__device__ __forceinline__ int row_level2(const RowStats2& st, int e, int naux, double* diag) {
-  *diag = ldexp((double)st.d, 2 * e - 30);
-  const double C = (double)st.c * 0x1p-40 * (1.0 + 0x1p-10);
-  const double slack = (0.5 + 0x1p-10) * sqrt((double)naux);
-  int k = kMaxLevelExp;
-  while (k > 0 && ldexp(sqrt(C), k) + slack > 2896.309375740099) --k;  // 2^11.5
-  return k;
+// for a row with pass-2 statistics st, i.e. 2^k sqrt(C) + slack <= 2^11.5 with
+// slack = (1/2 + 2^-10) sqrt(naux), or 4^k C <= T^2 with T = 2^11.5 - slack
+// (0 when none does); also writes the row's diagonal sum_Q B^2.  The FP32 sum
+// c is low by at most ~2^-19 relative: margin 2^-10.
+__device__ __forceinline__ int row_level2(const RowStats2& st, int e, const StatConsts& kc,
+                                          double* diag) {
+  *diag = times_pow2((double)st.d, 2 * e - 30);
+  if (st.c == 0.0f) return kMaxLevelExp;
+  const double C = (double)st.c * (0x1p-40 * (1.0 + 0x1p-10));
+  const int c = ceil_log2_bits(C * kc.inv_tsq);  // C / T^2 <= 2^c
+  const int k = (-c) >> 1;                       // the largest k with 2k <= -c
+  return k < 0 ? 0 : (k > kMaxLevelExp ? kMaxLevelExp : k);
 }
 
 // Row statistics are taken by blocks of 32 rows x QG Q-groups: for a fixed
@@ -237,7 +282,7 @@ __global__ void __launch_bounds__(32 * QG) rowstat2_kernel(const double* __restr
                                                            long long rbeg, long long rend,
                                                            int* __restrict__ erow,
                                                            double* __restrict__ diag, int* eref,
-                                                           int* kglob) {
+                                                           int* kglob, StatConsts kc) {
   __shared__ unsigned smax[QG][32];
   __shared__ float ssum[QG][32];
   __shared__ unsigned long long sd[QG][32];
@@ -258,7 +303,7 @@ __global__ void __launch_bounds__(32 * QG) rowstat2_kernel(const double* __restr
         m = smax[k][tx] > m ? smax[k][tx] : m;
         sfl += ssum[k][tx];
       }
-      e = row_scale2(m, sfl, naux);
+      e = row_scale2(m, sfl, kc);
       if (e > INT_MIN / 8) atomicMax(eref, e);
       erow[r] = e;
       if (e <= INT_MIN / 8) diag[r] = 0.0;
@@ -282,7 +327,7 @@ __global__ void __launch_bounds__(32 * QG) rowstat2_kernel(const double* __restr
       st.d += sd[k][tx];
     }
     double dg;
-    const int k = row_level2(st, e, naux, &dg);
+    const int k = row_level2(st, e, kc, &dg);
     diag[r] = dg;
     atomicMin(kglob, k);
   }
@@ -321,7 +366,7 @@ template <int RB>
 __global__ void __launch_bounds__(kStatThreads) rowstat2_smem_kernel(
     const double* __restrict__ b, int naux, long long R, long long rbeg, long long rend,
     int* __restrict__ erow,
-    double* __restrict__ diag, int* eref, int* kglob) {
+    double* __restrict__ diag, int* eref, int* kglob, StatConsts kc) {
   constexpr int NW = kStatThreads / 32;
   extern __shared__ __align__(16) double stage[];
   __shared__ unsigned long long w_d[NW][RB];
@@ -374,7 +419,7 @@ __global__ void __launch_bounds__(kStatThreads) rowstat2_smem_kernel(
     }
     int e = INT_MIN / 4;
     if (r < rend) {
-      e = row_scale2(m, sfl, naux);
+      e = row_scale2(m, sfl, kc);
       if (e > INT_MIN / 8) atomicMax(eref, e);
       erow[r] = e;
       if (e <= INT_MIN / 8) diag[r] = 0.0;
@@ -406,7 +451,7 @@ __global__ void __launch_bounds__(kStatThreads) rowstat2_smem_kernel(
       tot.d += w_d[w][t];
     }
     double dg;
-    const int k = row_level2(tot, se[t], naux, &dg);
+    const int k = row_level2(tot, se[t], kc, &dg);
     diag[r0 + t] = dg;
     atomicMin(kglob, k);
   }
@@ -459,8 +504,8 @@ __device__ __forceinline__ uint32_t pack16(int v0, int v1) {
 }
 
 // B[Q][r] -> digit planes in the tiled layout of the energy kernels
-// (kernels.h, slice_tile_offset): one 8 KB tile per (i, 32-Q block, plane,
-// 128-row virtual tile), each stored exactly as the 64-byte-swizzled shared
+// (kernels.h, slice_tile_offset): one 16 KB tile per (i, 64-Q block, plane,
+// 128-row virtual tile), each stored exactly as the 128-byte-swizzled shared
 // memory image the tensor-core descriptors read, so the kernels fetch a
 // tile with one linear bulk copy.  Rows a >= nvir of the last tile and
 // Q >= naux are zero.
@@ -666,15 +711,15 @@ cudaError_t launch_row_stats(const double* b, int naux, int nocc, int nvir, int 
       e = set_stat_smem<8>();
       if (e != cudaSuccess) return e;
       rowstat2_smem_kernel<8><<<(unsigned)((n + 7) / 8), kStatThreads, img8, s>>>(
-          b, naux, R, rbeg, rend, w.erow, w.diag, w.eref, w.eref + 1);
+          b, naux, R, rbeg, rend, w.erow, w.diag, w.eref, w.eref + 1, stat_consts(naux));
     } else if (img4 <= kStatSmemMax) {
       e = set_stat_smem<4>();
       if (e != cudaSuccess) return e;
       rowstat2_smem_kernel<4><<<(unsigned)((n + 3) / 4), kStatThreads, img4, s>>>(
-          b, naux, R, rbeg, rend, w.erow, w.diag, w.eref, w.eref + 1);
+          b, naux, R, rbeg, rend, w.erow, w.diag, w.eref, w.eref + 1, stat_consts(naux));
     } else {
       rowstat2_kernel<<<(unsigned)((n + 31) / 32), dim3(32, QG), 0, s>>>(
-          b, naux, R, rbeg, rend, w.erow, w.diag, w.eref, w.eref + 1);
+          b, naux, R, rbeg, rend, w.erow, w.diag, w.eref, w.eref + 1, stat_consts(naux));
     }
   } else {
     rowstat_kernel<<<(unsigned)((n + 31) / 32), dim3(32, QG), 0, s>>>(b, naux, R, rbeg, rend, p,
