@@ -360,10 +360,11 @@ int corr_rimp2_energy(corr_context* c, int nocc, int nvir, int naux, const doubl
 namespace corr {
 
 // Scratch of the energy stage for device-resident B and eps.
-static void energy_carve(Carver& w, int nocc, int nvir, int Qp, bool tc, int grid, SliceWork* sw,
-                         double** partials, unsigned long long** queue = nullptr,
+static void energy_carve(Carver& w, int nocc, int nvir, int Qp, bool tc, bool x20, int grid,
+                         SliceWork* sw, double** partials, unsigned long long** queue = nullptr,
                          double** red_scratch = nullptr) {
   const long long R = (long long)nocc * nvir;
+  if (tc && x20) sw->x20 = static_cast<int*>(w.take((size_t)Qp * R * 4));
   if (tc) {
     sw->S = static_cast<uint16_t*>(w.take(slice_bytes(nocc, nvir, Qp)));
     sw->erow = static_cast<int*>(w.take((size_t)R * 4));
@@ -380,6 +381,12 @@ static void energy_carve(Carver& w, int nocc, int nvir, int Qp, bool tc, int gri
   if (red_scratch) *red_scratch = rs;
 }
 
+// split_fp16 hands the row statistics' fixed-point values to the slice (one
+// extra 4-byte array of naux x nocc x nvir) when the statistics run in shared memory.
+static bool stage_x20(int precision, int naux) {
+  return precision == CORR_PREC_SPLIT_FP16 && row_stats_stage_x20(naux);
+}
+
 static int energy_grid(corr_context* c, const EnergyShape& sh, bool tc) {
   int grid = tc ? c->sms : c->sms * 2;
   if ((long long)grid > sh.nunits) grid = (int)sh.nunits;
@@ -393,7 +400,8 @@ size_t energy_scratch_bytes(corr_context* c, int nocc, int nvir, int naux, int p
   SliceWork sw{};
   double* part;
   Carver cv{nullptr, 0};
-  energy_carve(cv, nocc, nvir, Qp, tc, (int)std::max<long long>(2 * c->sms, sh.nunits), &sw,
+  energy_carve(cv, nocc, nvir, Qp, tc, stage_x20(precision, naux),
+               (int)std::max<long long>(2 * c->sms, sh.nunits), &sw,
                &part);  // partials of any grid or one per unit
   return cv.used + 256;
 }
@@ -444,8 +452,9 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
   double* partials;
   unsigned long long* queue;
   double* red_scratch;
-  energy_carve(w, nocc, nvir, Qp, tc, (int)std::max<long long>(2 * c->sms, sh.nunits), &sw,
-               &partials, &queue, &red_scratch);
+  energy_carve(w, nocc, nvir, Qp, tc, stage_x20(precision, naux),
+               (int)std::max<long long>(2 * c->sms, sh.nunits), &sw, &partials, &queue,
+               &red_scratch);
   if (!tc) {
     if (host_b)
       CORR_CUDA(cudaMemcpyAsync(const_cast<double*>(d_b), host_b,

@@ -52,7 +52,12 @@ struct SliceWork {
   float* dg;       // [R] diag in scaled units
   int* eref;       // [2] {e_ref, level exponent k (scheme 1)}
   double* scale;   // [2] {global energy factor 2^(4 e_ref), 1/L}
+  int* x20;        // [naux][R] fixed-point values at the row scale (scheme 1), or null:
+                   // written by the row statistics, read by the slice (row_stats_stage_x20)
 };
+// Whether the scheme-1 row statistics of this naux run in the shared-memory
+// form, which can hand the 20-bit fixed-point values on to the slice (SliceWork::x20).
+bool row_stats_stage_x20(int naux);
 // Slice schemes (split.cu).  0: three BF16 digits, six products per K step
 // (levels 0..2).  1: two FP16 digits, four products per K step into three
 // accumulators (s0.s0', s0.s1' + s1.s0', s1.s1').

@@ -150,12 +150,17 @@ struct RowStats2 {
   unsigned long long d = 0;
 };
 
-__device__ __forceinline__ void pass2_elem(double x, int e, RowStats2& st) {
+__device__ __forceinline__ int pass2_elem_x(double x, int e, RowStats2& st) {
   const int X = round_scaled32(x, 20 - e);
   const int s0 = (X + (1 << 19)) >> 20;
   const float fr = small_int_to_float(X - (s0 << 20));
   st.c = fmaf(fr, fr, st.c);
   st.d += (unsigned long long)((long long)X * X) >> 10;
+  return X;
+}
+
+__device__ __forceinline__ void pass2_elem(double x, int e, RowStats2& st) {
+  (void)pass2_elem_x(x, e, st);
 }
 
 // ceil_log2 of y >= 0 from its IEEE fields (integer instructions only; the
@@ -340,6 +345,13 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src, bool valid
                : "memory");
 }
 
+// 4-byte asynchronous global -> shared copy (zero-filled when !valid).
+__device__ __forceinline__ void cp_async4(void* dst, const void* src, bool valid) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(smem_u32(dst)), "l"(src),
+               "r"(valid ? 4 : 0)
+               : "memory");
+}
+
 // 16-byte asynchronous global -> shared copy of `bytes` (0, 8 or 16) source
 // bytes, zero-filling the rest; both addresses 16-byte aligned.
 __device__ __forceinline__ void cp_async16(void* dst, const void* src, int bytes) {
@@ -366,7 +378,7 @@ template <int RB>
 __global__ void __launch_bounds__(kStatThreads) rowstat2_smem_kernel(
     const double* __restrict__ b, int naux, long long R, long long rbeg, long long rend,
     int* __restrict__ erow,
-    double* __restrict__ diag, int* eref, int* kglob, StatConsts kc) {
+    double* __restrict__ diag, int* eref, int* kglob, StatConsts kc, int* __restrict__ x20) {
   constexpr int NW = kStatThreads / 32;
   extern __shared__ __align__(16) double stage[];
   __shared__ unsigned long long w_d[NW][RB];
@@ -428,12 +440,23 @@ __global__ void __launch_bounds__(kStatThreads) rowstat2_smem_kernel(
   }
   __syncthreads();
 
-  // pass 2 at the row's scale
+  // pass 2 at the row's scale; with x20, every row of the range also leaves
+  // its fixed-point values X20 (0 for a row without normal elements) for the
+  // slice, which then reads 4 bytes per element instead of 8
   const int e = se[row];
-  const bool live = r0 + row < rend && e > INT_MIN / 8;
+  const bool inrange = r0 + row < rend;
+  const bool live = inrange && e > INT_MIN / 8;
   RowStats2 st;
-  if (live)
+  if (x20) {
+    if (inrange)
+      for (int k = t; k < n; k += kStatThreads) {
+        int X = 0;
+        if (live) X = pass2_elem_x(stage[k], e, st);
+        x20[(long long)(k / RB) * R + r0 + row] = X;
+      }
+  } else if (live) {
     for (int k = t; k < n; k += kStatThreads) pass2_elem(stage[k], e, st);
+  }
 #pragma unroll
   for (int o = RB; o < 32; o <<= 1) {
     st.c += __shfl_xor_sync(0xffffffffu, st.c, o);
@@ -518,8 +541,9 @@ __device__ __forceinline__ uint32_t pack16(int v0, int v1) {
 // X = round(B 2^(2(p+1) - e_r)), s0 = round(X/L^2), s1 = round((X - s0 L^2)/L),
 // s2 = remainder; scheme 1: X20 = round(B 2^(20 - e_r)) and digits2, planes
 // s0, s1.
-template <int SCHEME, int FMT>
-__global__ void __launch_bounds__(256) slice_kernel(const double* __restrict__ b, int naux,
+template <int SCHEME, int FMT, bool X20IN>
+__global__ void __launch_bounds__(256) slice_kernel(const double* __restrict__ b,
+                                                    const int* __restrict__ x20, int naux,
                                                     int nocc, int nvir, int Qp, int p,
                                                     const int* __restrict__ erow,
                                                     const int* __restrict__ eref,
@@ -529,6 +553,7 @@ __global__ void __launch_bounds__(256) slice_kernel(const double* __restrict__ b
                                                     float* __restrict__ dg, double* scale_out) {
   const int* kglob = eref + 1;
   __shared__ __align__(16) double tile[64][65];
+  int(*tilei)[65] = reinterpret_cast<int(*)[65]>(&tile[0][0]);  // X20IN: X20 values
   const int t = threadIdx.x;
   const int ntiles = (nvir + 127) / 128, vp = ntiles * 128;
   const long long R = (long long)nocc * nvir, Rp = (long long)nocc * vp;
@@ -545,10 +570,13 @@ __global__ void __launch_bounds__(256) slice_kernel(const double* __restrict__ b
   const bool real = rp < Rp && a < nvir;
   const long long r = (long long)i * nvir + a;
 #pragma unroll
-  for (int k = t >> 6; k < 64; k += 4) {  // 16 asynchronous 8-byte copies, all in flight
+  for (int k = t >> 6; k < 64; k += 4) {  // 16 asynchronous copies, all in flight
     const int q = q0 + k;
     const bool valid = real && q < naux;
-    cp_async8(&tile[k][rl], valid ? b + (long long)q * R + r : b, valid);
+    if (X20IN)
+      cp_async4(&tilei[k][rl], valid ? x20 + (long long)q * R + r : x20, valid);
+    else
+      cp_async8(&tile[k][rl], valid ? b + (long long)q * R + r : b, valid);
   }
   cp_async_wait_all();
   __syncthreads();
@@ -592,7 +620,9 @@ __global__ void __launch_bounds__(256) slice_kernel(const double* __restrict__ b
       int d0[2], d1[2], d2[2];
 #pragma unroll
       for (int u = 0; u < 2; ++u) {
-        const int X = live ? round_scaled32(tile[qc + 8 * h + j + u][rl], cs) : 0;
+        const int X = !live ? 0
+                      : (X20IN ? tilei[qc + 8 * h + j + u][rl]
+                               : round_scaled32(tile[qc + 8 * h + j + u][rl], cs));
         if (SCHEME == kSchemeDigits2) {
           digits2(X, k, &d0[u], &d1[u]);
           d2[u] = 0;
@@ -711,12 +741,12 @@ cudaError_t launch_row_stats(const double* b, int naux, int nocc, int nvir, int 
       e = set_stat_smem<8>();
       if (e != cudaSuccess) return e;
       rowstat2_smem_kernel<8><<<(unsigned)((n + 7) / 8), kStatThreads, img8, s>>>(
-          b, naux, R, rbeg, rend, w.erow, w.diag, w.eref, w.eref + 1, stat_consts(naux));
+          b, naux, R, rbeg, rend, w.erow, w.diag, w.eref, w.eref + 1, stat_consts(naux), w.x20);
     } else if (img4 <= kStatSmemMax) {
       e = set_stat_smem<4>();
       if (e != cudaSuccess) return e;
       rowstat2_smem_kernel<4><<<(unsigned)((n + 3) / 4), kStatThreads, img4, s>>>(
-          b, naux, R, rbeg, rend, w.erow, w.diag, w.eref, w.eref + 1, stat_consts(naux));
+          b, naux, R, rbeg, rend, w.erow, w.diag, w.eref, w.eref + 1, stat_consts(naux), w.x20);
     } else {
       rowstat2_kernel<<<(unsigned)((n + 31) / 32), dim3(32, QG), 0, s>>>(
           b, naux, R, rbeg, rend, w.erow, w.diag, w.eref, w.eref + 1, stat_consts(naux));
@@ -728,22 +758,24 @@ cudaError_t launch_row_stats(const double* b, int naux, int nocc, int nvir, int 
   return cudaGetLastError();
 }
 
+bool row_stats_stage_x20(int naux) { return (size_t)naux * 4 * 8 <= kStatSmemMax; }
+
 cudaError_t launch_slice_planes(const double* b, int naux, int nocc, int nvir, int Qp,
                                 int scheme, int fmt, int p, SliceWork w, cudaStream_t s) {
   const long long Rp = (long long)nocc * ((nvir + 127) / 128) * 128;
   dim3 grid((unsigned)((Rp + 63) / 64), (unsigned)((Qp + 63) / 64));
-  if (scheme == kSchemeDigits2)
-    slice_kernel<kSchemeDigits2, 0><<<grid, 256, 0, s>>>(b, naux, nocc, nvir, Qp, p, w.erow,
-                                                         w.eref, w.S, w.diag, w.sc, w.dg,
-                                                         w.scale);
+  if (scheme == kSchemeDigits2 && w.x20 && row_stats_stage_x20(naux))
+    slice_kernel<kSchemeDigits2, 0, true><<<grid, 256, 0, s>>>(
+        b, w.x20, naux, nocc, nvir, Qp, p, w.erow, w.eref, w.S, w.diag, w.sc, w.dg, w.scale);
+  else if (scheme == kSchemeDigits2)
+    slice_kernel<kSchemeDigits2, 0, false><<<grid, 256, 0, s>>>(
+        b, nullptr, naux, nocc, nvir, Qp, p, w.erow, w.eref, w.S, w.diag, w.sc, w.dg, w.scale);
   else if (fmt == 0)
-    slice_kernel<kSchemeDigits3, 0><<<grid, 256, 0, s>>>(b, naux, nocc, nvir, Qp, p, w.erow,
-                                                         w.eref, w.S, w.diag, w.sc, w.dg,
-                                                         w.scale);
+    slice_kernel<kSchemeDigits3, 0, false><<<grid, 256, 0, s>>>(
+        b, nullptr, naux, nocc, nvir, Qp, p, w.erow, w.eref, w.S, w.diag, w.sc, w.dg, w.scale);
   else
-    slice_kernel<kSchemeDigits3, 1><<<grid, 256, 0, s>>>(b, naux, nocc, nvir, Qp, p, w.erow,
-                                                         w.eref, w.S, w.diag, w.sc, w.dg,
-                                                         w.scale);
+    slice_kernel<kSchemeDigits3, 1, false><<<grid, 256, 0, s>>>(
+        b, nullptr, naux, nocc, nvir, Qp, p, w.erow, w.eref, w.S, w.diag, w.sc, w.dg, w.scale);
   return cudaGetLastError();
 }
 
