@@ -448,12 +448,16 @@ __global__ void __launch_bounds__(kStatThreads) rowstat2_smem_kernel(
   const bool live = inrange && e > INT_MIN / 8;
   RowStats2 st;
   if (x20) {
-    if (inrange)
-      for (int k = t; k < n; k += kStatThreads) {
+    if (inrange) {
+      // element k = t + 512 j is (q, row) = (k / RB, k % RB): q advances by 512 / RB per step
+      int* xp = x20 + (long long)(t / RB) * R + r0 + row;
+      const long long step = (long long)(kStatThreads / RB) * R;
+      for (int k = t; k < n; k += kStatThreads, xp += step) {
         int X = 0;
         if (live) X = pass2_elem_x(stage[k], e, st);
-        x20[(long long)(k / RB) * R + r0 + row] = X;
+        *xp = X;
       }
+    }
   } else if (live) {
     for (int k = t; k < n; k += kStatThreads) pass2_elem(stage[k], e, st);
   }
