@@ -544,7 +544,8 @@ __device__ __forceinline__ uint32_t pack16(int v0, int v1) {
 // conflict-free shared reads) and stores one 32-byte sector per plane.  Scheme 0 (levels):
 // X = round(B 2^(2(p+1) - e_r)), s0 = round(X/L^2), s1 = round((X - s0 L^2)/L),
 // s2 = remainder; scheme 1: X20 = round(B 2^(20 - e_r)) and digits2, planes
-// s0, s1.
+// s0, s1.  X20IN (scheme 1): the tile holds the X20 values the row statistics
+// stored (4-byte copies of SliceWork::x20) instead of B, and no conversion runs.
 template <int SCHEME, int FMT, bool X20IN>
 __global__ void __launch_bounds__(256) slice_kernel(const double* __restrict__ b,
                                                     const int* __restrict__ x20, int naux,
