@@ -505,7 +505,8 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
   if (cluster) {
     CORR_CUDA(launch_energy_reduce(partials, lgrid, sw.scale, out_e, c->stream));
   } else {
-    nred = launch_unit_reduce(partials, (int)sh.nunits, sw.scale, out_e, red_scratch, c->stream);
+    nred = launch_unit_reduce(partials, (int)sh.nunits, sw.scale, out_e, red_scratch,
+                              reinterpret_cast<unsigned*>(queue + 1), c->stream);
     if (nred < 0) {
       set_error("energy reduction launch failed");
       return CORR_ERR_CUDA;

@@ -649,7 +649,8 @@ cudaError_t launch_energy_tc(const uint16_t* S, const double* eps, const float* 
   const uint32_t idesc = idesc_f16((uint32_t)fmt, TILE, TILE);
   const int nkb = Qp / KB;
   if (!cluster) {
-    cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
+    // the queue counter and, after it, the ticket of the final reduction
+    cudaError_t e = cudaMemsetAsync(queue, 0, 2 * sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
   }
   if (scheme == kSchemeDigits2)

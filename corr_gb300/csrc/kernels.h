@@ -85,12 +85,13 @@ cudaError_t launch_slice_planes(const double* b, int naux, int nocc, int nvir, i
                                 int scheme, int fmt, int p, SliceWork w, cudaStream_t s);
 // Sum per-CTA partial pairs {os, ss} in fixed order, times `scale` (device),
 // into out[4] = {E_SS, E_OS, E, E_SCS}.
-// The same for many pairs (one per unit): up to kReduceBlocks blocks sum fixed
-// chunks into scratch (kReduceBlocks pairs), one block sums those.  Returns the
-// kernels launched (1 or 2), or -1 on a launch error.
+// The same for many pairs (one per unit): kReduceBlocks blocks sum fixed
+// chunks into scratch (kReduceBlocks pairs) and the last block to finish sums
+// those in chunk order (one launch; *ticket, a device counter, must be 0).
+// Returns the kernels launched (1), or -1 on a launch error.
 constexpr int kReduceBlocks = 64;
 int launch_unit_reduce(const double* partials, int n, const double* scale, double* out,
-                       double* scratch, cudaStream_t s);
+                       double* scratch, unsigned* ticket, cudaStream_t s);
 cudaError_t launch_energy_reduce(const double* partials, int n, const double* scale, double* out,
                                  cudaStream_t s);
 

@@ -168,7 +168,8 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
     CORR_CUDA(launch_slices(bia, naux, nocc, nvir, Qp, scheme, fmt, p, sw, s));
     CORR_CUDA(launch_energy_tc(sw.S, eps, sw.sc, sw.dg, sw.scale, sh, Qp, fmt, scheme, false,
                                partials, grid, &hdr->status, queue, s));
-    if (launch_unit_reduce(partials, (int)sh.nunits, sw.scale, hdr->e, red_scratch, s) < 0) {
+    if (launch_unit_reduce(partials, (int)sh.nunits, sw.scale, hdr->e, red_scratch,
+                           reinterpret_cast<unsigned*>(queue + 1), s) < 0) {
       set_error("corr_rimp2_energy_noalloc: energy reduction launch failed");
       return CORR_ERR_CUDA;
     }

@@ -793,12 +793,17 @@ cudaError_t launch_slices(const double* b, int naux, int nocc, int nvir, int Qp,
   return e;
 }
 
-// First stage of a fixed-order reduction of n {os, ss} pairs: block b sums the
+// Fixed-order reduction of n {os, ss} pairs in one launch: block b sums the
 // contiguous chunk [b chunk, (b+1) chunk) (compensated per thread, then a
-// shared-memory tree) into scratch[2b], scratch[2b+1].
-__global__ void reduce_chunks_kernel(const double* __restrict__ part, int n, int chunk,
-                                     double* __restrict__ scratch) {
+// shared-memory tree) into scratch[2b], scratch[2b+1]; the last block to finish
+// (each block takes a ticket after a fenced write of its sums; no block waits
+// for another) forms the energy from the chunk sums in chunk order, exactly as
+// energy_reduce_kernel does from per-CTA partials.  *ticket is 0 on entry.
+__global__ void reduce_chunks_last_kernel(const double* __restrict__ part, int n, int chunk,
+                                          double* scratch, unsigned* ticket,
+                                          const double* __restrict__ scale, double* out) {
   __shared__ double s_os[256], s_ss[256];
+  __shared__ bool last;
   const int lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
   double os = 0.0, ss = 0.0, cos_ = 0.0, css = 0.0;
   for (int k = lo + threadIdx.x; k < hi; k += 256) {
@@ -824,19 +829,53 @@ __global__ void reduce_chunks_kernel(const double* __restrict__ part, int n, int
   if (threadIdx.x == 0) {
     scratch[2 * blockIdx.x] = s_os[0];
     scratch[2 * blockIdx.x + 1] = s_ss[0];
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const int nb = (int)gridDim.x;
+  os = ss = cos_ = css = 0.0;
+  for (int k = threadIdx.x; k < nb; k += 256) {  // compensated, fixed order
+    double y = __ldcg(&scratch[2 * k]) - cos_;
+    double t = os + y;
+    cos_ = (t - os) - y;
+    os = t;
+    y = __ldcg(&scratch[2 * k + 1]) - css;
+    t = ss + y;
+    css = (t - ss) - y;
+    ss = t;
+  }
+  s_os[threadIdx.x] = os;
+  s_ss[threadIdx.x] = ss;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      s_os[threadIdx.x] += s_os[threadIdx.x + w];
+      s_ss[threadIdx.x] += s_ss[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double sc = scale ? scale[0] : 1.0;
+    const double eos = s_os[0] * sc, ess = s_ss[0] * sc;
+    out[0] = ess;
+    out[1] = eos;
+    out[2] = ess + eos;
+    out[3] = ess / 3.0 + eos * 6.0 / 5.0;
   }
 }
 
 int launch_unit_reduce(const double* partials, int n, const double* scale, double* out,
-                       double* scratch, cudaStream_t s) {
+                       double* scratch, unsigned* ticket, cudaStream_t s) {
   if (n <= 2048) {
     energy_reduce_kernel<<<1, 256, 0, s>>>(partials, n, scale, out);
     return cudaGetLastError() == cudaSuccess ? 1 : -1;
   }
   const int nb = kReduceBlocks, chunk = (n + nb - 1) / nb;
-  reduce_chunks_kernel<<<nb, 256, 0, s>>>(partials, n, chunk, scratch);
-  energy_reduce_kernel<<<1, 256, 0, s>>>(scratch, nb, scale, out);
-  return cudaGetLastError() == cudaSuccess ? 2 : -1;
+  reduce_chunks_last_kernel<<<nb, 256, 0, s>>>(partials, n, chunk, scratch, ticket, scale, out);
+  return cudaGetLastError() == cudaSuccess ? 1 : -1;
 }
 
 cudaError_t launch_energy_reduce(const double* partials, int n, const double* scale, double* out,
