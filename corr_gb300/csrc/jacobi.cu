@@ -69,7 +69,7 @@ constexpr float kRotTol32 = 0x1p-20f;      // FP32 sweeps: relative threshold
 constexpr double kFloor32 = 0x1p-22;       // FP32 sweeps: absolute floor x n (||A||_F ~ 1)
 constexpr int kMaxSweeps = 40, kMaxSweeps32 = 30;
 constexpr int kStop32 = 32;                // FP32 sweeps end below 1/32 of the inner rotations
-constexpr int kMixedMin = 128;             // padded order from which the FP32 sweeps run first
+constexpr int kMixedMin = 64;              // padded order from which the FP32 sweeps run first
 
 template <typename T>
 struct Pair2;

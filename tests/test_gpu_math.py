@@ -137,7 +137,7 @@ def test_syev_degenerate_and_device(ctx):
 
 
 def test_syev_clusters_mixed_path(ctx):
-    """n >= 128 runs FP32 sweeps first: clustered and exactly repeated
+    """n >= 64 runs FP32 sweeps first: clustered and exactly repeated
     eigenvalues of both signs, and a matrix of tiny norm (the FP32 stage
     works on A scaled by a power of two)."""
     r = O.rng(77)

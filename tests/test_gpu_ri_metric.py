@@ -49,7 +49,7 @@ def test_inv_sqrt_vs_oracle(ctx, X):
 
 @pytest.mark.parametrize("X,decades", [(257, 6), (700, 7)])
 def test_inv_sqrt_ill_conditioned(ctx, X, decades):
-    """Orders from 128 on take the FP32 sweeps, the FP64 re-orthogonalisation
+    """Orders from 64 on take the FP32 sweeps, the FP64 re-orthogonalisation
     and the FP64 refinement sweeps; the result must still be the FP64
     J^-1/2 (spectrum 1 .. 1e-decades, a degenerate block at the top)."""
     r = O.rng(X + decades)
