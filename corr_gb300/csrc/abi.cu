@@ -201,6 +201,8 @@ int corr_destroy(corr_context* c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);  // uploads into the workspace
+  for (int k = 0; k < corr_context::kPreStreams; ++k)
+    if (c->pre_stream[k]) cudaStreamSynchronize(c->pre_stream[k]);
   if (c->ws.ptr) cudaFree(c->ws.ptr);
   if (c->batch_out.ptr) cudaFree(c->batch_out.ptr);
   if (c->pinned) cudaFreeHost(c->pinned);
@@ -211,6 +213,10 @@ int corr_destroy(corr_context* c) {
   for (int k = 0; k < 5; ++k)
     if (c->cev[k]) cudaEventDestroy(c->cev[k]);
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+  for (int k = 0; k < corr_context::kPreStreams; ++k)
+    if (c->pre_stream[k]) cudaStreamDestroy(c->pre_stream[k]);
+  for (int k = 0; k <= corr_context::kPreStreams; ++k)
+    if (c->pre_ev[k]) cudaEventDestroy(c->pre_ev[k]);
   delete c;
   return CORR_OK;
 }

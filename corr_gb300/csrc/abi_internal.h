@@ -59,6 +59,11 @@ struct corr_context {
   // chunked upload of host inputs (created on first use)
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t cev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  // side streams of the batched pre-pass (instances sliced concurrently) and
+  // their fork/join events (the last one marks the fork on the context stream)
+  static constexpr int kPreStreams = 8;
+  cudaStream_t pre_stream[kPreStreams] = {};
+  cudaEvent_t pre_ev[kPreStreams + 1] = {};
   size_t pinned_cap = 0;
 };
 

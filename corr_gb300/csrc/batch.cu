@@ -101,7 +101,7 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
   int* dorder;
   unsigned long long* queue;
   carve(cv, sws, &unit_part, &dtab, &dorder, &queue);
-  if (c->ws.cap < cv.used) {
+  if (c->ws.cap < cv.used || (tc && !c->pre_stream[0])) {  // workspace or side streams to create
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     cudaStreamIsCapturing(c->stream, &cs);
     if (cs != cudaStreamCaptureStatusNone) {
@@ -137,12 +137,25 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
   char* hp = static_cast<char*>(c->pinned);
   BatchInst* htab = reinterpret_cast<BatchInst*>(hp);
   int* horder = reinterpret_cast<int*>(hp + ((sizeof(BatchInst) * n + 127) & ~(size_t)127));
+  // The instances' pre-passes are independent and mostly small (a few blocks
+  // each): they run on kPreStreams side streams forked from and joined back
+  // into the context stream (parallel branches when the call is captured).
+  constexpr int K = corr_context::kPreStreams;
+  if (!c->pre_stream[0]) {
+    for (int k = 0; k < K; ++k)
+      CORR_CUDA(cudaStreamCreateWithFlags(&c->pre_stream[k], cudaStreamNonBlocking));
+    for (int k = 0; k <= K; ++k)
+      CORR_CUDA(cudaEventCreateWithFlags(&c->pre_ev[k], cudaEventDisableTiming));
+  }
+  const int nside = n < K ? n : K;
+  CORR_CUDA(cudaEventRecord(c->pre_ev[K], c->stream));
+  for (int k = 0; k < nside; ++k) CORR_CUDA(cudaStreamWaitEvent(c->pre_stream[k], c->pre_ev[K], 0));
   long long ub = 0;
   for (int k = 0; k < n; ++k) {
     const corr_rimp2_instance& x = in[order[k]];
     const Shape& s = shp[k];
     CORR_CUDA(launch_slices(x.bia, x.naux, x.nocc, x.nvir, s.Qp, scheme, fmt, s.p, sws[k],
-                            c->stream));
+                            c->pre_stream[k % nside]));
     BatchInst& b = htab[k];
     b.S = sws[k].S;
     b.eps = x.eps;
@@ -160,6 +173,10 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
     ub += s.sh.nunits;
   }
   c->launches += 2LL * n;  // row statistics and slice per instance
+  for (int k = 0; k < nside; ++k) {
+    CORR_CUDA(cudaEventRecord(c->pre_ev[k], c->pre_stream[k]));
+    CORR_CUDA(cudaStreamWaitEvent(c->stream, c->pre_ev[k], 0));
+  }
   CORR_CUDA(cudaMemcpyAsync(dtab, htab, sizeof(BatchInst) * n, cudaMemcpyHostToDevice, c->stream));
   CORR_CUDA(cudaMemcpyAsync(dorder, horder, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
   CORR_CUDA(cudaMemsetAsync(queue, 0, 8, c->stream));
