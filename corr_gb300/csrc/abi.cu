@@ -217,6 +217,8 @@ int corr_destroy(corr_context* c) {
     if (c->pre_stream[k]) cudaStreamDestroy(c->pre_stream[k]);
   for (int k = 0; k <= corr_context::kPreStreams; ++k)
     if (c->pre_ev[k]) cudaEventDestroy(c->pre_ev[k]);
+  for (auto& g : c->sweep_graph)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
   delete c;
   return CORR_OK;
 }

@@ -64,6 +64,17 @@ struct corr_context {
   static constexpr int kPreStreams = 8;
   cudaStream_t pre_stream[kPreStreams] = {};
   cudaEvent_t pre_ev[kPreStreams + 1] = {};
+  // instantiated Jacobi sweep graphs, reused while the order and the work
+  // buffers (workspace addresses) repeat; kind 0 = FP64 sweep, 1 = FP32 block sweep
+  struct SweepGraph {
+    int kind = -1;
+    int n = 0;
+    const void* ptr[5] = {};
+    cudaGraphExec_t exec = nullptr;
+  };
+  static constexpr int kSweepGraphs = 4;
+  SweepGraph sweep_graph[kSweepGraphs];
+  int sweep_graph_next = 0;
   size_t pinned_cap = 0;
 };
 
