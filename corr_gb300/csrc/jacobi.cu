@@ -97,12 +97,21 @@ __global__ void jacobi_params(const T* __restrict__ A, int n, int r, T tol, T fl
     const T app = A[(size_t)p * n + p], aqq = A[(size_t)q * n + q], apq = A[sym_at(p, q, n)];
     T c = 1, s = 0;
     const T mag = fabs(apq);
-    if (mag > tol * sqrt(fabs(app * aqq)) && mag > floor_abs) {
+    // |a_pq| > tol sqrt|a_pp a_qq| in squared form (no square root for the pairs
+    // that stay: FP64 arithmetic is a long dependent chain here)
+    if (mag * mag > (tol * tol) * fabs(app * aqq) && mag > floor_abs) {
       rot = true;
       const T tau = (aqq - app) / (T(2) * apq);
-      const T t = (tau >= T(0) ? T(1) : T(-1)) / (fabs(tau) + sqrt(T(1) + tau * tau));
-      c = T(1) / sqrt(T(1) + t * t);
-      s = t * c;
+      const T at = fabs(tau);
+      if (at > T(134217728)) {
+        // |tau| > 2^27: t = sign / (2 |tau|) to within rounding, t^2 < 2^-56, so
+        // (c, s) = (1, t) is orthogonal to working precision
+        s = (tau >= T(0) ? T(0.5) : T(-0.5)) / at;
+      } else {
+        const T t = (tau >= T(0) ? T(1) : T(-1)) / (at + sqrt(T(1) + tau * tau));
+        c = T(1) / sqrt(T(1) + t * t);
+        s = t * c;
+      }
     }
     cs[k].x = c;
     cs[k].y = s;
