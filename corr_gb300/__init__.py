@@ -156,17 +156,19 @@ class Context:
         status CORR_ERR_DEVICE_TIMEOUT; the context stays usable)."""
         check(self._L.corr_selftest_wait_timeout(self._h, int(limit_ms)))
 
-    def set_energy_policy(self, cluster):
-        """1: multicast cluster form of the energy kernel where it applies; 0: one-CTA form."""
-        check(self._L.corr_set_energy_policy(self._h, int(cluster)))
+    def set_energy_tiles(self, tiles):
+        """1 (default): a last virtual tile of at most 64 columns runs 64 wide;
+        0: every tile 128 wide."""
+        check(self._L.corr_set_energy_tiles(self._h, int(tiles)))
 
-    def set_batch_policy(self, order, stages):
-        check(self._L.corr_set_batch_policy(self._h, int(order), int(stages)))
+    def set_batch_policy(self, order, stages, tiles=1):
+        check(self._L.corr_set_batch_policy(self._h, int(order), int(stages), int(tiles)))
 
     def batch_autotune(self, items, precision="split_bf16", cache=None):
-        """Pick the batched launch variant by timing them on this batch.  With
-        a cache path, results are stored per batch signature (sorted shape
-        list) and reused without timing."""
+        """Pick the batched launch variant (unit order, pipeline stages, tile
+        shape) by timing them on this batch.  With a cache path, results are
+        stored per batch signature (sorted shape list) and reused without
+        timing.  Returns (order, stages, tiles, ms)."""
         import hashlib
         import json
         import os
@@ -182,24 +184,25 @@ class Context:
                     db = json.load(f)
             except Exception:
                 db = {}
-        if key in db:
-            order, stages = db[key]["order"], db[key]["stages"]
-            self.set_batch_policy(order, stages)
-            return order, stages, db[key]["ms"]
+        if key in db and "tiles" in db[key]:
+            e = db[key]
+            self.set_batch_policy(e["order"], e["stages"], e["tiles"])
+            return e["order"], e["stages"], e["tiles"], e["ms"]
         arr, n = self._instances(items)
-        order, stages, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        order, stages, tiles, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
         check(self._L.corr_rimp2_batch_autotune(self._h, n, arr, _prec(precision),
                                                 ctypes.byref(order), ctypes.byref(stages),
-                                                ctypes.byref(ms)))
+                                                ctypes.byref(tiles), ctypes.byref(ms)))
         if cache:
-            db[key] = {"order": order.value, "stages": stages.value, "ms": ms.value}
+            db[key] = {"order": order.value, "stages": stages.value, "tiles": tiles.value,
+                       "ms": ms.value}
             d = os.path.dirname(os.path.abspath(cache))
             os.makedirs(d, exist_ok=True)
             tmp = cache + ".tmp"
             with open(tmp, "w") as f:
                 json.dump(db, f, indent=1)
             os.replace(tmp, cache)
-        return order.value, stages.value, ms.value
+        return order.value, stages.value, tiles.value, ms.value
 
     def sync(self):
         check(self._L.corr_sync(self._h))

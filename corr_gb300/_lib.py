@@ -76,11 +76,12 @@ SIGNATURES = {
     "corr_rimp2_energy_batched": [_vp, _i, ctypes.POINTER(RIMP2Instance), _i,
                                   ctypes.POINTER(MP2Energy)],
     "corr_rimp2_energy_batched_async": [_vp, _i, ctypes.POINTER(RIMP2Instance), _i, _vp],
-    "corr_set_batch_policy": [_vp, _i, _i],
-    "corr_set_energy_policy": [_vp, _i],
+    "corr_set_batch_policy": [_vp, _i, _i, _i],
+    "corr_set_energy_tiles": [_vp, _i],
     "corr_selftest_wait_timeout": [_vp, _i],
     "corr_rimp2_batch_autotune": [_vp, _i, ctypes.POINTER(RIMP2Instance), _i, ctypes.POINTER(_i),
-                                  ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_float)],
+                                  ctypes.POINTER(_i), ctypes.POINTER(_i),
+                                  ctypes.POINTER(ctypes.c_float)],
     "corr_build_fmo": [_vp, _i, _vp, _vp, _vp],
     "corr_motrans": [_vp, _i, _i, _vp, _ll, _vp, _vp, _vp, _vp],
     "corr_motrans_ovov": [_vp, _i, _i, _vp, _ll, _vp, _vp, _vp, _vp],

@@ -260,10 +260,11 @@ int corr_sync(corr_context* c) {
   return CORR_OK;
 }
 
-int corr_set_energy_policy(corr_context* c, int cluster) {
+int corr_set_energy_tiles(corr_context* c, int tiles) {
   CORR_CHECK_ARG(c != nullptr, "null context");
-  CORR_CHECK_ARG(cluster == 0 || cluster == 1, "corr_set_energy_policy: cluster must be 0 or 1");
-  c->tc_policy = cluster;
+  CORR_CHECK_ARG(tiles == 0 || tiles == 1,
+                 "corr_set_energy_tiles: tiles must be 0 (128 wide) or 1 (narrow last tile)");
+  c->energy_tiles = tiles;
   return CORR_OK;
 }
 
@@ -378,7 +379,7 @@ static void energy_carve(Carver& w, int nocc, int nvir, int Qp, bool tc, bool x2
     sw->erow = static_cast<int*>(w.take((size_t)R * 4));
     sw->diag = static_cast<double*>(w.take((size_t)R * 8));
     sw->sc = static_cast<float*>(w.take((size_t)R * 4));
-    sw->dg = static_cast<float*>(w.take((size_t)R * 4));
+    sw->dg = static_cast<float2*>(w.take((size_t)R * 8));
     sw->eref = static_cast<int*>(w.take(16));
     sw->scale = static_cast<double*>(w.take(16));
   }
@@ -496,29 +497,19 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
   CORR_CUDA(launch_slice_planes(d_b, naux, nocc, nvir, Qp, scheme, fmt, p, sw, c->stream));
   c->launches += 1;
   if (!c->attrs_set) {
-    CORR_CUDA(prepare_energy_tc(&c->tc_clusters));
+    CORR_CUDA(prepare_energy_tc());
     c->attrs_set = true;
   }
-  // 2 x 2 multicast clusters when at least 8 fit and nocc leaves little
-  // padding (pairs outside i <= j < nocc in the diagonal blocks are idle)
-  const long long cwork = energy_tc_cluster_work(sh);
-  const bool cluster = c->tc_policy == 1 && c->tc_clusters >= 8 && nocc >= 8;
-  const int lgrid =
-      cluster ? kTcCluster * (int)std::min<long long>(c->tc_clusters, cwork) : grid;
+  const TcInst inst = make_tc_inst(sw, d_e, sh, Qp, c->energy_tiles == 1, 0);
   mark(c, 1);
-  CORR_CUDA(launch_energy_tc(sw.S, d_e, sw.sc, sw.dg, sw.scale, sh, Qp, fmt, scheme, cluster,
-                             partials, lgrid, &c->dres->status, queue, c->stream));
+  CORR_CUDA(launch_energy_tc(inst, fmt, scheme, 3, grid, partials, &c->dres->status, queue,
+                             c->stream));
   mark(c, 2);
-  int nred = 1;
-  if (cluster) {
-    CORR_CUDA(launch_energy_reduce(partials, lgrid, sw.scale, out_e, c->stream));
-  } else {
-    nred = launch_unit_reduce(partials, (int)sh.nunits, sw.scale, out_e, red_scratch,
-                              reinterpret_cast<unsigned*>(queue + 1), c->stream);
-    if (nred < 0) {
-      set_error("energy reduction launch failed");
-      return CORR_ERR_CUDA;
-    }
+  const int nred = launch_unit_reduce(partials, (int)sh.nunits, sw.scale, out_e, red_scratch,
+                                      reinterpret_cast<unsigned*>(queue + 1), c->stream);
+  if (nred < 0) {
+    set_error("energy reduction launch failed");
+    return CORR_ERR_CUDA;
   }
   c->launches += 1 + nred;  // energy, reduction
   return CORR_OK;

@@ -48,12 +48,11 @@ struct corr_context {
   float t_prepass = 0.f, t_kernel = 0.f, t_total = 0.f;
   long long launches = 0;
   bool attrs_set = false;  // one-time kernel attributes (kept out of graph capture)
-  int tc_clusters = 0;     // 4-CTA clusters of the energy kernel that fit at once
-  int tc_policy = 0;       // 0: one-CTA form (default), 1: cluster form when it applies
+  int energy_tiles = 1;    // 1: a last virtual tile of <= 64 columns runs at N = 64
   // batched driver
-  bool batch_attrs_set = false;
   int batch_order = 1;   // 0 input order, 1 cost-descending
   int batch_stages = 3;
+  int batch_tiles = 1;
   corr::Workspace batch_out;
   void* pinned = nullptr;
   // chunked upload of host inputs (created on first use)

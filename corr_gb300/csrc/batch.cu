@@ -1,14 +1,15 @@
 // Host side of the batched RI-MP2 driver: instance table, per-instance slicing,
-// unit-order policies, the synchronous/asynchronous entry points and the
-// autotuner that picks the launch variant (unit order x pipeline depth) by
-// timing them on the caller's batch.
+// unit-order policies, the synchronous/asynchronous entry points, the
+// per-instance reduction and the autotuner that picks the launch variant
+// (unit order x pipeline depth x tile shape) by timing them on the caller's
+// batch.  The kernel itself is the precision-form energy kernel of
+// energy_tc.cu in its table-driven form.
 #include <algorithm>
 #include <cstring>
 #include <numeric>
 #include <vector>
 
 #include "abi_internal.h"
-#include "batch.h"
 #include "common.cuh"
 #include "kernels.h"
 
@@ -16,11 +17,46 @@ namespace corr {
 
 namespace {
 
-struct Plan {
-  std::vector<int> order;           // table position -> caller index
-  std::vector<BatchInst> table;     // host copy (device pointers filled)
-  long long total = 0;
-};
+// Per instance k of the table: Kahan-compensated sum of its unit partials in
+// unit order, a fixed tree over the 256 threads, times the instance's energy
+// scale, into out[4 out_index[k] + {0,1,2,3}] = {E_SS, E_OS, E, E_SCS}.
+__global__ void batch_reduce_kernel(const TcInst* __restrict__ insts,
+                                    const double* __restrict__ unit_part,
+                                    const int* __restrict__ out_index, double* __restrict__ out) {
+  const TcInst b = insts[blockIdx.x];
+  __shared__ double s_os[256], s_ss[256];
+  double os = 0.0, ss = 0.0, cos_ = 0.0, css = 0.0;
+  for (long long k = threadIdx.x; k < b.nunits; k += 256) {
+    const long long u = b.unit_begin + k;
+    double y = unit_part[2 * u] - cos_;
+    double t = os + y;
+    cos_ = (t - os) - y;
+    os = t;
+    y = unit_part[2 * u + 1] - css;
+    t = ss + y;
+    css = (t - ss) - y;
+    ss = t;
+  }
+  s_os[threadIdx.x] = os;
+  s_ss[threadIdx.x] = ss;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      s_os[threadIdx.x] += s_os[threadIdx.x + w];
+      s_ss[threadIdx.x] += s_ss[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double sc = b.scale ? b.scale[0] : 1.0;
+    const double eos = s_os[0] * sc, ess = s_ss[0] * sc;
+    double* o = out + 4 * (size_t)out_index[blockIdx.x];
+    o[0] = ess;
+    o[1] = eos;
+    o[2] = ess + eos;
+    o[3] = ess / 3.0 + eos * 6.0 / 5.0;
+  }
+}
 
 double instance_cost(const corr_rimp2_instance& x) {
   return 2.0 * x.nocc * (double)x.nocc * x.nvir * (double)x.nvir * x.naux;
@@ -48,7 +84,7 @@ int grow_pinned(corr_context* c, size_t bytes) {
 
 // Enqueue one batched evaluation; energies (4 per caller instance) to `out`.
 int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int precision,
-                  double* out, int order_policy, int stages) {
+                  double* out, int order_policy, int stages, int tiles) {
   const bool tc = precision != CORR_PREC_FP64;
   // ---- plan: order and per-instance shapes
   std::vector<int> order(n);
@@ -75,7 +111,7 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
     total += s.sh.nunits;
   }
   // ---- workspace
-  auto carve = [&](Carver& w, std::vector<SliceWork>& sws, double** unit_part, BatchInst** dtab,
+  auto carve = [&](Carver& w, std::vector<SliceWork>& sws, double** unit_part, TcInst** dtab,
                    int** dorder, unsigned long long** queue) {
     sws.resize(n);
     for (int k = 0; k < n; ++k) {
@@ -86,18 +122,18 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
       sw.erow = static_cast<int*>(w.take((size_t)s.R * 4));
       sw.diag = static_cast<double*>(w.take((size_t)s.R * 8));
       sw.sc = static_cast<float*>(w.take((size_t)s.R * 4));
-      sw.dg = static_cast<float*>(w.take((size_t)s.R * 4));
+      sw.dg = static_cast<float2*>(w.take((size_t)s.R * 8));
       sw.eref = static_cast<int*>(w.take(16));
       sw.scale = static_cast<double*>(w.take(16));
     }
     *unit_part = static_cast<double*>(w.take((size_t)(tc ? total : (long long)c->sms * 2 * n) * 16));
-    *dtab = static_cast<BatchInst*>(w.take(sizeof(BatchInst) * n));
+    *dtab = static_cast<TcInst*>(w.take(sizeof(TcInst) * n));
     *dorder = static_cast<int*>(w.take(sizeof(int) * n));
     *queue = static_cast<unsigned long long*>(w.take(16));
   };
   std::vector<SliceWork> sws;
   double* unit_part;
-  BatchInst* dtab;
+  TcInst* dtab;
   int* dorder;
   unsigned long long* queue;
   carve(cv, sws, &unit_part, &dtab, &dorder, &queue);
@@ -132,11 +168,11 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
   // ---- per-instance slicing and the host copy of the table
   const int scheme = scheme_for_precision(precision);
   const int fmt = format_for_scheme(scheme);
-  const size_t hbytes = sizeof(BatchInst) * n + sizeof(int) * n + 256;
+  const size_t hbytes = sizeof(TcInst) * n + sizeof(int) * n + 256;
   CORR_TRY(grow_pinned(c, hbytes));
   char* hp = static_cast<char*>(c->pinned);
-  BatchInst* htab = reinterpret_cast<BatchInst*>(hp);
-  int* horder = reinterpret_cast<int*>(hp + ((sizeof(BatchInst) * n + 127) & ~(size_t)127));
+  TcInst* htab = reinterpret_cast<TcInst*>(hp);
+  int* horder = reinterpret_cast<int*>(hp + ((sizeof(TcInst) * n + 127) & ~(size_t)127));
   // The instances' pre-passes are independent and mostly small (a few blocks
   // each): they run on kPreStreams side streams forked from and joined back
   // into the context stream (parallel branches when the call is captured).
@@ -156,19 +192,7 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
     const Shape& s = shp[k];
     CORR_CUDA(launch_slices(x.bia, x.naux, x.nocc, x.nvir, s.Qp, scheme, fmt, s.p, sws[k],
                             c->pre_stream[k % nside]));
-    BatchInst& b = htab[k];
-    b.S = sws[k].S;
-    b.eps = x.eps;
-    b.sc = sws[k].sc;
-    b.dg = sws[k].dg;
-    b.scale = sws[k].scale;
-    b.unit_begin = ub;
-    b.nunits = s.sh.nunits;
-    b.o = x.nocc;
-    b.v = x.nvir;
-    b.ntiles = s.sh.ntiles;
-    b.ntpairs = s.sh.ntpairs;
-    b.nkb = s.Qp / kSliceQ;
+    htab[k] = make_tc_inst(sws[k], x.eps, s.sh, s.Qp, tiles == 1, ub);
     horder[k] = order[k];
     ub += s.sh.nunits;
   }
@@ -177,18 +201,17 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
     CORR_CUDA(cudaEventRecord(c->pre_ev[k], c->pre_stream[k]));
     CORR_CUDA(cudaStreamWaitEvent(c->stream, c->pre_ev[k], 0));
   }
-  CORR_CUDA(cudaMemcpyAsync(dtab, htab, sizeof(BatchInst) * n, cudaMemcpyHostToDevice, c->stream));
+  CORR_CUDA(cudaMemcpyAsync(dtab, htab, sizeof(TcInst) * n, cudaMemcpyHostToDevice, c->stream));
   CORR_CUDA(cudaMemcpyAsync(dorder, horder, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
-  CORR_CUDA(cudaMemsetAsync(queue, 0, 8, c->stream));
-  if (!c->batch_attrs_set) {
-    CORR_CUDA(prepare_energy_batch());
-    c->batch_attrs_set = true;
+  if (!c->attrs_set) {
+    CORR_CUDA(prepare_energy_tc());
+    c->attrs_set = true;
   }
   int grid = c->sms;
   if ((long long)grid > total) grid = (int)total;
   mark(c, 1);
-  CORR_CUDA(launch_energy_batch(dtab, n, total, queue, fmt, scheme, stages, grid,
-                                unit_part, &c->dres->status, c->stream));
+  CORR_CUDA(launch_energy_tc_batch(dtab, n, total, fmt, scheme, stages, grid, unit_part,
+                                   &c->dres->status, queue, c->stream));
   mark(c, 2);
   CORR_CUDA(launch_batch_reduce(dtab, n, unit_part, dorder, out, c->stream));
   c->launches += 2;
@@ -210,18 +233,27 @@ int check_batch(corr_context* c, int n, const corr_rimp2_instance* in, int preci
 }
 
 }  // namespace
+
+cudaError_t launch_batch_reduce(const TcInst* dtab, int n, const double* partials,
+                                const int* out_index, double* out, cudaStream_t s) {
+  batch_reduce_kernel<<<n, 256, 0, s>>>(dtab, partials, out_index, out);
+  return cudaGetLastError();
+}
+
 }  // namespace corr
 
 using namespace corr;
 
 extern "C" {
 
-int corr_set_batch_policy(corr_context* c, int order, int stages) {
+int corr_set_batch_policy(corr_context* c, int order, int stages, int tiles) {
   CORR_CHECK_ARG(c != nullptr, "null context");
   CORR_CHECK_ARG(order == 0 || order == 1, "order policy must be 0 (input) or 1 (cost-descending)");
   CORR_CHECK_ARG(stages == 2 || stages == 3, "stages must be 2 or 3");
+  CORR_CHECK_ARG(tiles == 0 || tiles == 1, "tiles must be 0 (128 wide) or 1 (narrow last tile)");
   c->batch_order = order;
   c->batch_stages = stages;
+  c->batch_tiles = tiles;
   return CORR_OK;
 }
 
@@ -230,7 +262,8 @@ int corr_rimp2_energy_batched_async(corr_context* c, int n, const corr_rimp2_ins
   CORR_TRY(check_batch(c, n, inst, precision));
   CORR_CHECK_ARG(is_device_ptr(energies_dev), "energies_dev must be a device pointer");
   CORR_CUDA(cudaSetDevice(c->device));
-  return batch_enqueue(c, n, inst, precision, energies_dev, c->batch_order, c->batch_stages);
+  return batch_enqueue(c, n, inst, precision, energies_dev, c->batch_order, c->batch_stages,
+                       c->batch_tiles);
 }
 
 int corr_rimp2_energy_batched(corr_context* c, int n, const corr_rimp2_instance* inst,
@@ -242,7 +275,8 @@ int corr_rimp2_energy_batched(corr_context* c, int n, const corr_rimp2_instance*
   double* dout = static_cast<double*>(c->batch_out.ptr);
   CORR_CUDA(cudaMemsetAsync(c->dres, 0, sizeof(ResultBlock), c->stream));
   mark(c, 0);
-  CORR_TRY(batch_enqueue(c, n, inst, precision, dout, c->batch_order, c->batch_stages));
+  CORR_TRY(batch_enqueue(c, n, inst, precision, dout, c->batch_order, c->batch_stages,
+                         c->batch_tiles));
   std::vector<double> h((size_t)n * 4);
   CORR_CUDA(cudaMemcpyAsync(h.data(), dout, (size_t)n * 32, cudaMemcpyDeviceToHost, c->stream));
   CORR_TRY(finish_results(c, 0));
@@ -260,7 +294,8 @@ int corr_rimp2_energy_batched(corr_context* c, int n, const corr_rimp2_instance*
 }
 
 int corr_rimp2_batch_autotune(corr_context* c, int n, const corr_rimp2_instance* inst,
-                              int precision, int* order_out, int* stages_out, float* ms_out) {
+                              int precision, int* order_out, int* stages_out, int* tiles_out,
+                              float* ms_out) {
   CORR_TRY(check_batch(c, n, inst, precision));
   CORR_CUDA(cudaSetDevice(c->device));
   CORR_TRY(c->batch_out.reserve((size_t)n * 32));
@@ -269,33 +304,49 @@ int corr_rimp2_batch_autotune(corr_context* c, int n, const corr_rimp2_instance*
   CORR_CUDA(cudaEventCreate(&e0));
   CORR_CUDA(cudaEventCreate(&e1));
   float best = 1e30f;
-  int bo = c->batch_order, bs = c->batch_stages;
-  const int orders[2] = {0, 1}, stages[2] = {3, 2};
-  for (int oi = 0; oi < 2; ++oi)
-    for (int si = 0; si < 2; ++si) {
-      // one untimed warm-up, then the median of three timed runs
-      CORR_TRY(batch_enqueue(c, n, inst, precision, dout, orders[oi], stages[si]));
-      float t[3];
-      for (int r = 0; r < 3; ++r) {
-        CORR_CUDA(cudaEventRecord(e0, c->stream));
-        CORR_TRY(batch_enqueue(c, n, inst, precision, dout, orders[oi], stages[si]));
-        CORR_CUDA(cudaEventRecord(e1, c->stream));
-        CORR_CUDA(cudaEventSynchronize(e1));
-        CORR_CUDA(cudaEventElapsedTime(&t[r], e0, e1));
+  int bo = c->batch_order, bs = c->batch_stages, bt = c->batch_tiles;
+  // the three-digit form always runs 2 stages: one stage value to try
+  const int orders[2] = {0, 1}, stages[2] = {3, 2}, tiles[2] = {1, 0};
+  const int nst = precision == CORR_PREC_SPLIT_FP16 ? 2 : 1;
+  int st = CORR_OK;
+  for (int oi = 0; oi < 2 && st == CORR_OK; ++oi)
+    for (int si = 0; si < nst && st == CORR_OK; ++si)
+      for (int ti = 0; ti < 2 && st == CORR_OK; ++ti) {
+        const int so = orders[oi], ss = nst == 2 ? stages[si] : 2, stl = tiles[ti];
+        // one untimed warm-up, then the median of three timed runs
+        st = batch_enqueue(c, n, inst, precision, dout, so, ss, stl);
+        float t[3] = {0.f, 0.f, 0.f};
+        for (int r = 0; r < 3 && st == CORR_OK; ++r) {
+          if (cudaEventRecord(e0, c->stream) != cudaSuccess) st = CORR_ERR_CUDA;
+          if (st == CORR_OK) st = batch_enqueue(c, n, inst, precision, dout, so, ss, stl);
+          if (st == CORR_OK && (cudaEventRecord(e1, c->stream) != cudaSuccess ||
+                                cudaEventSynchronize(e1) != cudaSuccess ||
+                                cudaEventElapsedTime(&t[r], e0, e1) != cudaSuccess))
+            st = CORR_ERR_CUDA;
+        }
+        if (st != CORR_OK) break;
+        std::sort(t, t + 3);
+        if (t[1] < best) {
+          best = t[1];
+          bo = so;
+          bs = ss;
+          bt = stl;
+        }
       }
-      std::sort(t, t + 3);
-      if (t[1] < best) {
-        best = t[1];
-        bo = orders[oi];
-        bs = stages[si];
-      }
-    }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (st == CORR_ERR_CUDA) {
+    set_error("batched autotune: %s", cudaGetErrorString(cudaGetLastError()));
+    return st;
+  }
+  if (st != CORR_OK) return st;
+  CORR_TRY(corr_sync(c));  // a device-side timeout in any variant
   c->batch_order = bo;
   c->batch_stages = bs;
+  c->batch_tiles = bt;
   if (order_out) *order_out = bo;
   if (stages_out) *stages_out = bs;
+  if (tiles_out) *tiles_out = bt;
   if (ms_out) *ms_out = best;
   return CORR_OK;
 }

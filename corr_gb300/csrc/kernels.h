@@ -49,7 +49,7 @@ struct SliceWork {
   int* erow;       // [R] row exponents
   double* diag;    // [R] FP64 sum_Q B^2
   float* sc;       // [R] 2^(e_r - e_ref)
-  float* dg;       // [R] diag in scaled units
+  float2* dg;      // [R] FP64 diag in scaled units as float-float (hi, lo)
   int* eref;       // [2] {e_ref, level exponent k (scheme 1)}
   double* scale;   // [2] {global energy factor 2^(4 e_ref), 1/L}
   int* x20;        // [naux][R] fixed-point values at the row scale (scheme 1), or null:
@@ -96,23 +96,44 @@ cudaError_t launch_energy_reduce(const double* partials, int n, const double* sc
                                  cudaStream_t s);
 
 // ---- fused energy kernels ---------------------------------------------------
-// tcgen05 precision form (energy_tc.cu) over the tiled digit planes S.
-// scale: the SliceWork scale pair (the kernel reads 1/L from scale[1]).
-// cluster: the 2 x 2 multicast form (grid = a multiple of kTcCluster, at most
-// kTcCluster x the max_clusters of prepare_energy_tc); else one CTA per SM
-// taking units from the device counter `queue` (8 bytes, zeroed here on the
-// stream before the launch).  partials: pairs {os, ss}, one per unit
-// (sh.nunits) in the queue form, one per CTA (grid) in the cluster form.
-constexpr int kTcCluster = 4;
-cudaError_t launch_energy_tc(const uint16_t* S, const double* eps, const float* sc,
-                             const float* dg, const double* scale, const EnergyShape& sh, int Qp,
-                             int fmt, int scheme, bool cluster, double* partials, int grid,
-                             int* status, unsigned long long* queue, cudaStream_t s);
-// One-time attributes (dynamic smem size) and the number of 4-CTA clusters
-// that fit at once (0: no cluster form).
-cudaError_t prepare_energy_tc(int* max_clusters);
-long long energy_tc_cluster_work(const EnergyShape& sh);  // super-units of the cluster form
+// One RI-MP2 instance as the tcgen05 precision-form kernel (energy_tc.cu) reads
+// it: its digit planes and row factors (SliceWork), orbital energies, shape,
+// and its first unit in the launch's global unit numbering.  The batch form
+// holds an array of these in device memory.
 constexpr int kTcTile = 128;
+struct TcInst {
+  const uint16_t* S;     // digit planes in the tiled layout
+  const double* eps;     // [o+v]
+  const float* sc;       // [o*v] row factors 2^(e_r - e_ref)
+  const float2* dg;      // [o*v] FP64 diagonal (ia|ia) in scaled units (float-float)
+  const double* scale;   // [2] {energy factor 2^(4 e_ref), 1/L of the digits}
+  long long unit_begin;  // first global unit of this instance
+  long long nunits;
+  int o, v, ntiles, ntpairs, nkb;
+  int narrow;            // 1: the last virtual tile (<= 64 columns) runs at N = 64
+};
+// narrow: the caller's tile policy; it takes effect only when nvir % 128 is
+// in 1..64.
+TcInst make_tc_inst(const SliceWork& sw, const double* eps, const EnergyShape& sh, int Qp,
+                    bool narrow, long long unit_begin);
+// Shared-memory attributes of every kernel variant (once per device, outside
+// stream capture).
+cudaError_t prepare_energy_tc();
+// One instance: units 0 .. nunits-1 from the device counter `queue` (16
+// bytes, zeroed here on the stream before the launch; the second word is the
+// ticket of launch_unit_reduce).  partials: {os, ss} per unit.  stages: 2 or
+// 3 (scheme 1; scheme 0 always runs 2).
+cudaError_t launch_energy_tc(const TcInst& inst, int fmt, int scheme, int stages, int grid,
+                             double* partials, int* status, unsigned long long* queue,
+                             cudaStream_t s);
+// A batch: dtab[n] in device memory with consecutive unit ranges (total units).
+cudaError_t launch_energy_tc_batch(const TcInst* dtab, int n, long long total, int fmt,
+                                   int scheme, int stages, int grid, double* partials,
+                                   int* status, unsigned long long* queue, cudaStream_t s);
+// Per instance k of the table: the fixed-order sum of its unit partials times
+// its energy scale, into out[4 out_index[k] + {0,1,2,3}] = {E_SS, E_OS, E, E_SCS}.
+cudaError_t launch_batch_reduce(const TcInst* dtab, int n, const double* partials,
+                                const int* out_index, double* out, cudaStream_t s);
 
 // FP64 form on the FP64 tensor path (energy_fp64.cu).
 cudaError_t launch_energy_fp64(const double* bia, const double* eps, const EnergyShape& sh,

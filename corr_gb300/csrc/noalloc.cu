@@ -14,11 +14,12 @@
 // device with cudaGetSymbolAddress, with that device current, on the entry
 // point's first call on the device (which also sets the energy kernel's
 // shared-memory attribute there); make that first call before any stream
-// capture on the device.  All calls share the one array, which keeps the
-// previous call's contents: every value a call reads is written or cleared by
-// the same call first.  Calls whose GPU work overlaps (different streams or
-// threads on one device) race on the array and must be serialised by the
-// caller.
+// capture on the device.  Every call is synchronous: it waits for its stream
+// to finish the work before it returns the energies.  All calls share the one
+// array, which keeps the previous call's contents: every value a call reads is
+// written or cleared by the same call first.  Calls whose GPU work overlaps
+// (different streams or threads on one device) race on the array and must be
+// serialised by the caller.
 #include <algorithm>
 #include <cmath>
 #include <mutex>
@@ -59,8 +60,7 @@ int setup_device(int device, DeviceScratch* out) {
     }
     int sms = 0;
     CORR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    int clusters = 0;  // the allocation-free entry point runs the one-CTA form
-    CORR_CUDA(prepare_energy_tc(&clusters));
+    CORR_CUDA(prepare_energy_tc());
     d.sms = sms;
     d.ptr = p;
   }
@@ -98,6 +98,8 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
                  "corr_rimp2_energy_noalloc: sizes must be positive");
   CORR_CHECK_ARG(precision >= CORR_PREC_FP64 && precision <= CORR_PREC_SPLIT_BF16,
                  "corr_rimp2_energy_noalloc: unknown precision %d", precision);
+  CORR_CHECK_ARG((long long)nocc * nvir <= (1ll << 31) && nocc <= 46000,
+                 "corr_rimp2_energy_noalloc: nocc*nvir too large");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
     cudaGetLastError();
@@ -125,15 +127,15 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
   auto carve = [&](Carver& w, Header** hdr, double** partials, unsigned long long** queue,
                    double** red_scratch, SliceWork* sw) {
     *hdr = static_cast<Header*>(w.take(256));
-    *partials = static_cast<double*>(
-        w.take((size_t)std::max<long long>(kMaxGrid, sh.nunits) * 16));  // per CTA or per unit
+    // the FP64 form writes one partial per CTA, the precision forms one per unit
+    *partials = static_cast<double*>(w.take((size_t)(tc ? sh.nunits : kMaxGrid) * 16));
     *queue = static_cast<unsigned long long*>(w.take(16));
     *red_scratch = static_cast<double*>(w.take((size_t)kReduceBlocks * 16));
     if (tc) {
       sw->erow = static_cast<int*>(w.take((size_t)R * 4));
       sw->diag = static_cast<double*>(w.take((size_t)R * 8));
       sw->sc = static_cast<float*>(w.take((size_t)R * 4));
-      sw->dg = static_cast<float*>(w.take((size_t)R * 4));
+      sw->dg = static_cast<float2*>(w.take((size_t)R * 8));
       sw->eref = static_cast<int*>(w.take(16));
       sw->scale = static_cast<double*>(w.take(16));
       sw->S = static_cast<uint16_t*>(w.take(slice_bytes(nocc, nvir, Qp)));
@@ -166,8 +168,8 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
     const int fmt = format_for_scheme(scheme);
     const int p = slice_bits_for(Qp);
     CORR_CUDA(launch_slices(bia, naux, nocc, nvir, Qp, scheme, fmt, p, sw, s));
-    CORR_CUDA(launch_energy_tc(sw.S, eps, sw.sc, sw.dg, sw.scale, sh, Qp, fmt, scheme, false,
-                               partials, grid, &hdr->status, queue, s));
+    const TcInst inst = make_tc_inst(sw, eps, sh, Qp, true, 0);
+    CORR_CUDA(launch_energy_tc(inst, fmt, scheme, 3, grid, partials, &hdr->status, queue, s));
     if (launch_unit_reduce(partials, (int)sh.nunits, sw.scale, hdr->e, red_scratch,
                            reinterpret_cast<unsigned*>(queue + 1), s) < 0) {
       set_error("corr_rimp2_energy_noalloc: energy reduction launch failed");

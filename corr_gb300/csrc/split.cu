@@ -555,7 +555,7 @@ __global__ void __launch_bounds__(256) slice_kernel(const double* __restrict__ b
                                                     uint16_t* __restrict__ S,
                                                     const double* __restrict__ diag,
                                                     float* __restrict__ sc,
-                                                    float* __restrict__ dg, double* scale_out) {
+                                                    float2* __restrict__ dg, double* scale_out) {
   const int* kglob = eref + 1;
   __shared__ __align__(16) double tile[64][65];
   int(*tilei)[65] = reinterpret_cast<int(*)[65]>(&tile[0][0]);  // X20IN: X20 values
@@ -598,7 +598,9 @@ __global__ void __launch_bounds__(256) slice_kernel(const double* __restrict__ b
     if (er < -4000) er = 0;  // every row zero
     if (real) {
       sc[r] = live ? (float)ldexp(1.0, e - er) : 0.0f;
-      dg[r] = (float)ldexp(diag[r], -2 * er);
+      const double d = ldexp(diag[r], -2 * er);
+      const float dh = (float)d;
+      dg[r] = make_float2(dh, (float)(d - (double)dh));
     }
     if (lin == 0 && t == 0) {
       scale_out[0] = ldexp(1.0, 4 * er);

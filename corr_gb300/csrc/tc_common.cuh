@@ -1,5 +1,5 @@
-// tcgen05 epilogue helpers shared by the precision-form energy kernels
-// (energy_tc.cu: one instance; energy_batch.cu: batched instances).
+// tcgen05 epilogue helpers of the precision-form energy kernel (energy_tc.cu)
+// and of its adjoint (adjoint_tc.cu).
 #pragma once
 
 #include "common.cuh"
@@ -36,6 +36,15 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
       : "r"(taddr));
 #pragma unroll
   for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+// After tcgen05.wait::ld: an empty asm that "modifies" each destination
+// register, ordered after the wait (both are volatile), so no arithmetic on
+// the loaded values can be scheduled before the load has completed.
+template <int N>
+__device__ __forceinline__ void ld_ready(float* v) {
+#pragma unroll
+  for (int k = 0; k < N; ++k) asm volatile("" : "+f"(v[k]));
 }
 
 __device__ __forceinline__ void tc_wait_st() {
@@ -83,6 +92,9 @@ __device__ __forceinline__ void load_level_sum(uint32_t tb, int c, float inv_l, 
   tmem_ld32(tb + 128u + (uint32_t)c, a1);
   tmem_ld32(tb + 256u + (uint32_t)c, a2);
   tc_wait_ld();
+  ld_ready<32>(a0);
+  ld_ready<32>(a1);
+  ld_ready<32>(a2);
 #pragma unroll
   for (int k = 0; k < 32; ++k) {
     const float t = fmaf(a2[k], inv_l2, fmaf(a1[k], inv_l, a0[k]));
@@ -99,11 +111,103 @@ __device__ __forceinline__ void load_level_sum16(uint32_t tb, int c, float inv_l
   tmem_ld16(tb + 128u + (uint32_t)c, a1);
   tmem_ld16(tb + 256u + (uint32_t)c, a2);
   tc_wait_ld();
+  ld_ready<16>(a0);
+  ld_ready<16>(a1);
+  ld_ready<16>(a2);
 #pragma unroll
   for (int k = 0; k < 16; ++k) {
     const float t = fmaf(a2[k], inv_l2, fmaf(a1[k], inv_l, a0[k]));
     d[k] = t * (sca * scb[c + k]);
   }
+}
+
+// ---- energy arithmetic with FP32 instructions only ----------------------
+// GB300 runs FP64 at about 1/64 of its FP32 rate, so the per-element energy
+// arithmetic uses float-float values (hi + lo, about 48 significand bits)
+// built from error-free transformations: Knuth's TwoSum, the FMA residual of
+// a product (x*x - RN(x*x) is exact as fmaf(x, x, -RN(x*x))), one
+// Newton-Raphson step for the reciprocal, and a float-float running sum.
+
+// s + e == a + b exactly (Knuth's TwoSum; no ordering of |a|, |b| needed).
+__device__ __forceinline__ void two_sum(float a, float b, float* s, float* e) {
+  const float t = a + b;
+  const float bb = t - a;
+  *e = (a - (t - bb)) + (b - bb);
+  *s = t;
+}
+
+// An FP64 value as a float-float pair (hi = RN(d), lo = RN(d - hi)).
+__device__ __forceinline__ float2 ff_split(double d) {
+  const float hi = (float)d;
+  return make_float2(hi, (float)(d - (double)hi));
+}
+
+// 1/(da + db) for float-float da, db as rh + rl: D = dh + dl by TwoSum of the
+// high parts, r0 = rcp.approx(dh) (relative error below 2^-22), the residual
+// e = 1 - D r0 by two FMAs, and 1/D = r0 / (1 - e) ~ r0 + r0 e (one
+// Newton-Raphson step): relative error about e^2 + 2^-46, i.e. ~2^-44.
+__device__ __forceinline__ void recip_ff(float2 da, float2 db, float* rh, float* rl) {
+  float dh, dl;
+  two_sum(da.x, db.x, &dh, &dl);
+  dl += da.y + db.y;
+  float r0;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(dh));
+  float e = fmaf(-dh, r0, 1.0f);
+  e = fmaf(-dl, r0, e);
+  *rh = r0;
+  *rl = r0 * e;
+}
+
+// Running sum of float-float terms: h + l, with h updated by TwoSum (exact)
+// and l collecting the TwoSum errors and the terms' low parts in FP32.
+// flush() adds h + l to the FP64 total d and restarts: over m terms the FP32
+// roundings of l stay below m^2 2^-48 of the sum, so callers flush every 32
+// terms (a compensated sum in the sense of Kahan's, but carried to
+// float-float accuracy: plain Kahan summation in FP32 only reaches ~2^-23).
+struct FFSum {
+  float h = 0.0f, l = 0.0f;
+  double d = 0.0;
+  __device__ __forceinline__ void add(float hi, float lo) {
+    float t, e;
+    two_sum(h, hi, &t, &e);
+    h = t;
+    l += e + lo;
+  }
+  __device__ __forceinline__ void flush() {
+    d += (double)h + (double)l;
+    h = 0.0f;
+    l = 0.0f;
+  }
+};
+
+// Terms of one element (a, b) of a pair i != j with x = (ia|jb), y = (ib|ja)
+// (scaled FP32 values) and 1/D = rh + rl:
+//   E_OS += (x^2 + y^2)/D,  E_SS += (x - y)^2/D,
+// the squares and the difference error-free, the products with 1/D to
+// float-float accuracy.
+__device__ __forceinline__ void pair_terms(float x, float y, float rh, float rl, FFSum& os,
+                                           FFSum& ss) {
+  const float px = x * x, ex = fmaf(x, x, -px);
+  const float py = y * y, ey = fmaf(y, y, -py);
+  float nh, nl;
+  two_sum(px, py, &nh, &nl);
+  nl += ex + ey;
+  float dh, dl;
+  two_sum(x, -y, &dh, &dl);
+  const float mh = dh * dh;
+  const float ml = fmaf(dh, dh, -mh) + 2.0f * dh * dl;
+  const float th = nh * rh;
+  os.add(th, fmaf(nh, rh, -th) + fmaf(nh, rl, nl * rh));
+  const float uh = mh * rh;
+  ss.add(uh, fmaf(mh, rh, -uh) + fmaf(mh, rl, ml * rh));
+}
+
+// The term of one element of a pair i == j (D2 == D1 == x): E_OS += 2 x^2/D.
+__device__ __forceinline__ void same_pair_term(float x, float rh, float rl, FFSum& os) {
+  const float px = x * x, ex = fmaf(x, x, -px);
+  const float th = px * rh;
+  const float tl = fmaf(px, rh, -th) + fmaf(px, rl, ex * rh);
+  os.add(2.0f * th, 2.0f * tl);
 }
 
 // The MMAs of one K=16 step: r[l], q[l] are the row/column descriptors of

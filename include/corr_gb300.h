@@ -174,23 +174,25 @@ int corr_rimp2_energy_batched_async(corr_context* ctx, int n, const corr_rimp2_i
  * the context remains usable. */
 int corr_selftest_wait_timeout(corr_context* ctx, int limit_ms);
 
-/* Form of the tcgen05 energy kernel used by corr_rimp2_energy(_async) and
- * corr_rimp2_energy_from_3index (no counterpart in the reference): 0 (the
- * default) = one CTA per work stream; 1 = 2x2 clusters that multicast shared
- * operand tiles, used when nocc >= 8 and at least 8 clusters fit on the
- * device (half the L2 traffic, but slower on GB300 at the measured sizes).
- * Both give the same energies up to FP64 summation order. */
-int corr_set_energy_policy(corr_context* ctx, int cluster);
+/* Tile shape of the tcgen05 energy kernel used by corr_rimp2_energy(_async),
+ * corr_rimp2_energy_estimate and corr_rimp2_energy_from_3index (no
+ * counterpart in the reference): 1 (the default) = when nvir % 128 is in
+ * 1..64, the units whose column tile is the last virtual tile run 64 columns
+ * wide (half the tensor-core work of a padded 128-wide tile); 0 = every tile
+ * 128 wide.  Both give the same energies up to FP64 summation order. */
+int corr_set_energy_tiles(corr_context* ctx, int tiles);
 
 /* Launch variant of the batched kernel: unit order (0 = input order,
- * 1 = costliest instance first) and shared-memory pipeline depth in stages of
- * one 64-wide Q block (2 or 3; the three-digit form always runs 2). */
-int corr_set_batch_policy(corr_context* ctx, int order, int stages);
+ * 1 = costliest instance first), shared-memory pipeline depth in stages of
+ * one 64-wide Q block (2 or 3; the three-digit form always runs 2) and tile
+ * shape (tiles as in corr_set_energy_tiles, per instance). */
+int corr_set_batch_policy(corr_context* ctx, int order, int stages, int tiles);
 
-/* Time every launch variant on this batch (median of three runs after a
- * warm-up), keep the fastest in the context and report it. */
+/* Time every launch variant on this batch (order x stages x tiles; median of
+ * three runs after a warm-up), keep the fastest in the context and report it
+ * (any output pointer may be NULL). */
 int corr_rimp2_batch_autotune(corr_context* ctx, int n, const corr_rimp2_instance* inst,
-                              int precision, int* order, int* stages, float* ms);
+                              int precision, int* order, int* stages, int* tiles, float* ms);
 
 /* RI-MP2 adjoint (no counterpart in the reference, which has no gradients):
  * dbia[(Q*nocc+i)*nvir+a] = dE/dB^Q_ia and deps[p] = dE/d eps_p for

@@ -42,19 +42,28 @@ def test_batched_policies_agree_and_autotune(ctx, tmp_path):
     sizes = O.synth_batch_sizes(24, 55)
     sizes = [(o, v, X) for (o, v, X) in sizes if o <= 25]  # keep the test quick
     items = _gpu_instances(sizes, 8)
+    assert any(0 < v % 128 <= 64 for (_, v, _) in sizes)  # the tile-shape choice matters
     for prec in ("split_fp16", "split_bf16"):
-        base = None
-        for order in (0, 1):
-            for stages in (2, 3):
-                ctx.set_batch_policy(order, stages)
-                got = [g.e_total for g in ctx.rimp2_energy_batched(items, prec)]
-                if base is None:
-                    base = got
-                assert got == base  # per-unit partials are reduced in a fixed order
+        for tiles in (1, 0):
+            base = None
+            for order in (0, 1):
+                for stages in (2, 3):
+                    ctx.set_batch_policy(order, stages, tiles)
+                    got = [g.e_total for g in ctx.rimp2_energy_batched(items, prec)]
+                    if base is None:
+                        base = got
+                    assert got == base  # per-unit partials are reduced in a fixed order
+            if tiles == 1:
+                narrow = base
+        # narrow last tiles only drop padded zero terms
+        for a, b in zip(narrow, base):
+            assert abs(a - b) <= 1e-13 * abs(b), (prec, a, b)
+    ctx.set_batch_policy(1, 3, 1)
     cache = str(tmp_path / "autotune.json")
-    o1, s1, ms1 = ctx.batch_autotune(items, "split_fp16", cache=cache)
-    o2, s2, ms2 = ctx.batch_autotune(items, "split_fp16", cache=cache)  # from the cache
-    assert (o1, s1) == (o2, s2) and ms1 == ms2 and ms1 > 0
+    o1, s1, t1, ms1 = ctx.batch_autotune(items, "split_fp16", cache=cache)
+    o2, s2, t2, ms2 = ctx.batch_autotune(items, "split_fp16", cache=cache)  # from the cache
+    assert (o1, s1, t1) == (o2, s2, t2) and ms1 == ms2 and ms1 > 0
+    assert t1 in (0, 1) and s1 in (2, 3)
 
 
 def test_batched_graph_capture(ctx):

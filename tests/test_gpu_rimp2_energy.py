@@ -135,24 +135,56 @@ def test_split_wide_dynamic_range(ctx, prec):
     assert abs(got.e_os - ref[1]) <= 2e-7 * abs(ref[1]), (prec, got, ref)
 
 
-@pytest.mark.parametrize("o,v,X", [(8, 130, 70), (9, 257, 100), (13, 360, 300), (40, 360, 1200)])
+@pytest.mark.parametrize("o,v,X", [(3, 64, 40), (5, 150, 70), (7, 300, 90), (4, 192, 50),
+                                   (9, 257, 100)])
 @pytest.mark.parametrize("prec", ["split_fp16", "split_bf16"])
-def test_cluster_form_matches_one_cta_form(ctx, o, v, X, prec):
-    """The 2x2 multicast cluster form (odd nocc leaves idle members in the
-    last block) against the one-CTA form: same digit products, different
-    FP64 summation order."""
-    B, eps = O.synth_rimp2(o, v, X, 31 + o)
-    one = ctx.rimp2_energy(B, eps, o, v, X, prec)
-    ctx.set_energy_policy(1)
+def test_narrow_last_tile_matches_full_tiles(ctx, o, v, X, prec):
+    """nvir % 128 in 1..64: the units of the last virtual tile run 64 columns
+    wide (tiles = 1, the default) or padded to 128 (tiles = 0).  The digit
+    products are the same; only padded zero terms differ.  (257 leaves one
+    column in the last tile.)"""
+    B, eps = O.synth_rimp2(o, v, X, 61 + v)
+    narrow = ctx.rimp2_energy(B, eps, o, v, X, prec)
+    ctx.set_energy_tiles(0)
     try:
-        clu = ctx.rimp2_energy(B, eps, o, v, X, prec)
+        full = ctx.rimp2_energy(B, eps, o, v, X, prec)
     finally:
-        ctx.set_energy_policy(0)
-    for a, b in zip(clu.as_tuple(), one.as_tuple()):
-        assert abs(a - b) <= 1e-9 * abs(one.e_total), (prec, clu, one)
-    if o * v * X <= 13 * 360 * 300:
-        ref = O.rimp2_energy(B, eps, o, v)
-        assert abs(clu.e_total - ref[2]) <= 2e-7 * abs(ref[2]), (prec, clu, ref)
+        ctx.set_energy_tiles(1)
+    for a, b in zip(narrow.as_tuple(), full.as_tuple()):
+        assert abs(a - b) <= 1e-13 * abs(full.e_total), (prec, narrow, full)
+    ref = O.rimp2_energy(B, eps, o, v)
+    assert abs(narrow.e_total - ref[2]) <= 2e-7 * abs(ref[2]), (prec, narrow, ref)
+
+
+def _exact_digit_inputs(o, v, X, seed):
+    """B whose rows are small integers times 2^-10 (|k| <= 20, one element of
+    each row at +-20): every row scaled by its power of two is an integer of at
+    most 11 bits, so both precision forms represent B exactly in their leading
+    digit and every tensor-core sum, hence every (ia|jb) value the epilogue
+    receives, is exact in FP32."""
+    r = O.rng(seed)
+    k = r.integers(-20, 21, size=(X, o, v)).astype(np.float64)
+    k[0] = np.where(r.uniform(size=(o, v)) < 0.5, -20.0, 20.0)
+    B = np.ascontiguousarray(k * 2.0 ** -10)
+    eps = np.concatenate([np.sort(r.uniform(-1.5, -0.3, o)), np.sort(r.uniform(0.05, 3.0, v))])
+    return B, eps
+
+
+@pytest.mark.parametrize("o,v,X,seed", [(1, 1, 1, 71), (3, 5, 7, 72), (6, 129, 70, 73),
+                                        (4, 257, 40, 74), (8, 300, 256, 75), (12, 200, 600, 76)])
+@pytest.mark.parametrize("prec", ["split_fp16", "split_bf16"])
+def test_epilogue_accuracy_on_exact_digits(ctx, o, v, X, seed, prec):
+    """The energy arithmetic of the precision forms in isolation: on inputs
+    whose digit representation is exact, every (ia|jb) reaches the epilogue
+    without error, so the difference from the FP64 energy of the same B is the
+    epilogue's own (denominators from FP64 orbital energies, 1/D, squares,
+    products and the compensated per-unit sums).  Bound: 1e-12 relative."""
+    B, eps = _exact_digit_inputs(o, v, X, seed)
+    ref = O.rimp2_energy(B, eps, o, v)
+    got = ctx.rimp2_energy(B, eps, o, v, X, prec)
+    rel = [abs(g - r) / abs(ref[2]) for g, r in zip(got.as_tuple(), ref)]
+    print(f"{prec} o={o} v={v} X={X}: relative deviation E_SS/E_OS/E {rel}")
+    assert max(rel) <= 1e-12, (prec, got, ref, rel)
 
 
 @pytest.mark.parametrize("prec", ["split_fp16", "split_bf16"])
