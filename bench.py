@@ -210,25 +210,26 @@ def read_peak():
 
 # ---------------------------------------------------------------------------
 def run_reference(args):
+    """The reference's RI-MP2 energy (can_mp2.cc:53-132) on the host cores:
+    one full evaluation of the workload per step (all nocc^2 pair GEMMs)."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     from corr_gb300 import workloads as W
 
     B, eps = W.synth_rimp2(NOCC, NVIR, NAUX, SEED)
-    nocc_s = 6  # 36 of the 1600 pair GEMMs per step
-    for _ in range(args.warmup):
-        cpu_sample(B, eps, nocc_s, min_seconds=0.0, max_reps=1)
+    fn, kind = cpu_energy_fn()
+    for _ in range(max(1, min(args.warmup, 2))):
+        fn(B, eps, NOCC, NVIR)
     times = []
-    kind = "port"
     for _ in range(args.steps):
-        tf, kind, dt, reps = cpu_sample(B, eps, nocc_s, min_seconds=0.0, max_reps=1)
-        times.append(dt)
-    f_step = 2.0 * nocc_s * nocc_s * NVIR * NVIR * NAUX
+        t0 = time.perf_counter()
+        fn(B, eps, NOCC, NVIR)
+        times.append(time.perf_counter() - t0)
     tot = sum(times)
-    value = f_step * len(times) / tot / 1e12
-    sample = (f"nocc={nocc_s} of {NOCC} occupied orbitals ({nocc_s * nocc_s} of {NOCC * NOCC} "
-              f"pair GEMMs), nvir={NVIR}, naux={NAUX}, one pass per step")
+    value = FLOPS * len(times) / tot / 1e12
+    sample = (f"the full workload every step: all {NOCC * NOCC} pair GEMMs of nocc={NOCC}, "
+              f"nvir={NVIR}, naux={NAUX}")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -242,6 +243,44 @@ def run_reference(args):
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+C3_SIZES = (480, 100, 1520)  # nbf, nocc, naux of the 20-water cluster (def2-SVP / def2-SVP-RI)
+
+
+def time_to_ecorr_c3(ctx, reps=3):
+    """RI-MP2 time-to-E_corr from the 3-index integrals at the water-cluster
+    sizes (nbf=480, nocc=100, naux=1520): (P|ia) transform, RI metric,
+    B = J^-1/2 (P|ia) and the energy in one call of the host API
+    (corr_rimp2_energy_from_3index), each precision form against the FP64
+    form of the same call.  Inputs: seeded synthetic stand-ins of the
+    integrals, MO coefficients and orbital energies resident on the GPU."""
+    import torch
+
+    from corr_gb300 import workloads as W
+
+    N, o, X = C3_SIZES
+    mos, eps, J, P = W.synth_ri_pipeline(N, o, X, 303)
+    out = {"workload": f"nbf={N} nocc={o} naux={X}: seeded synthetic J, (P|mn), C, eps on the "
+                       "GPU (seed 303), the water-cluster sizes"}
+    e = {}
+    for prec in ("split_fp16", "split_bf16", "fp64"):
+        ctx.rimp2_energy_from_3index(2 * o, mos, eps, J, P, prec)  # warm (sizes the workspace)
+        ts = []
+        for _ in range(reps if prec != "fp64" else 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r, ncut = ctx.rimp2_energy_from_3index(2 * o, mos, eps, J, P, prec)
+            ts.append((time.perf_counter() - t0) * 1e3)
+        e[prec] = r.e_total
+        out[f"{prec}_ms"] = statistics.median(ts)
+    for prec in ("split_fp16", "split_bf16"):
+        out[f"{prec}_speedup_vs_fp64"] = out["fp64_ms"] / out[f"{prec}_ms"]
+        out[f"{prec}_abs_dE_vs_fp64"] = abs(e[prec] - e["fp64"])
+        out[f"{prec}_rel_dE_vs_fp64"] = abs(e[prec] - e["fp64"]) / abs(e["fp64"])
+    out["e_fp64"] = e["fp64"]
+    out["metric_path"] = "cholesky" if ncut == 0 else f"jacobi, {ncut} cut"
+    return out
 
 
 def run_ours(args):
@@ -361,6 +400,9 @@ def run_ours(args):
         f64_ms.append(t0.elapsed_time(t1))
     f64 = statistics.median(f64_ms)
 
+    # ---- the metric's time-to-E_corr leg at the water-cluster sizes
+    c3 = time_to_ecorr_c3(ctx)
+
     # ---- end to end through the public API with host buffers
     Bh = torch.from_numpy(B).pin_memory()
     eh = torch.from_numpy(eps).pin_memory()
@@ -403,6 +445,7 @@ def run_ours(args):
                    "l2": "FP64 input 138 MB > L2 (129 MB); 256 MB L2 flush between timed "
                          "steps, outside the timed region"},
         "time_to_ecorr_ms": ms_step,
+        "time_to_ecorr_c3": c3,
         "graph_energy_matches": e_graph[2] == e_split.e_total,
         "energy": {"split": [e_split.e_ss, e_split.e_os, e_split.e_total],
                    "fp64": [e64.e_ss, e64.e_os, e64.e_total],
@@ -461,7 +504,7 @@ def run_batch(args):
         flops += 2.0 * o * o * v * v * X
     ctx = corr_gb300.Context(0, stream=stream)
     prec = args.precision if args.precision != "fp64" else "split_fp16"
-    order, stages, tune_ms = ctx.batch_autotune(items, prec)
+    order, stages, tiles, tune_ms = ctx.batch_autotune(items, prec)
     out = torch.zeros(4 * len(items), dtype=torch.float64, device="cuda")
     ctx.rimp2_energy_batched_async(items, prec, out)
     ctx.sync()
@@ -526,6 +569,7 @@ def run_batch(args):
         "config": {"workload": f"{len(items)} instances, nocc~U{{5..60}}, nvir=nocc*U{{4..8}}, "
                                "naux=round(3.5 nvir), seed 5005/5006",
                    "precision": prec, "policy": {"order": order, "stages": stages,
+                                                 "tiles": "narrow last tile" if tiles else "128",
                                                  "autotune_ms": tune_ms},
                    "b_bytes": int(sum(B.numel() * 8 for B, _, _, _ in items))},
         "tflops_algorithmic": flops / (ms * 1e-3) / 1e12,
