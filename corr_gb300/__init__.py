@@ -10,10 +10,10 @@ from __future__ import annotations
 
 import ctypes
 
-from ._lib import PRECISION, CorrError, MP2Energy, RIMP2Instance, Timing, check, load
+from ._lib import PRECISION, CorrError, MP2Energy, RIMP2Instance, SystemInfo, Timing, check, load
 
 __all__ = ["Context", "CorrError", "MP2Energy", "PRECISION", "default_context",
-           "run_canonical_mp2_ri"]
+           "read_system", "run_canonical_mp2_ri", "write_wav_hf"]
 
 
 def _ptr(x):
@@ -312,6 +312,58 @@ class Context:
                                                     ctypes.byref(out), ctypes.byref(ncut)))
         return out, ncut.value
 
+    # -- hand-off files (src/IO/ops_io.cc) -----------------------------------
+    # Output arrays may be numpy arrays or torch tensors (CUDA tensors are
+    # filled through pinned chunk buffers on the context stream).
+    def _filled(self, like, shape, dtype, out):
+        if out is not None:
+            return out
+        import numpy as np
+
+        if like == "cuda":
+            import torch
+
+            return torch.empty(shape, dtype={np.float64: torch.float64, np.int64: torch.int64,
+                                             np.uint16: torch.int16}[dtype],
+                               device=f"cuda:{self.device}")
+        return np.empty(shape, dtype=dtype)
+
+    def read_oei(self, prefix, nroao, device="cpu"):
+        """read_oei (ops_io.cc:112): (H, T, S, V) of PREFIX.oei."""
+        import numpy as np
+
+        mats = [self._filled(device, (nroao, nroao), np.float64, None) for _ in range(4)]
+        check(self._L.corr_read_oei(self._h, prefix.encode(), int(nroao), *[_ptr(m) for m in mats]))
+        return tuple(mats)
+
+    def read_tei(self, prefix, nrofint, device="cpu"):
+        """read_tei (ops_io.cc:203): (sortcount[4], intval, intnums[nrofint][4])."""
+        import numpy as np
+
+        sc = np.zeros(4, dtype=np.int64)
+        iv = self._filled(device, (int(nrofint),), np.float64, None)
+        inum = self._filled(device, (int(nrofint), 4), np.uint16, None)
+        check(self._L.corr_read_tei(self._h, prefix.encode(), int(nrofint), _ptr(sc), _ptr(iv),
+                                    _ptr(inum)))
+        return sc, iv, inum
+
+    def read_wav_hf(self, prefix, nroao, device="cpu"):
+        """read_wav_HF (ops_io.cc:283): (MO energies, MO coefficients [p][mu])."""
+        import numpy as np
+
+        e = self._filled(device, (nroao,), np.float64, None)
+        c = self._filled(device, (nroao, nroao), np.float64, None)
+        check(self._L.corr_read_wav_hf(self._h, prefix.encode(), int(nroao), _ptr(e), _ptr(c)))
+        return e, c
+
+    def read_rimp2(self, prefix, naux, nroao, device="cpu"):
+        """BPQ[naux][nroao][nroao] of PREFIX.rimp2 (read by read_transform_ri, ri.cc:109)."""
+        import numpy as np
+
+        b = self._filled(device, (naux, nroao, nroao), np.float64, None)
+        check(self._L.corr_read_rimp2(self._h, prefix.encode(), int(naux), int(nroao), _ptr(b)))
+        return b
+
     # -- dense FP64 helpers (src/MATH/ops_mat.cc) ----------------------------
     def dgemm(self, A, B, transa=False, transb=False, alpha=1.0, beta=0.0, out=None):
         """C = alpha op(A) op(B) + beta C for row-major 2-D arrays (mat_mat_T:
@@ -337,6 +389,42 @@ class Context:
         vecs = self._out(A, (n, n), vecs)
         check(self._L.corr_syev(self._h, n, _ptr(A), _ptr(w), _ptr(vecs)))
         return w, vecs
+
+
+def read_system(prefix):
+    """read_system (ops_io.cc:63): (SystemInfo, coord[nroa][3], charges, zeff,
+    mass) of PREFIX.sys.  Host arrays; needs no GPU."""
+    import numpy as np
+
+    L = load()
+    info = SystemInfo()
+    check(L.corr_read_system(prefix.encode(), ctypes.byref(info), None, None, None, None))
+    na = info.nroa
+    coord = np.empty((na, 3))
+    charges, zeff, mass = np.empty(na), np.empty(na), np.empty(na)
+    check(L.corr_read_system(prefix.encode(), ctypes.byref(info), _ptr(coord), _ptr(charges),
+                             _ptr(zeff), _ptr(mass)))
+    return info, coord, charges, zeff, mass
+
+
+def write_wav_hf(path, moens, mos):
+    """write_wav_HF (ops_io.cc:259) of host arrays."""
+    check(load().corr_write_wav_hf(path.encode(), int(moens.shape[0]), _ptr(moens), _ptr(mos)))
+
+
+def read_files_host(prefix, nroao, nrofint):
+    """The packed ERIs and one-electron matrices of PREFIX.tei/.oei into host
+    arrays without a context or GPU (the readers' host path)."""
+    import numpy as np
+
+    L = load()
+    mats = [np.empty((nroao, nroao)) for _ in range(4)]
+    check(L.corr_read_oei(None, prefix.encode(), int(nroao), *[_ptr(m) for m in mats]))
+    sc = np.zeros(4, dtype=np.int64)
+    iv = np.empty(int(nrofint))
+    inum = np.empty((int(nrofint), 4), dtype=np.uint16)
+    check(L.corr_read_tei(None, prefix.encode(), int(nrofint), _ptr(sc), _ptr(iv), _ptr(inum)))
+    return tuple(mats), (sc, iv, inum)
 
 
 _DEFAULT = None

@@ -18,7 +18,7 @@ CORR_OK = 0
 STATUS = {
     0: "CORR_OK", 1: "CORR_ERR_BAD_ARG", 2: "CORR_ERR_OOM", 3: "CORR_ERR_NOT_PD",
     4: "CORR_ERR_DEVICE_TIMEOUT", 5: "CORR_ERR_CUDA", 6: "CORR_ERR_NO_DEVICE",
-    7: "CORR_ERR_NUMERIC",
+    7: "CORR_ERR_NUMERIC", 8: "CORR_ERR_IO",
 }
 PRECISION = {"fp64": 0, "split_fp16": 1, "split_bf16": 2}
 
@@ -44,6 +44,14 @@ class MP2Energy(ctypes.Structure):
 class Timing(ctypes.Structure):
     _fields_ = [("prepass_ms", ctypes.c_float), ("kernel_ms", ctypes.c_float),
                 ("total_ms", ctypes.c_float), ("launches_total", ctypes.c_longlong)]
+
+
+class SystemInfo(ctypes.Structure):
+    _fields_ = [("nroe", ctypes.c_int), ("nroa", ctypes.c_int), ("nroao", ctypes.c_int),
+                ("naux_1", ctypes.c_int), ("naux_2", ctypes.c_int),
+                ("nrofint", ctypes.c_longlong), ("nrofaux", ctypes.c_longlong),
+                ("nrofaux2", ctypes.c_longlong), ("basis_ob", ctypes.c_char * 33),
+                ("basis_jk", ctypes.c_char * 33), ("basis_ri", ctypes.c_char * 33)]
 
 
 class RIMP2Instance(ctypes.Structure):
@@ -96,6 +104,12 @@ SIGNATURES = {
                                       ctypes.POINTER(MP2Energy), ctypes.POINTER(_i)],
     "corr_dgemm": [_vp, _i, _i, _i, _i, _i, _d, _vp, _i, _vp, _i, _d, _vp, _i],
     "corr_syev": [_vp, _i, _vp, _vp, _vp],
+    "corr_read_system": [ctypes.c_char_p, ctypes.POINTER(SystemInfo), _vp, _vp, _vp, _vp],
+    "corr_read_oei": [_vp, ctypes.c_char_p, _i, _vp, _vp, _vp, _vp],
+    "corr_read_tei": [_vp, ctypes.c_char_p, _ll, _vp, _vp, _vp],
+    "corr_read_wav_hf": [_vp, ctypes.c_char_p, _i, _vp, _vp],
+    "corr_write_wav_hf": [ctypes.c_char_p, _i, _vp, _vp],
+    "corr_read_rimp2": [_vp, ctypes.c_char_p, _i, _i, _vp],
 }
 _RESTYPES = {"corr_version": ctypes.c_char_p, "corr_last_error": ctypes.c_char_p}
 

@@ -206,6 +206,10 @@ int corr_destroy(corr_context* c) {
   if (c->ws.ptr) cudaFree(c->ws.ptr);
   if (c->batch_out.ptr) cudaFree(c->batch_out.ptr);
   if (c->pinned) cudaFreeHost(c->pinned);
+  for (int k = 0; k < 2; ++k) {
+    if (c->io_pinned[k]) cudaFreeHost(c->io_pinned[k]);
+    if (c->io_ev[k]) cudaEventDestroy(c->io_ev[k]);
+  }
   if (c->dres) cudaFree(c->dres);
   if (c->hres) cudaFreeHost(c->hres);
   for (int k = 0; k < 4; ++k)

@@ -75,6 +75,9 @@ struct corr_context {
   SweepGraph sweep_graph[kSweepGraphs];
   int sweep_graph_next = 0;
   size_t pinned_cap = 0;
+  // pinned chunk buffers of the file readers (io.cu), created on first use
+  void* io_pinned[2] = {nullptr, nullptr};
+  cudaEvent_t io_ev[2] = {nullptr, nullptr};
 };
 
 namespace corr {

@@ -229,3 +229,61 @@ void trans_mat(int np, double* mat, double* trans, double* tmpmat, int dir) {
 void pmv(double* mat, double* vi, double* vo, int nroao) {
   check(corr_dgemm(ctx(), 0, 0, nroao, 1, nroao, 1.0, mat, nroao, vi, 1, 0.0, vo, 1), "pmv");
 }
+
+// ---- hand-off files (src/IO/ops_io.cc) --------------------------------------
+
+void write_wav_HF(std::string wavfile, int nroao, double* MOens, double* MOs) {
+  check(corr_write_wav_hf(wavfile.c_str(), nroao, MOens, MOs), "write_wav_HF");
+}
+
+#ifdef CORR_SHIM_USE_REFERENCE_HEADERS
+void read_system(systeminfo* sysinfo) {
+  corr_system_info info;
+  check(corr_read_system(sysinfo->prefix.c_str(), &info, nullptr, nullptr, nullptr, nullptr),
+        "read_system");
+  const int na = info.nroa;
+  sysinfo->nroe = info.nroe;
+  sysinfo->nroa = na;
+  sysinfo->nroao = info.nroao;
+  sysinfo->naux_1 = info.naux_1;
+  sysinfo->naux_2 = info.naux_2;
+  sysinfo->nrofint = info.nrofint;
+  sysinfo->nrofaux = info.nrofaux;
+  sysinfo->nrofaux2 = info.nrofaux2;
+  sysinfo->coord = new double[3 * na];
+  sysinfo->charges = new double[na];
+  sysinfo->zeff = new double[na];
+  sysinfo->mass = new double[na];
+  check(corr_read_system(sysinfo->prefix.c_str(), &info, sysinfo->coord, sysinfo->charges,
+                         sysinfo->zeff, sysinfo->mass),
+        "read_system");
+  sysinfo->basisNameOB = info.basis_ob;
+  sysinfo->basisNameJK = info.basis_jk;
+  sysinfo->basisNameRI = info.basis_ri;
+  sysinfo->atoms.resize(na);
+  for (int i = 0; i < na; ++i) {
+    sysinfo->atoms[i].atomic_number = sysinfo->charges[i];
+    sysinfo->atoms[i].x = sysinfo->coord[3 * i + 0];
+    sysinfo->atoms[i].y = sysinfo->coord[3 * i + 1];
+    sysinfo->atoms[i].z = sysinfo->coord[3 * i + 2];
+  }
+}
+
+void read_oei(systeminfo* sysinfo, OEints* onemats) {
+  check(corr_read_oei(nullptr, sysinfo->prefix.c_str(), sysinfo->nroao, onemats->Hmat,
+                      onemats->Tmat, onemats->Smat, onemats->Vmat),
+        "read_oei");
+}
+
+void read_tei(systeminfo* sysinfo, TEints* twomats) {
+  check(corr_read_tei(nullptr, sysinfo->prefix.c_str(), sysinfo->nrofint, twomats->sortcount,
+                      twomats->intval, twomats->intnums),
+        "read_tei");
+}
+
+void read_wav_HF(systeminfo* sysinfo, OEints* onemats) {
+  check(corr_read_wav_hf(nullptr, sysinfo->prefix.c_str(), sysinfo->nroao, onemats->MOens,
+                         onemats->MOs),
+        "read_wav_HF");
+}
+#endif

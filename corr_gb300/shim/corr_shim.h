@@ -76,6 +76,17 @@ void calculate_ri_from_integrals(int naux, int nroao, const double* J, const dou
 void read_transform_ri(std::string prefix, int nroe, int nroao, int naux_2, double* MOs,
                        double* Bia);
 
+// src/IO/ops_io.h:33 -- writes nroao, MOens, MOs to `wavfile` (host arrays).
+void write_wav_HF(std::string wavfile, int nroao, double* MOens, double* MOs);
+#ifdef CORR_SHIM_USE_REFERENCE_HEADERS
+// The readers need systeminfo::prefix, a member the standalone layout above
+// does not declare: they exist in the build against the reference's util.h.
+void read_system(systeminfo* sysinfo);                   // ops_io.h:37, allocates as the reference
+void read_oei(systeminfo* sysinfo, OEints* onemats);      // ops_io.h:38, caller-allocated arrays
+void read_tei(systeminfo* sysinfo, TEints* twomats);      // ops_io.h:39, caller-allocated arrays
+void read_wav_HF(systeminfo* sysinfo, OEints* onemats);   // ops_io.h:34, caller-allocated arrays
+#endif
+
 // Dense FP64 helpers of src/MATH/ops_mat.h, row-major np x np, on the GPU.
 void diag_mat(int nroao, double* mat, double* vals, double* vecs);          // ops_mat.h:3
 void symmortho_mat(int nroao, double* mat, double* tmat, double* dummat);   // ops_mat.h:4

@@ -42,7 +42,9 @@ def synth_batch_sizes(count, seed):
 def synth_ri_pipeline(nbf, nocc, naux, seed, device="cuda"):
     """(mos[p][mu], eps, J[P][Q], Pmn[P][mu][nu]) as float64 torch tensors on
     `device`.  J = L L^T / naux + 0.5 I (condition number ~10), (P|mn)
-    symmetric in m, n with a decaying auxiliary spectrum, mos orthonormal."""
+    symmetric in m, n with a decaying auxiliary spectrum, mos orthonormal.
+    The (P|mn) amplitude 0.0035 exp(-P/600) puts the RI-MP2 energy at the
+    water-cluster sizes near -4 Eh, the magnitude of the molecule's."""
     import torch
 
     g = torch.Generator(device=device)
@@ -50,7 +52,7 @@ def synth_ri_pipeline(nbf, nocc, naux, seed, device="cuda"):
     f64 = torch.float64
     L = torch.randn((naux, naux), generator=g, device=device, dtype=f64)
     J = L @ L.T / naux + 0.5 * torch.eye(naux, device=device, dtype=f64)
-    s = 0.1 * torch.exp(-torch.arange(naux, device=device, dtype=f64) / 600.0)
+    s = 0.0035 * torch.exp(-torch.arange(naux, device=device, dtype=f64) / 600.0)
     P = torch.randn((naux, nbf, nbf), generator=g, device=device, dtype=f64) * s[:, None, None]
     P = 0.5 * (P + P.transpose(1, 2))
     # orthonormalised on the host: torch's lazily loaded GPU linear-algebra

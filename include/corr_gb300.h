@@ -39,7 +39,8 @@ enum corr_status {
   CORR_ERR_DEVICE_TIMEOUT = 4, /* a bounded device-side wait gave up           */
   CORR_ERR_CUDA = 5,           /* any other CUDA runtime error                 */
   CORR_ERR_NO_DEVICE = 6,      /* no usable sm_103 GPU                          */
-  CORR_ERR_NUMERIC = 7         /* non-finite input or zero energy denominator  */
+  CORR_ERR_NUMERIC = 7,        /* non-finite input or zero energy denominator  */
+  CORR_ERR_IO = 8              /* a file is missing, short or not writable     */
 };
 
 /* Arithmetic of the RI-MP2 contraction (ia|jb) = sum_Q B^Q_ia B^Q_jb. */
@@ -325,6 +326,50 @@ int corr_dgemm(corr_context* ctx, int transa, int transb, int m, int n, int k, d
  * output read row-major).  Cyclic Jacobi in FP64 on the GPU; each eigenvector's
  * sign is arbitrary, as LAPACK's.  A is not modified.  n <= 32768. */
 int corr_syev(corr_context* ctx, int n, const double* A, double* w, double* vecs);
+
+/* ---- on-disk hand-off files (src/IO/ops_io.cc) --------------------------- */
+
+/* System description of PREFIX.sys. */
+typedef struct corr_system_info {
+  int nroe, nroa, nroao, naux_1, naux_2;
+  long long nrofint, nrofaux, nrofaux2;
+  char basis_ob[33], basis_jk[33], basis_ri[33];
+} corr_system_info;
+
+/* Replaces read_system (src/IO/ops_io.cc:63-109, declared at src/IO/ops_io.h:37):
+ * the sizes of PREFIX.sys into *info; with coord[3 nroa], charges, zeff and
+ * mass[nroa] (host arrays, all four or none) also the atoms and the three
+ * 32-byte basis-name fields.  Call once with NULL arrays to learn nroa. */
+int corr_read_system(const char* prefix, corr_system_info* info, double* coord, double* charges,
+                     double* zeff, double* mass);
+
+/* Replaces read_oei (ops_io.cc:112-121, ops_io.h:38): H, T, S, V (nroao^2
+ * each) from PREFIX.oei.  The files readers below take host or device arrays
+ * (device arrays of ctx's GPU stream through pinned chunks; ctx may be NULL
+ * when every array is host memory) and return CORR_ERR_IO for a missing or
+ * short file. */
+int corr_read_oei(corr_context* ctx, const char* prefix, int nroao, double* hmat, double* tmat,
+                  double* smat, double* vmat);
+
+/* Replaces read_tei (ops_io.cc:203-212, ops_io.h:39): the packed AO ERIs of
+ * PREFIX.tei (sortcount[4], intval[nrofint], intnums[4 nrofint]), the input
+ * of corr_motrans. */
+int corr_read_tei(corr_context* ctx, const char* prefix, long long nrofint, long long* sortcount,
+                  double* intval, unsigned short* intnums);
+
+/* Replaces read_wav_HF (ops_io.cc:283-299, ops_io.h:34): MO energies and
+ * coefficients from PREFIX.ahfw; CORR_ERR_BAD_ARG when the file holds another
+ * orbital count (the reference exits there). */
+int corr_read_wav_hf(corr_context* ctx, const char* prefix, int nroao, double* moens,
+                     double* mos);
+
+/* Replaces write_wav_HF (ops_io.cc:259-267, ops_io.h:33): writes the file
+ * `path` (host arrays). */
+int corr_write_wav_hf(const char* path, int nroao, const double* moens, const double* mos);
+
+/* BPQ[naux][nroao][nroao] from PREFIX.rimp2, the file read_transform_ri reads
+ * (src/POSTHF/ri.cc:109-119). */
+int corr_read_rimp2(corr_context* ctx, const char* prefix, int naux, int nroao, double* bpq);
 
 #ifdef __cplusplus
 }

@@ -9,7 +9,9 @@ import os
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("CORR_REFERENCE_DIR", "/root/reference")
+# the reference checkout: CORR_REFERENCE_DIR, else a sibling of the repository
+REF = os.environ.get("CORR_REFERENCE_DIR",
+                     os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 L = {"S": 0, "P": 1, "D": 2, "F": 3, "G": 4}
 
 

@@ -12,10 +12,12 @@
 #include <cstdlib>
 #include <cstring>
 #include <iostream>
+#include <cstdio>
 #include <sstream>
 #include <string>
 #include <vector>
 
+#include "IO/ops_io.h"
 #include "MATH/ops_mat.h"
 #include "POSTHF/can_mp2.h"
 #include "POSTHF/motrans.h"
@@ -314,6 +316,78 @@ void ref_rhf(int nroe, int nroao, double ion_rep, const double* S, const double*
   std::memcpy(moens_out, oe.MOens, sizeof(double) * nroao);
   out_e[0] = grab(text, "HF-Results", "TOTAL E:");
   delete[] oe.Hmat;  // allocate_onemats hands out one block starting at Hmat
+}
+
+// src/IO/ops_io.cc:63 read_system.  ints = {nroe, nroa, nroao, naux_1,
+// naux_2}, lls = {nrofint, nrofaux, nrofaux2}; atoms (caller-sized by a first
+// call with coord == NULL) and the three basis names, each into 33 bytes.
+void ref_read_system(const char* prefix, int* ints, long long* lls, double* coord,
+                     double* charges, double* zeff, double* mass, char* names) {
+  systeminfo si;
+  si.prefix = prefix;
+  read_system(&si);
+  ints[0] = si.nroe;
+  ints[1] = si.nroa;
+  ints[2] = si.nroao;
+  ints[3] = si.naux_1;
+  ints[4] = si.naux_2;
+  lls[0] = si.nrofint;
+  lls[1] = si.nrofaux;
+  lls[2] = si.nrofaux2;
+  if (coord) {
+    std::memcpy(coord, si.coord, sizeof(double) * 3 * si.nroa);
+    std::memcpy(charges, si.charges, sizeof(double) * si.nroa);
+    std::memcpy(zeff, si.zeff, sizeof(double) * si.nroa);
+    std::memcpy(mass, si.mass, sizeof(double) * si.nroa);
+    std::snprintf(names, 33, "%s", si.basisNameOB.c_str());
+    std::snprintf(names + 33, 33, "%s", si.basisNameJK.c_str());
+    std::snprintf(names + 66, 33, "%s", si.basisNameRI.c_str());
+  }
+  delete[] si.coord;
+  delete[] si.charges;
+  delete[] si.zeff;
+  delete[] si.mass;
+}
+
+// src/IO/ops_io.cc:112 read_oei into the caller's four nroao^2 arrays.
+void ref_read_oei(const char* prefix, int nroao, double* H, double* T, double* S, double* V) {
+  systeminfo si;
+  si.prefix = prefix;
+  si.nroao = nroao;
+  OEints oe;
+  oe.Hmat = H;
+  oe.Tmat = T;
+  oe.Smat = S;
+  oe.Vmat = V;
+  read_oei(&si, &oe);
+}
+
+// src/IO/ops_io.cc:203 read_tei into caller arrays.
+void ref_read_tei(const char* prefix, long long nrofint, long long* sortcount, double* intval,
+                  unsigned short* intnums) {
+  systeminfo si;
+  si.prefix = prefix;
+  si.nrofint = nrofint;
+  TEints te;
+  te.intval = intval;
+  te.intnums = intnums;
+  read_tei(&si, &te);
+  for (int k = 0; k < 4; ++k) sortcount[k] = te.sortcount[k];
+}
+
+// src/IO/ops_io.cc:283 read_wav_HF and :259 write_wav_HF.
+void ref_read_wav_hf(const char* prefix, int nroao, double* moens, double* mos) {
+  systeminfo si;
+  si.prefix = prefix;
+  si.nroao = nroao;
+  OEints oe;
+  oe.MOens = moens;
+  oe.MOs = mos;
+  read_wav_HF(&si, &oe);
+}
+
+void ref_write_wav_hf(const char* path, int nroao, double* moens, double* mos) {
+  write_wav_HF(std::string(path), nroao, moens, mos);
 }
 
 }  // extern "C"

@@ -17,7 +17,9 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("CORR_REFERENCE_DIR", "/root/reference")
+# the reference checkout: CORR_REFERENCE_DIR, else a sibling of the repository
+REF = os.environ.get("CORR_REFERENCE_DIR",
+                     os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 SO = os.path.join(HERE, "_ref", "libcorr_ref.so")
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -208,3 +210,49 @@ def pmv(mat, vi):
     vo = np.zeros(m.shape[0])
     getattr(lib(), "_Z3pmvPdS_S_i")(_p(m), _p(v), _p(vo), m.shape[0])
     return vo
+
+
+# ---- hand-off files (src/IO/ops_io.cc) ------------------------------------
+def read_system(prefix):
+    """The reference's read_system: (ints[5], lls[3], coord, charges, zeff,
+    mass, [three basis names])."""
+    L = lib()
+    ints = np.zeros(5, dtype=np.int32)
+    lls = np.zeros(3, dtype=np.int64)
+    names = ctypes.create_string_buffer(99)
+    L.ref_read_system(prefix.encode(), ints.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                      _p(lls, _i64p), None, None, None, None, names)
+    na = int(ints[1])
+    coord, charges, zeff, mass = np.empty(3 * na), np.empty(na), np.empty(na), np.empty(na)
+    L.ref_read_system(prefix.encode(), ints.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                      _p(lls, _i64p), _p(coord), _p(charges), _p(zeff), _p(mass), names)
+    raw = names.raw
+    nm = [raw[33 * k:33 * k + 33].split(b"\0")[0].decode() for k in range(3)]
+    return ints, lls, coord.reshape(na, 3), charges, zeff, mass, nm
+
+
+def read_oei(prefix, nroao):
+    mats = [np.empty((nroao, nroao)) for _ in range(4)]
+    lib().ref_read_oei(prefix.encode(), int(nroao), *[_p(m) for m in mats])
+    return tuple(mats)
+
+
+def read_tei(prefix, nrofint):
+    sc = np.zeros(4, dtype=np.int64)
+    iv = np.empty(int(nrofint))
+    inum = np.empty((int(nrofint), 4), dtype=np.uint16)
+    lib().ref_read_tei(prefix.encode(), ctypes.c_longlong(int(nrofint)), _p(sc, _i64p), _p(iv),
+                       _p(inum, _u16p))
+    return sc, iv, inum
+
+
+def read_wav_hf(prefix, nroao):
+    e = np.empty(nroao)
+    c = np.empty((nroao, nroao))
+    lib().ref_read_wav_hf(prefix.encode(), int(nroao), _p(e), _p(c))
+    return e, c
+
+
+def write_wav_hf(path, moens, mos):
+    lib().ref_write_wav_hf(path.encode(), int(moens.shape[0]), _p(np.ascontiguousarray(moens)),
+                           _p(np.ascontiguousarray(mos)))
