@@ -312,6 +312,24 @@ class Context:
                                                     ctypes.byref(out), ctypes.byref(ncut)))
         return out, ncut.value
 
+    # -- CCSD consumer of the MO integrals (src/POSTHF/ccsd.cc) --------------
+    def ints_so(self, prec, out=None):
+        """calc_ints_so (ccsd.cc:509): <ij||kl> over 2N spin orbitals from the
+        spatial MO integrals prec[N][N][N][N] (corr_motrans layout)."""
+        N = prec.shape[0]
+        out = self._out(prec, (2 * N,) * 4, out)
+        check(self._L.corr_ints_so(self._h, N, _ptr(prec), _ptr(out)))
+        return out
+
+    def cc_fock(self, nroe, mos, hmat, prec):
+        """form_fock (ccsd.cc:11): spin-orbital (h, f), each 2N x 2N."""
+        N = mos.shape[0]
+        h = self._out(prec, (2 * N, 2 * N), None)
+        f = self._out(prec, (2 * N, 2 * N), None)
+        check(self._L.corr_cc_fock(self._h, int(nroe), N, _ptr(mos), _ptr(hmat), _ptr(prec),
+                                   _ptr(h), _ptr(f)))
+        return h, f
+
     # -- hand-off files (src/IO/ops_io.cc) -----------------------------------
     # Output arrays may be numpy arrays or torch tensors (CUDA tensors are
     # filled through pinned chunk buffers on the context stream).

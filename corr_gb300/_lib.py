@@ -104,6 +104,8 @@ SIGNATURES = {
                                       ctypes.POINTER(MP2Energy), ctypes.POINTER(_i)],
     "corr_dgemm": [_vp, _i, _i, _i, _i, _i, _d, _vp, _i, _vp, _i, _d, _vp, _i],
     "corr_syev": [_vp, _i, _vp, _vp, _vp],
+    "corr_ints_so": [_vp, _i, _vp, _vp],
+    "corr_cc_fock": [_vp, _i, _i, _vp, _vp, _vp, _vp, _vp],
     "corr_read_system": [ctypes.c_char_p, ctypes.POINTER(SystemInfo), _vp, _vp, _vp, _vp],
     "corr_read_oei": [_vp, ctypes.c_char_p, _i, _vp, _vp, _vp, _vp],
     "corr_read_tei": [_vp, ctypes.c_char_p, _ll, _vp, _vp, _vp],

@@ -327,6 +327,22 @@ int corr_dgemm(corr_context* ctx, int transa, int transb, int m, int n, int k, d
  * sign is arbitrary, as LAPACK's.  A is not modified.  n <= 32768. */
 int corr_syev(corr_context* ctx, int n, const double* A, double* w, double* vecs);
 
+/* ---- CCSD consumer of the MO integrals (src/POSTHF/ccsd.cc) -------------- */
+
+/* Replaces calc_ints_so (src/POSTHF/ccsd.cc:509-535, with get_integral,
+ * ccsd.cc:6-9): the antisymmetrized spin-orbital integrals
+ * ints_so[((i*M + j)*M + k)*M + l] = <ij||kl>, M = 2 nroao spin orbitals
+ * (spin p % 2, spatial orbital p / 2), from prec (corr_motrans layout; keep it
+ * on the device to skip the N^4 host round trip).  16 nroao^4 doubles out. */
+int corr_ints_so(corr_context* ctx, int nroao, const double* prec, double* ints_so);
+
+/* Replaces form_fock (ccsd.cc:11-48): the spin-orbital core Hamiltonian
+ * h_so[p*M + q] = (C H C^T)_{p/2,q/2} [same spin] and Fock matrix
+ * f_so = h_so + sum_{j < nroe} <pj||qj>, from mos[p*N + mu], hmat[N*N] and
+ * prec; M = 2 nroao. */
+int corr_cc_fock(corr_context* ctx, int nroe, int nroao, const double* mos, const double* hmat,
+                 const double* prec, double* h_so, double* f_so);
+
 /* ---- on-disk hand-off files (src/IO/ops_io.cc) --------------------------- */
 
 /* System description of PREFIX.sys. */

@@ -373,3 +373,41 @@ def read_transform_ri(path, nroe, nroao, naux, mos):
     `path` (prefix + ".rimp2"), then the transform_ri contractions."""
     bpq = np.fromfile(path, dtype=np.float64, count=naux * nroao * nroao)
     return transform_ri(nroe, mos, bpq.reshape(naux, nroao, nroao))
+
+
+# ---- CCSD consumer of the MO integrals (src/POSTHF/ccsd.cc) --------------------
+def ints_so(prec):
+    """Restates calc_ints_so (ccsd.cc:509-535) with get_integral (ccsd.cc:6-9):
+    so[i,j,k,l] = (i/2 k/2 | j/2 l/2)[s_i=s_k][s_j=s_l]
+                - (i/2 l/2 | j/2 k/2)[s_i=s_l][s_j=s_k],  s_p = p % 2."""
+    prec = np.asarray(prec)
+    N = prec.shape[0]
+    T = prec.transpose(0, 2, 1, 3)  # T[a,b,c,d] = (a c | b d)
+    A = T
+    B = T.transpose(0, 1, 3, 2)     # B[a,b,c,d] = (a d | b c)
+    for ax in range(4):
+        A = A.repeat(2, axis=ax)
+        B = B.repeat(2, axis=ax)
+    s = np.arange(2 * N) % 2
+    si, sj, sk, sl = (s[:, None, None, None], s[None, :, None, None], s[None, None, :, None],
+                      s[None, None, None, :])
+    return A * ((si == sk) & (sj == sl)) - B * ((si == sl) & (sj == sk))
+
+
+def cc_fock(nroe, mos, hmat, prec):
+    """Restates form_fock (ccsd.cc:11-48): h = spin-blocked C H C^T,
+    f_pq = h_pq + sum_{j < nroe} <pj||qj>.  Returns (h, f)."""
+    mos, hmat, prec = (np.asarray(x) for x in (mos, hmat, prec))
+    N = mos.shape[0]
+    M = 2 * N
+    s = np.arange(M) % 2
+    hs = mos @ hmat @ mos.T
+    h = hs[np.ix_(np.arange(M) // 2, np.arange(M) // 2)] * (s[:, None] == s[None, :])
+    p = np.arange(M)
+    twoe = np.zeros((M, M))
+    for j in range(nroe):
+        a = prec[p[:, None] // 2, p[None, :] // 2, j // 2, j // 2] * (s[:, None] == s[None, :])
+        b = prec[p[:, None] // 2, j // 2, j // 2, p[None, :] // 2] * (
+            (s[:, None] == s[j]) & (s[j] == s[None, :]))
+        twoe += a - b
+    return h, h + twoe

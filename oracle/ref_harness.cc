@@ -20,6 +20,7 @@
 #include "IO/ops_io.h"
 #include "MATH/ops_mat.h"
 #include "POSTHF/can_mp2.h"
+#include "POSTHF/ccsd.h"
 #include "POSTHF/motrans.h"
 #include "POSTHF/ri.h"
 #include "SCF/ops_rhf.h"
@@ -103,6 +104,10 @@ double grab(const std::string& text, const char* block, const char* key) {
 std::string g_last_output;
 
 }  // namespace
+
+// defined with external linkage in src/POSTHF/ccsd.cc (:509, :11), not declared in ccsd.h
+void calc_ints_so(cc_helper* CC, pHF* postHF);
+void form_fock(cc_helper* CC, pHF* postHF);
 
 extern "C" {
 
@@ -316,6 +321,43 @@ void ref_rhf(int nroe, int nroao, double ion_rep, const double* S, const double*
   std::memcpy(moens_out, oe.MOens, sizeof(double) * nroao);
   out_e[0] = grab(text, "HF-Results", "TOTAL E:");
   delete[] oe.Hmat;  // allocate_onemats hands out one block starting at Hmat
+}
+
+// src/POSTHF/ccsd.cc:509 calc_ints_so: ints_so[norb^4] (norb = 2 nroao) from
+// the spatial MO integrals prec_ints[N^4].
+void ref_ints_so(int nroe, int nroao, const double* prec, double* out) {
+  cc_helper cc;
+  cc.nocc = nroe;
+  cc.nroao = nroao;
+  cc.norb = 2 * nroao;
+  cc.nvir = cc.norb - nroe;
+  pHF ph;
+  ph.prec_ints = const_cast<double*>(prec);
+  calc_ints_so(&cc, &ph);
+  const size_t n = (size_t)cc.norb * cc.norb * cc.norb * cc.norb;
+  std::memcpy(out, ph.ints_so, sizeof(double) * n);
+  delete[] ph.ints_so;
+}
+
+// src/POSTHF/ccsd.cc:11 form_fock: spin-orbital h and f (norb x norb) from the
+// MO coefficients, the AO core Hamiltonian and prec_ints.
+void ref_form_fock(int nroe, int nroao, const double* mos, const double* hmat, const double* prec,
+                   double* h_out, double* f_out) {
+  cc_helper cc;
+  cc.nocc = nroe;
+  cc.nroao = nroao;
+  cc.norb = 2 * nroao;
+  cc.nvir = cc.norb - nroe;
+  cc.MOs = const_cast<double*>(mos);
+  cc.Hmat = const_cast<double*>(hmat);
+  pHF ph;
+  ph.prec_ints = const_cast<double*>(prec);
+  form_fock(&cc, &ph);
+  const size_t n = (size_t)cc.norb * cc.norb;
+  std::memcpy(h_out, cc.h, sizeof(double) * n);
+  std::memcpy(f_out, cc.f, sizeof(double) * n);
+  delete[] cc.h;
+  delete[] cc.f;
 }
 
 // src/IO/ops_io.cc:63 read_system.  ints = {nroe, nroa, nroao, naux_1,

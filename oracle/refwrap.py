@@ -256,3 +256,20 @@ def read_wav_hf(prefix, nroao):
 def write_wav_hf(path, moens, mos):
     lib().ref_write_wav_hf(path.encode(), int(moens.shape[0]), _p(np.ascontiguousarray(moens)),
                            _p(np.ascontiguousarray(mos)))
+
+
+# ---- CCSD consumer (src/POSTHF/ccsd.cc) -------------------------------------
+def ints_so(nroe, prec):
+    N = prec.shape[0]
+    out = np.empty((2 * N,) * 4)
+    lib().ref_ints_so(int(nroe), int(N), _p(np.ascontiguousarray(prec)), _p(out))
+    return out
+
+
+def cc_fock(nroe, mos, hmat, prec):
+    N = mos.shape[0]
+    h, f = np.empty((2 * N, 2 * N)), np.empty((2 * N, 2 * N))
+    lib().ref_form_fock(int(nroe), int(N), _p(np.ascontiguousarray(mos)),
+                        _p(np.ascontiguousarray(hmat)), _p(np.ascontiguousarray(prec)), _p(h),
+                        _p(f))
+    return h, f

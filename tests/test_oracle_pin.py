@@ -239,3 +239,24 @@ def test_read_transform_ri_restatement_vs_golden(tmp_path):
     bpq.tofile(tmp_path / "case.rimp2")
     got = O.read_transform_ri(str(tmp_path / "case.rimp2"), 2 * nocc, N, naux, mos)
     assert np.allclose(got, g["read_transform_ri_bia"], rtol=0, atol=1e-14)
+
+
+def test_ccsd_spin_orbital_restatements_vs_reference():
+    """oracle.ints_so / oracle.cc_fock against the reference's calc_ints_so and
+    form_fock (src/POSTHF/ccsd.cc:509, :11) on synthetic MO integrals."""
+    from oracle import refwrap
+
+    if not refwrap.available():
+        pytest.skip("reference oracle not available")
+    N, nroe = 7, 6
+    eri, _ = O.synth_eri(N, 81)
+    mos = O.synth_orbitals(N, 82)
+    prec = O.motrans(mos, O.pack_eri(eri))
+    ref = refwrap.ints_so(nroe, prec)
+    assert np.array_equal(O.ints_so(prec), ref)
+    H = O.rng(83).standard_normal((N, N))
+    H = H + H.T
+    rh, rf = refwrap.cc_fock(nroe, mos, H, prec)
+    h, f = O.cc_fock(nroe, mos, H, prec)
+    assert np.abs(h - rh).max() <= 1e-13 * np.abs(rh).max()
+    assert np.abs(f - rf).max() <= 1e-13 * np.abs(rf).max()
