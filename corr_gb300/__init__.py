@@ -10,9 +10,10 @@ from __future__ import annotations
 
 import ctypes
 
-from ._lib import PRECISION, CorrError, MP2Energy, RIMP2Instance, SystemInfo, Timing, check, load
+from ._lib import (PRECISION, BasisC, CorrError, MP2Energy, RIMP2Instance, SystemInfo, Timing,
+                   check, load)
 
-__all__ = ["Context", "CorrError", "MP2Energy", "PRECISION", "default_context",
+__all__ = ["Basis", "Context", "CorrError", "MP2Energy", "PRECISION", "default_context",
            "read_system", "run_canonical_mp2_ri", "write_wav_hf"]
 
 
@@ -37,6 +38,28 @@ def _prec(p):
             raise ValueError(f"unknown precision {p!r}; choose from {sorted(PRECISION)}")
         return PRECISION[p]
     return int(p)
+
+
+class Basis:
+    """Contracted Gaussian shells (corr_basis): l[s], nprim[s], poff[s],
+    center[s][3] (bohr), exps and coefs of normalised primitives as in a
+    basis-set file.  Functions: real solid harmonics m = -l..l per shell."""
+
+    def __init__(self, l, nprim, poff, center, exps, coefs):
+        import numpy as np
+
+        self.l = np.ascontiguousarray(l, dtype=np.int32)
+        self.nprim = np.ascontiguousarray(nprim, dtype=np.int32)
+        self.poff = np.ascontiguousarray(poff, dtype=np.int32)
+        self.center = np.ascontiguousarray(center, dtype=np.float64).reshape(-1)
+        self.exps = np.ascontiguousarray(exps, dtype=np.float64)
+        self.coefs = np.ascontiguousarray(coefs, dtype=np.float64)
+        self.nbf = int(sum(2 * int(x) + 1 for x in self.l))
+
+    def c(self):
+        return BasisC(len(self.l), self.l.ctypes.data, self.nprim.ctypes.data,
+                      self.poff.ctypes.data, self.center.ctypes.data, self.exps.ctypes.data,
+                      self.coefs.ctypes.data)
 
 
 class Context:
@@ -312,6 +335,20 @@ class Context:
                                                     ctypes.byref(out), ctypes.byref(ncut)))
         return out, ncut.value
 
+    # -- RI integrals (the libint part of calculate_ri, src/POSTHF/ri.cc) -----
+    def ri_integrals(self, obs, aux, device="cuda", metric=True, three_index=True):
+        """(J[X][X], pmn[X][N][N]) = ((P|Q), (P|mu nu)) for Basis objects obs
+        and aux, computed on the GPU; outputs as CUDA tensors (device="cuda")
+        or numpy arrays."""
+        X = aux.nbf
+        J = self._filled(device, (X, X), "float64", None) if metric else None
+        P = (self._filled(device, (X, obs.nbf, obs.nbf), "float64", None)
+             if three_index else None)
+        bo, ba = obs.c() if obs is not None else None, aux.c()
+        check(self._L.corr_ri_integrals(self._h, ctypes.byref(bo) if bo is not None else None,
+                                        ctypes.byref(ba), _ptr(J), _ptr(P)))
+        return J, P
+
     # -- CCSD consumer of the MO integrals (src/POSTHF/ccsd.cc) --------------
     def ints_so(self, prec, out=None):
         """calc_ints_so (ccsd.cc:509): <ij||kl> over 2N spin orbitals from the
@@ -338,6 +375,7 @@ class Context:
             return out
         import numpy as np
 
+        dtype = np.dtype(dtype).type
         if like == "cuda":
             import torch
 

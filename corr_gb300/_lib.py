@@ -54,6 +54,12 @@ class SystemInfo(ctypes.Structure):
                 ("basis_jk", ctypes.c_char * 33), ("basis_ri", ctypes.c_char * 33)]
 
 
+class BasisC(ctypes.Structure):
+    _fields_ = [("nsh", ctypes.c_int), ("l", ctypes.c_void_p), ("nprim", ctypes.c_void_p),
+                ("poff", ctypes.c_void_p), ("center", ctypes.c_void_p),
+                ("exps", ctypes.c_void_p), ("coefs", ctypes.c_void_p)]
+
+
 class RIMP2Instance(ctypes.Structure):
     _fields_ = [("nocc", ctypes.c_int), ("nvir", ctypes.c_int), ("naux", ctypes.c_int),
                 ("bia", ctypes.c_void_p), ("eps", ctypes.c_void_p)]
@@ -104,6 +110,7 @@ SIGNATURES = {
                                       ctypes.POINTER(MP2Energy), ctypes.POINTER(_i)],
     "corr_dgemm": [_vp, _i, _i, _i, _i, _i, _d, _vp, _i, _vp, _i, _d, _vp, _i],
     "corr_syev": [_vp, _i, _vp, _vp, _vp],
+    "corr_ri_integrals": [_vp, ctypes.POINTER(BasisC), ctypes.POINTER(BasisC), _vp, _vp],
     "corr_ints_so": [_vp, _i, _vp, _vp],
     "corr_cc_fock": [_vp, _i, _i, _vp, _vp, _vp, _vp, _vp],
     "corr_read_system": [ctypes.c_char_p, ctypes.POINTER(SystemInfo), _vp, _vp, _vp, _vp],

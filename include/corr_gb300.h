@@ -295,6 +295,33 @@ int corr_calculate_ri(corr_context* ctx, int naux, int nroao, const double* J, c
 int corr_ri_apply_metric(corr_context* ctx, int naux, long long ncols, const double* jm12,
                          const double* in, double* out);
 
+/* A basis of contracted Gaussian shells, as a libint2::BasisSet holds it:
+ * shell s has angular momentum l[s] (0..3), nprim[s] primitives with
+ * exponents exps[poff[s] + k] and contraction coefficients coefs[poff[s] + k]
+ * of normalised primitives (the numbers of a basis-set file), centred at
+ * center[3s..3s+2] (bohr).  Its functions are the real solid harmonics
+ * m = -l..l of each shell in shell order, each normalised to one; Cartesian
+ * components are ordered lx = l..0, ly = l-lx..0. */
+typedef struct corr_basis {
+  int nsh;
+  const int* l;
+  const int* nprim;
+  const int* poff;
+  const double* center;
+  const double* exps;
+  const double* coefs;
+} corr_basis;
+
+/* The integrals calculate_ri computes with libint (src/POSTHF/ri.cc:25-47,
+ * 70-100; the psi4 plugin's syshfwplug/plugin.cc:478-503), on the GPU:
+ * J[P][Q] = (P|Q) over the auxiliary basis and pmn[P][mu][nu] = (P|mu nu)
+ * (orbital shells up to d), McMurchie-Davidson in FP64.  Either output may be
+ * NULL; obs may be NULL when pmn is.  The outputs feed
+ * corr_rimp2_energy_from_3index / corr_calculate_ri directly (keep them on the
+ * device: (P|mu nu) is the largest hand-off of the RI path). */
+int corr_ri_integrals(corr_context* ctx, const corr_basis* obs, const corr_basis* aux, double* J,
+                      double* pmn);
+
 /* The RI-MP2 energy from integrals, all on the GPU: (P|ia) from
  * pmn[P][mu][nu] = (P|mu nu) and the MO coefficients (the contractions of
  * transform_ri, ri.cc:147-172), J^-1/2 with the reference's cutoff
