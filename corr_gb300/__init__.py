@@ -367,6 +367,41 @@ class Context:
                                    _ptr(h), _ptr(f)))
         return h, f
 
+    # -- RHF (src/SCF) --------------------------------------------------------
+    def build_fmat(self, pmat, hmat, sortcount, intval, intnums, out=None):
+        """build_Fmat (ops_rhf.cc:549): F = H + sum P ((mn|ls) - 1/2 (ml|ns))."""
+        N = pmat.shape[0]
+        out = self._out(pmat, (N, N), out)
+        check(self._L.corr_build_fmat(self._h, N, _ptr(pmat), _ptr(hmat), int(intval.shape[0]),
+                                      _ptr(sortcount), _ptr(intval), _ptr(intnums), _ptr(out)))
+        return out
+
+    def run_scf(self, nroe, smat, hmat, sortcount, intval, intnums, mos=None, ion_rep=0.0,
+                maxiter=100):
+        """run_scf (scf.cc:145): RHF on the GPU.  ``mos`` (orbitals as rows)
+        is the guess; None or a near-zero diagonal takes the core guess.
+        Returns a dict with mos, fmat, moens, the energies run_scf prints
+        (total, one, two) and the iteration count."""
+        import numpy as np
+
+        N = smat.shape[0]
+        on_dev = hasattr(smat, "is_cuda") and smat.is_cuda
+        if mos is None:
+            mos = self._out(smat, (N, N), None)
+            mos[...] = 0
+        else:
+            mos = mos.clone() if on_dev else np.array(mos, dtype=np.float64, copy=True)
+        fmat = self._out(smat, (N, N), None)
+        moens = self._out(smat, (N,), None)
+        e = np.zeros(3)
+        it = ctypes.c_int(0)
+        check(self._L.corr_run_scf(self._h, int(nroe), N, float(ion_rep), _ptr(smat), _ptr(hmat),
+                                   int(intval.shape[0]), _ptr(sortcount), _ptr(intval),
+                                   _ptr(intnums), int(maxiter), _ptr(mos), _ptr(fmat),
+                                   _ptr(moens), _ptr(e), ctypes.byref(it)))
+        return {"mos": mos, "fmat": fmat, "moens": moens, "energy": float(e[0]),
+                "one": float(e[1]), "two": float(e[2]), "iterations": it.value}
+
     # -- hand-off files (src/IO/ops_io.cc) -----------------------------------
     # Output arrays may be numpy arrays or torch tensors (CUDA tensors are
     # filled through pinned chunk buffers on the context stream).

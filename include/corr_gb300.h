@@ -333,6 +333,40 @@ int corr_rimp2_energy_from_3index(corr_context* ctx, int nroe, int nroao, int na
                                   const double* pmn, int precision, corr_mp2_energy* out,
                                   int* ncut);
 
+/* ---- RHF on the GPU (src/SCF) ------------------------------------------- */
+
+/* Replaces build_Fmat (src/SCF/ops_rhf.cc:549-591): the closed-shell Fock
+ * matrix fmat = hmat + sum_ls pmat[ls] ((mn|ls) - 1/2 (ml|ns)) from the packed
+ * unique integrals (intval, intnums, sortcount: the .tei layout that
+ * corr_motrans reads).  Every array may be host or device memory.  The
+ * integral list is expanded once into the dense nroao^4 tensor on the device
+ * (nroao^4 doubles of workspace); each F_mn is a fixed-order sum. */
+int corr_build_fmat(corr_context* ctx, int nroao, const double* pmat, const double* hmat,
+                    long long nrofint, const long long* sortcount, const double* intval,
+                    const unsigned short* intnums, double* fmat);
+
+/* Replaces run_scf (src/SCF/scf.cc:145-321) with its fixed settings: damped
+ * density (damp 0.5, P = 2(1-damp) C_occ C_occ^T + damp P), Fock build, DIIS
+ * over 8 Fock/error pairs (error S P F - F P S, started once the mean |error|
+ * is below 1e-3 from the 8th iteration on, damping then off; dgels-style
+ * least-squares solve), symmetric orthogonalisation with S^-1/2 (calc_S12,
+ * ops_rhf.cc:342-378) and diagonalisation (diag_Fmat, ops_rhf.cc:425-431),
+ * until |dE| <= 1e-8 or maxiter iterations.  mos (nroao x nroao, orbitals as
+ * rows) is the guess on entry; when |sum_i mos[i][i]| < 0.1 the core guess
+ * (diagonalised hmat, check_initial_guess, ops_rhf.cc:15-36) replaces it.  On
+ * return: mos, fmat (rebuilt from the final density, scf.cc:289-290), moens
+ * (the last diagonalisation's orbital energies; unchanged when none ran) and
+ * energies[3] = {TOTAL E, ONE E, TWO E} as run_scf prints them
+ * (scf.cc:305-314).  *iterations optional.  The overlap must be positive
+ * definite (CORR_ERR_BAD_ARG otherwise; the reference would divide by the
+ * square root of a non-positive eigenvalue).  Runs all on the device; host or
+ * device arrays; nroao <= 2048; its own device allocation of nroao^4 +
+ * 28 nroao^2 doubles plus the integral list. */
+int corr_run_scf(corr_context* ctx, int nroe, int nroao, double ion_rep, const double* smat,
+                 const double* hmat, long long nrofint, const long long* sortcount,
+                 const double* intval, const unsigned short* intnums, int maxiter, double* mos,
+                 double* fmat, double* moens, double* energies, int* iterations);
+
 /* ---- dense FP64 helpers (src/MATH/ops_mat.cc) ---------------------------- */
 
 /* C = alpha op(A) op(B) + beta C, all row-major FP64: op(A) is m x k (A stored

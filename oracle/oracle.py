@@ -317,6 +317,90 @@ def mp2_from_ovov(ovov, eps, nocc, nvir):
     return tuple(out)
 
 
+# ---------------------------------------------------------------------------
+# RHF: src/SCF/ops_rhf.cc, src/SCF/scf.cc
+# ---------------------------------------------------------------------------
+
+def build_fmat(pmat, hmat, packed):
+    """build_Fmat (ops_rhf.cc:549-591): the five permutation-class loops over
+    the unique integrals add up to F = H + sum_ls P_ls ((mn|ls) - 1/2 (ml|ns))."""
+    N = pmat.shape[0]
+    eri = unpack_eri(N, packed)
+    J = np.einsum("mnls,ls->mn", eri, pmat, optimize=True)
+    K = np.einsum("mlns,ls->mn", eri, pmat, optimize=True)
+    return hmat + J - 0.5 * K
+
+
+def _dgels(A, b):
+    """LAPACK dgels ('N': QR least squares), the solver scf.cc:262-266 calls;
+    A here is symmetric, so its column-major reading there is A itself."""
+    from scipy.linalg import lapack
+
+    _, x, info = lapack.dgels(A, b.reshape(-1, 1))
+    assert info == 0, info
+    return x[:, 0]
+
+
+def run_scf(nroe, S, H, packed, ion_rep=0.0, maxiter=100, mos=None):
+    """run_scf (scf.cc:145-321) step for step: calc_S12 (ops_rhf.cc:342),
+    check_initial_guess (ops_rhf.cc:15; core guess when |sum_i C_ii| < 0.1),
+    the damped density (build_Pmat, scf.cc:41-61), DIIS over 8 pairs with the
+    bordered least-squares system (dgels), Calc_e_el, diag_Fmat
+    (ops_rhf.cc:425).  Returns dict(mos [p][mu], fmat, moens, energy, one,
+    two, iterations)."""
+    N = S.shape[0]
+    nocc = nroe // 2
+    w, U = np.linalg.eigh(S)
+    T = U @ np.diag(w ** -0.5) @ U.T
+
+    def diag(F):
+        e, V = np.linalg.eigh(T @ F @ T)
+        return V.T @ T.T, e  # eigenvectors as rows, then transform_MOs
+
+    C = np.zeros((N, N)) if mos is None else np.array(mos, dtype=np.float64)
+    moens = np.zeros(N)
+    if abs(np.trace(C)) < 0.1:
+        C, moens = diag(H)
+
+    def density(C, P, damp):
+        Co = C[:nocc]
+        return 2.0 * (1.0 - damp) * Co.T @ Co + damp * P
+
+    P = density(C, np.zeros((N, N)), 0.0)
+    eri = unpack_eri(N, packed)
+
+    def fock(P):
+        return H + np.einsum("mnls,ls->mn", eri, P) - 0.5 * np.einsum("mlns,ls->mn", eri, P)
+
+    hist_f = [np.zeros((N, N))] * 8
+    hist_e = [np.zeros((N, N))] * 8
+    damp, Eold, DE, it = 0.5, 100.0, 10.0, 0
+    while it < maxiter and abs(DE) > 1e-8:
+        P = density(C, P, damp)
+        F = fock(P)
+        err = S @ P @ F - F @ P @ S
+        hist_f = hist_f[1:] + [F]
+        hist_e = hist_e[1:] + [err]
+        if np.mean(np.abs(err)) < 1e-3 and it >= 8:
+            damp = 0.0
+            B = np.zeros((9, 9))
+            B[:8, :8] = [[np.dot(a.ravel(), b.ravel()) for b in hist_e] for a in hist_e]
+            B[:8, 8] = B[8, :8] = -1.0
+            rhs = np.zeros(9)
+            rhs[8] = -1.0
+            c = _dgels(B, rhs)
+            F = sum(c[j] * hist_f[j] for j in range(8))
+        E = 0.5 * np.sum(P * (F + H))
+        DE, Eold = E - Eold, E
+        C, moens = diag(F)
+        it += 1
+    P = density(C, P, damp)
+    F = fock(P)
+    one, two = np.sum(P * H), np.sum(P * F)
+    return {"mos": C, "fmat": F, "moens": moens, "energy": 0.5 * (one + two) + ion_rep,
+            "one": one + ion_rep, "two": 0.5 * (two - one), "iterations": it}
+
+
 def build_fmo(mos, fmat):
     N = mos.shape[0]
     out = np.zeros((N, N))

@@ -323,6 +323,17 @@ void ref_rhf(int nroe, int nroao, double ion_rep, const double* S, const double*
   delete[] oe.Hmat;  // allocate_onemats hands out one block starting at Hmat
 }
 
+// src/SCF/ops_rhf.cc:549 build_Fmat: the Fock matrix of density pmat from the
+// packed unique integrals.
+void ref_build_fmat(int nroao, const double* pmat, const double* hmat, long long nrofint,
+                    const long long* sortcount, const double* intval,
+                    const unsigned short* intnums, double* fmat_out) {
+  long long sc[4];
+  for (int k = 0; k < 4; ++k) sc[k] = sortcount[k];
+  build_Fmat(nroao, fmat_out, const_cast<double*>(pmat), const_cast<double*>(hmat),
+             const_cast<double*>(intval), const_cast<unsigned short*>(intnums), sc, nrofint);
+}
+
 // src/POSTHF/ccsd.cc:509 calc_ints_so: ints_so[norb^4] (norb = 2 nroao) from
 // the spatial MO integrals prec_ints[N^4].
 void ref_ints_so(int nroe, int nroao, const double* prec, double* out) {

@@ -152,6 +152,24 @@ def rhf(nroe, ion_rep, S, T, V, packed):
     return mos, f, e, float(eh[0])
 
 
+def build_fmat(pmat, hmat, packed):
+    """src/SCF/ops_rhf.cc:549 build_Fmat -> F."""
+    N = pmat.shape[0]
+    f = np.zeros((N, N))
+    lib().ref_build_fmat(N, _p(np.ascontiguousarray(pmat)), _p(np.ascontiguousarray(hmat)),
+                         ctypes.c_longlong(packed.nrofint), _p(packed.sortcount, _i64p),
+                         _p(packed.intval), _p(packed.intnums, _u16p), _p(f))
+    return f
+
+
+def rhf_iterations():
+    """Iterations the last rhf() call ran: the rows of run_scf's table."""
+    import re
+
+    text = lib().ref_last_output().decode()
+    return len(re.findall(r"^\s*\d+:", text, flags=re.M))
+
+
 # ---- src/MATH/ops_mat.cc (mangled C++ symbols of the unmodified sources) ----
 
 def _sq(*arrs):

@@ -1,0 +1,129 @@
+"""RHF on the GPU (src/SCF) against the oracle and the reference's outputs.
+
+corr_build_fmat  build_Fmat (ops_rhf.cc:549): F from a density and the packed
+                 unique integrals, against oracle.build_fmat (pinned to the
+                 reference's build_Fmat) and the reference's final Fock matrix
+                 of H2O / def2-SVP; host and device arrays.
+corr_run_scf     run_scf (scf.cc:145): the whole damped + DIIS iteration on the
+                 GPU, against the reference's printed HF energy, its Fock
+                 matrix and orbital energies (through oracle.run_scf, which
+                 reproduces the reference's iteration count).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import molecule as M
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+with open(os.path.join(HERE, "golden", "golden_molecules.json")) as _f:
+    GOLD = json.load(_f)["config1"]
+
+
+@pytest.fixture(scope="module")
+def h2o():
+    I = M.Integrals(M.water(), "def2-svp")
+    pk = O.pack_eri(I.eri())
+    fx = np.load(os.path.join(HERE, "golden", "config1_h2o.npz"))
+    return I, pk, fx
+
+
+def test_build_fmat_matches_oracle_and_reference(ctx, h2o):
+    I, pk, fx = h2o
+    H = I.T + I.V
+    Co = fx["mos"][:5]
+    P = 2.0 * Co.T @ Co
+    F = ctx.build_fmat(P, H, pk.sortcount, pk.intval, pk.intnums)
+    assert np.abs(F - O.build_fmat(P, H, pk)).max() <= 1e-12
+    assert np.abs(F - fx["fmat"]).max() <= 1e-12  # the reference's final Fmat
+    # a non-physical symmetric density exercises every permutation class
+    R = O.rng(5).standard_normal(P.shape)
+    R = R + R.T
+    F2 = ctx.build_fmat(R, H, pk.sortcount, pk.intval, pk.intnums)
+    ref = O.build_fmat(R, H, pk)
+    assert np.abs(F2 - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
+def test_build_fmat_device_arrays(ctx, h2o):
+    import torch
+
+    I, pk, fx = h2o
+    H = I.T + I.V
+    Co = fx["mos"][:5]
+    P = 2.0 * Co.T @ Co
+    dev = "cuda:0"
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    F = ctx.build_fmat(t(P), t(H), t(pk.sortcount), t(pk.intval),
+                       torch.from_numpy(pk.intnums.view(np.int16)).to(dev))
+    assert F.is_cuda
+    assert np.abs(F.cpu().numpy() - fx["fmat"]).max() <= 1e-12
+
+
+def test_build_fmat_synthetic_eri(ctx):
+    N = 13
+    eri, _ = O.synth_eri(N, 17)
+    pk = O.pack_eri(eri)
+    H = O.rng(18).standard_normal((N, N))
+    H = H + H.T
+    P = O.rng(19).standard_normal((N, N))
+    P = P + P.T
+    F = ctx.build_fmat(P, H, pk.sortcount, pk.intval, pk.intnums)
+    ref = O.build_fmat(P, H, pk)
+    assert np.abs(F - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
+def test_run_scf_h2o_core_guess(ctx, h2o):
+    I, pk, fx = h2o
+    H = I.T + I.V
+    r = ctx.run_scf(10, I.S, H, pk.sortcount, pk.intval, pk.intnums, ion_rep=I.enuc)
+    o = O.run_scf(10, I.S, H, pk, I.enuc)
+    # the reference prints TOTAL E = -75.9610148102 after 17 iterations; the
+    # stop test |dE| > 1e-8 sits close to iteration 15's 1.07e-8, so one
+    # iteration more or less is rounding, not a different method
+    assert abs(r["energy"] - GOLD["E_HF_reference_scf"]) <= 1e-9, r
+    assert abs(r["iterations"] - o["iterations"]) <= 1, (r["iterations"], o["iterations"])
+    assert abs(r["one"] - o["one"]) <= 1e-7 and abs(r["two"] - o["two"]) <= 1e-7
+    assert np.abs(r["fmat"] - fx["fmat"]).max() <= 1e-6
+    assert np.abs(r["moens"] - o["moens"]).max() <= 1e-6
+    # orbitals: each row up to its sign; the density is sign-free
+    C = r["mos"]
+    Pg = 2.0 * C[:5].T @ C[:5]
+    Pr = 2.0 * fx["mos"][:5].T @ fx["mos"][:5]
+    assert np.abs(Pg - Pr).max() <= 1e-6
+    # orthonormal in the metric S
+    assert np.abs(C @ I.S @ C.T - np.eye(I.N)).max() <= 1e-10
+
+
+def test_run_scf_from_converged_orbitals(ctx, h2o):
+    """The reference's converged orbitals as the guess (check_initial_guess
+    keeps them): damping still starts at 0.5, so the run converges back to the
+    same energy."""
+    I, pk, fx = h2o
+    H = I.T + I.V
+    r = ctx.run_scf(10, I.S, H, pk.sortcount, pk.intval, pk.intnums, mos=fx["mos"],
+                    ion_rep=I.enuc)
+    o = O.run_scf(10, I.S, H, pk, I.enuc, mos=fx["mos"])
+    assert abs(r["energy"] - GOLD["E_HF_reference_scf"]) <= 1e-9
+    assert abs(r["energy"] - o["energy"]) <= 1e-10
+    assert abs(r["iterations"] - o["iterations"]) <= 1
+
+
+def test_run_scf_zero_iterations_and_bad_overlap(ctx, h2o):
+    import corr_gb300
+
+    I, pk, fx = h2o
+    H = I.T + I.V
+    r = ctx.run_scf(10, I.S, H, pk.sortcount, pk.intval, pk.intnums, mos=fx["mos"],
+                    ion_rep=I.enuc, maxiter=0)
+    o = O.run_scf(10, I.S, H, pk, I.enuc, mos=fx["mos"], maxiter=0)
+    assert r["iterations"] == 0
+    assert abs(r["energy"] - o["energy"]) <= 1e-10
+    bad = I.S.copy()
+    bad[0, 0] = -1.0
+    with pytest.raises(corr_gb300.CorrError):
+        ctx.run_scf(10, bad, H, pk.sortcount, pk.intval, pk.intnums, ion_rep=I.enuc)

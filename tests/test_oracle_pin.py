@@ -260,3 +260,47 @@ def test_ccsd_spin_orbital_restatements_vs_reference():
     h, f = O.cc_fock(nroe, mos, H, prec)
     assert np.abs(h - rh).max() <= 1e-13 * np.abs(rh).max()
     assert np.abs(f - rf).max() <= 1e-13 * np.abs(rf).max()
+
+
+def _h2o_scf_inputs():
+    from oracle import molecule as M
+
+    I = M.Integrals(M.water(), "def2-svp")
+    return I, O.pack_eri(I.eri())
+
+
+def test_scf_restatement_vs_golden():
+    """oracle.run_scf (run_scf, scf.cc:145) on H2O / def2-SVP reproduces the
+    reference's printed HF energy, and its final Fock matrix the reference's
+    (config1_h2o.npz, written by the reference's own run_scf)."""
+    import json
+
+    I, pk = _h2o_scf_inputs()
+    with open(os.path.join(HERE, "golden", "golden_molecules.json")) as f:
+        g = json.load(f)["config1"]
+    r = O.run_scf(10, I.S, I.T + I.V, pk, I.enuc)
+    assert abs(r["energy"] - g["E_HF_reference_scf"]) < 1e-9
+    fx = np.load(os.path.join(HERE, "golden", "config1_h2o.npz"))
+    assert np.abs(r["fmat"] - fx["fmat"]).max() < 1e-6
+    Co = fx["mos"][:5]
+    P = 2.0 * Co.T @ Co
+    assert np.abs(O.build_fmat(P, I.T + I.V, pk) - fx["fmat"]).max() < 1e-12
+
+
+def test_scf_restatements_vs_reference():
+    """oracle.build_fmat / oracle.run_scf against the reference's build_Fmat
+    (ops_rhf.cc:549) and run_scf (scf.cc:145): same Fock matrices, the same
+    energy and the same number of iterations."""
+    R = _ref()
+    I, pk = _h2o_scf_inputs()
+    H = I.T + I.V
+    P = O.rng(91).standard_normal((I.N, I.N))
+    P = P + P.T
+    ref = R.build_fmat(P, H, pk)
+    assert np.abs(O.build_fmat(P, H, pk) - ref).max() <= 1e-12 * np.abs(ref).max()
+    mos, f, e, E = R.rhf(10, I.enuc, I.S, I.T, I.V, pk)
+    r = O.run_scf(10, I.S, H, pk, I.enuc)
+    assert r["iterations"] == R.rhf_iterations()
+    assert abs(r["energy"] - E) < 1e-9  # E is printed to 10 decimals
+    assert np.abs(r["fmat"] - f).max() < 1e-7
+    assert np.abs(r["moens"] - e).max() < 1e-7
