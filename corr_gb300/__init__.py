@@ -456,9 +456,11 @@ class Context:
         return b
 
     # -- dense FP64 helpers (src/MATH/ops_mat.cc) ----------------------------
-    def dgemm(self, A, B, transa=False, transb=False, alpha=1.0, beta=0.0, out=None):
+    def dgemm(self, A, B, transa=False, transb=False, alpha=1.0, beta=0.0, out=None,
+              tensor_cores=False):
         """C = alpha op(A) op(B) + beta C for row-major 2-D arrays (mat_mat_T:
-        transb, mat_T_mat: transa).  `out` is read when beta != 0."""
+        transb, mat_T_mat: transa).  `out` is read when beta != 0.
+        tensor_cores: the FP64-accurate digit-sliced form (corr_dgemm_tc)."""
         m = A.shape[1] if transa else A.shape[0]
         k = A.shape[0] if transa else A.shape[1]
         n = B.shape[0] if transb else B.shape[1]
@@ -467,8 +469,9 @@ class Context:
         if beta != 0.0 and out is None:
             raise ValueError("dgemm: beta != 0 needs out")
         out = self._out(A, (m, n), out)
-        check(self._L.corr_dgemm(self._h, int(transa), int(transb), m, n, k, float(alpha), _ptr(A),
-                                 A.shape[1], _ptr(B), B.shape[1], float(beta), _ptr(out), n))
+        fn = self._L.corr_dgemm_tc if tensor_cores else self._L.corr_dgemm
+        check(fn(self._h, int(transa), int(transb), m, n, k, float(alpha), _ptr(A), A.shape[1],
+                 _ptr(B), B.shape[1], float(beta), _ptr(out), n))
         return out
 
     def syev(self, A, w=None, vecs=None):

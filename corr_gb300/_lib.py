@@ -113,6 +113,7 @@ SIGNATURES = {
     "corr_ri_integrals": [_vp, ctypes.POINTER(BasisC), ctypes.POINTER(BasisC), _vp, _vp],
     "corr_ints_so": [_vp, _i, _vp, _vp],
     "corr_cc_fock": [_vp, _i, _i, _vp, _vp, _vp, _vp, _vp],
+    "corr_dgemm_tc": [_vp, _i, _i, _i, _i, _i, _d, _vp, _i, _vp, _i, _d, _vp, _i],
     "corr_build_fmat": [_vp, _i, _vp, _vp, _ll, _vp, _vp, _vp, _vp],
     "corr_run_scf": [_vp, _i, _i, _d, _vp, _vp, _ll, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp],
     "corr_read_system": [ctypes.c_char_p, ctypes.POINTER(SystemInfo), _vp, _vp, _vp, _vp],

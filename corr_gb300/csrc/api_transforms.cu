@@ -1,6 +1,7 @@
 // C-ABI entry points of the FP64 transforms and the canonical MP2 energy.
 #include "abi_internal.h"
 #include "common.cuh"
+#include "dgemm_tc.h"
 #include "gemm_fp64.h"
 #include "kernels.h"
 
@@ -306,6 +307,10 @@ namespace corr {
 size_t jacobi_workspace_bytes(int m);
 size_t chol_workspace_bytes(int m);
 int chol_norm_inf(corr_context* c, void* scratch, const double* J, int m, double* out);
+__global__ void set_diagonal_kernel(double* __restrict__ A, int m, double d) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x < m) A[(size_t)x * m + x] = d;
+}
 int chol_factor_device(corr_context* c, void* ws, const double* J, int m, double shift,
                        double** Lm_out, double** Linv_out, bool* ok);
 int chol_solve_device(corr_context* c, const double* Lm, const double* Linv, int m, double* P,
@@ -434,6 +439,10 @@ int corr_rimp2_energy_from_3index(corr_context* c, int nroe, int nroao, int naux
                nj = (size_t)X * X;
   const bool mdev = is_device_ptr(mos), edev = is_device_ptr(eps), jdev = is_device_ptr(J),
              pdev = is_device_ptr(pmn);
+  // The precision forms run the three FP64 contractions on the tensor cores
+  // (dgemm_tc.cu, FP64-accurate digit slicing); the FP64 form keeps the FP64
+  // pipe throughout.
+  const bool tc = precision != CORR_PREC_FP64;
   // Region 1 (persistent across the stages): staged inputs, (P|ia), B, J^-1/2.
   auto plan = [&](Carver& w, void** sm, void** se, void** sj, void** sp, double** pia,
                   double** bia, double** jm, double** biq, void** jws) {
@@ -452,7 +461,13 @@ int corr_rimp2_energy_from_3index(corr_context* c, int nroe, int nroao, int naux
   double *pia, *bia, *jm, *biq;
   Carver cv{nullptr, 0};
   plan(cv, &sm, &se, &sj, &sp, &pia, &bia, &jm, &biq, &jws);
-  CORR_TRY(c->ws.reserve(cv.used + energy_scratch_bytes(c, o, v, X, precision)));
+  // Region 2, reused: the digit planes of the tensor-core contractions (and
+  // the identity that becomes L^-1), then the energy's scratch.
+  const size_t dg_bytes =
+      tc ? std::max(std::max(dgemm_tc_workspace(X * N, o, N), dgemm_tc_workspace(X * o, v, N)),
+                    dgemm_tc_workspace(X, o * v, X)) + 2 * nj * 8 + 512
+         : 0;
+  CORR_TRY(c->ws.reserve(cv.used + std::max(dg_bytes, energy_scratch_bytes(c, o, v, X, precision))));
   Carver w{c->ws.ptr, 0};
   plan(w, &sm, &se, &sj, &sp, &pia, &bia, &jm, &biq, &jws);
   CORR_CUDA(cudaMemsetAsync(c->dres, 0, sizeof(ResultBlock), c->stream));
@@ -463,13 +478,39 @@ int corr_rimp2_energy_from_3index(corr_context* c, int nroe, int nroao, int naux
   const double* d_p = static_cast<const double*>(stage_in(c, pmn, np * 8, sp));
   CORR_CHECK_ARG(d_m && d_e && d_j && d_p, "host-to-device copy failed");
   // (P|ia) = C_occ (P|mu nu) C_vir^T  (the transform_ri contractions, ri.cc:147-172)
-  GemmF64 g1 = gemm_args(d_m, d_p, biq, o, N, N, N, N, N, 0, 0);
-  g1.sb = (long long)N * N;
-  g1.sc = (long long)o * N;
-  g1.batch = X;
-  CORR_TRY(gemm_f64(g1, &c->dres->status, c->stream));
-  CORR_TRY(gemm_f64(gemm_args(biq, d_m + (size_t)o * N, pia, X * o, v, N, N, N, v, 0, 1),
-                    &c->dres->status, c->stream));
+  if (tc) {
+    Carver r2 = w;
+    void* dws = r2.take(dg_bytes);
+    // (P|i nu): rows (P, nu) of (P|mu nu) (symmetric in mu nu) against the
+    // occupied rows of C, written in the [P][i][nu] layout
+    DgemmTc g1;
+    g1.A = mat_view(d_p, N, 1);
+    g1.B = mat_view(d_m, N, 1);
+    g1.C = OutView{biq, (long long)o * N, 1, N, N};
+    g1.M = X * N;
+    g1.N = o;
+    g1.K = N;
+    g1.alpha = 1.0;
+    g1.accumulate = false;
+    g1.a_lower = false;
+    CORR_TRY(dgemm_tc(c, g1, dws));
+    // (P|ia): rows (P, i) against the virtual rows of C
+    DgemmTc g2 = g1;
+    g2.A = mat_view(biq, N, 1);
+    g2.B = mat_view(d_m + (size_t)o * N, N, 1);
+    g2.C = out_view(pia, v, 1);
+    g2.M = X * o;
+    g2.N = v;
+    CORR_TRY(dgemm_tc(c, g2, dws));
+  } else {
+    GemmF64 g1 = gemm_args(d_m, d_p, biq, o, N, N, N, N, N, 0, 0);
+    g1.sb = (long long)N * N;
+    g1.sc = (long long)o * N;
+    g1.batch = X;
+    CORR_TRY(gemm_f64(g1, &c->dres->status, c->stream));
+    CORR_TRY(gemm_f64(gemm_args(biq, d_m + (size_t)o * N, pia, X * o, v, N, N, N, v, 0, 1),
+                      &c->dres->status, c->stream));
+  }
   // The metric.  The energy sees J only through J^-1 = W^T W: when the
   // reference's cutoff (ri.cc:56-66, lambda/lambda_max < 1e-10) provably cuts
   // nothing -- J - 10 tol ||J||_inf I is positive definite -- W = L^-1 from a
@@ -484,15 +525,50 @@ int corr_rimp2_energy_from_3index(corr_context* c, int nroe, int nroao, int naux
                                                &certified));
   bool factored = false;
   if (certified) CORR_TRY(chol_factor_device(c, jws, d_j, X, 0.0, &Lm, &Linv, &factored));
+  // W as an explicit matrix for the tensor-core product: L^-1 (lower
+  // triangular, by the blocked substitution on the identity) or J^-1/2
+  double* W = nullptr;
   if (factored) {
-    CORR_TRY(chol_solve_device(c, Lm, Linv, X, pia, (long long)o * v, bia));
     if (ncut) *ncut = 0;
+    if (tc) {
+      Carver r2 = w;
+      r2.take(dg_bytes - 2 * nj * 8 - 512);
+      double* eye = static_cast<double*>(r2.take(nj * 8));
+      W = static_cast<double*>(r2.take(nj * 8));
+      CORR_CUDA(cudaMemsetAsync(eye, 0, nj * 8, c->stream));
+      set_diagonal_kernel<<<(X + 255) / 256, 256, 0, c->stream>>>(eye, X, 1.0);
+      CORR_CUDA(cudaGetLastError());
+      CORR_TRY(chol_solve_device(c, Lm, Linv, X, eye, X, W));
+      c->launches += 1;
+    } else {
+      CORR_TRY(chol_solve_device(c, Lm, Linv, X, pia, (long long)o * v, bia));
+    }
   } else {
     CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, X, tol, jm, ncut));
-    CORR_TRY(gemm_f64(gemm_args(jm, pia, bia, X, o * v, X, X, (long long)o * v,
-                                (long long)o * v, 0, 0),
-                      &c->dres->status, c->stream));
-    c->launches += 1;
+    W = jm;
+    if (!tc) {
+      CORR_TRY(gemm_f64(gemm_args(jm, pia, bia, X, o * v, X, X, (long long)o * v,
+                                  (long long)o * v, 0, 0),
+                        &c->dres->status, c->stream));
+      c->launches += 1;
+    }
+  }
+  if (tc) {
+    // B[Q][ia] = sum_P W[Q][P] (P|ia): rows Q of W against the columns ia of
+    // (P|ia) read as rows over P
+    Carver r2 = w;
+    void* dws = r2.take(dg_bytes - 2 * nj * 8 - 512);
+    DgemmTc g3;
+    g3.A = mat_view(W, X, 1);
+    g3.B = mat_view(pia, 1, (long long)o * v);
+    g3.C = out_view(bia, (long long)o * v, 1);
+    g3.M = X;
+    g3.N = o * v;
+    g3.K = X;
+    g3.alpha = 1.0;
+    g3.accumulate = false;
+    g3.a_lower = factored;
+    CORR_TRY(dgemm_tc(c, g3, dws));
   }
   c->launches += 2;
   // energy on the device-resident B; its scratch is carved after region 1

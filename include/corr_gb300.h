@@ -381,6 +381,20 @@ int corr_dgemm(corr_context* ctx, int transa, int transb, int m, int n, int k, d
                const double* A, int lda, const double* B, int ldb, double beta, double* C,
                int ldc);
 
+/* corr_dgemm on the tensor cores, FP64-accurate: both operands are split
+ * exactly into eight balanced 7-bit integer digits per row of op(A) and per
+ * column of op(B) (scaled by the row's / column's largest binary exponent),
+ * the 36 digit products of significance up to 2^-56 run as BF16 tcgen05 MMAs
+ * whose level sums are exact in FP32 (K in passes of 512), and the levels are
+ * recombined in 64-bit integers with one rounding to FP64.  Error per element
+ * <= ~2^-53 sqrt(k) max|A row| max|B column| -- comparable to an FP64 GEMM for
+ * data without a wide range inside a row; elements much smaller than their
+ * row/column scales carry a larger relative error than in FP64.  Inputs must
+ * be finite.  Same arguments as corr_dgemm. */
+int corr_dgemm_tc(corr_context* ctx, int transa, int transb, int m, int n, int k, double alpha,
+                  const double* A, int lda, const double* B, int ldb, double beta, double* C,
+                  int ldc);
+
 /* Replaces diag_mat (ops_mat.cc:21-45, LAPACK dsyev with JOBZ='V'): the
  * eigenvalues of the symmetric n x n matrix A in ascending order in w[n], and
  * vecs[k*n + i] = component i of the eigenvector of w[k] (dsyev's column-major
