@@ -62,30 +62,38 @@ __host__ __device__ constexpr int tuv_index(int t, int u, int v) {
   return tuv_count(t + u + v - 1 >= 0 ? t + u + v - 1 : -1) + ((u + v) * (u + v + 1)) / 2 + v;
 }
 
+// Boys function F_n(T), n <= NMAX: for T < kBoysTmax an 8-term Taylor
+// expansion of F_NMAX about the nearest point of a tabulated grid (spacing
+// 1/16, |dT| <= 1/32, truncation below 2^-55 relative) and downward
+// recursion F_n = (2T F_{n+1} + e^-T) / (2n + 1); above, the asymptotic
+// F_0 = sqrt(pi/T) / 2 (erf(sqrt T) = 1 to 1e-18) and upward recursion
+// without the e^-T term (below 4e-18 relative).
+constexpr int kBoysOrders = 16;                // tabulated n = 0..15
+constexpr int kBoysPerUnit = 16;               // grid points per unit of T
+constexpr double kBoysTmax = 40.0;
+constexpr int kBoysPoints = (int)kBoysTmax * kBoysPerUnit + 1;
+__device__ double d_boys[kBoysPoints][kBoysOrders];
+
 template <int NMAX>
 __device__ __forceinline__ void boys(double T, double* F) {
-  if (T < 1e-15) {
+  static_assert(NMAX + 8 <= kBoysOrders, "Boys table orders");
+  if (T < kBoysTmax) {
+    const int i = __double2int_rn(T * kBoysPerUnit);
+    const double x = (double)i * (1.0 / kBoysPerUnit) - T;  // -dT
+    const double* f = d_boys[i] + NMAX;
+    double s = f[7];
 #pragma unroll
-    for (int n = 0; n <= NMAX; ++n) F[n] = 1.0 / (2 * n + 1);
+    for (int k = 6; k >= 0; --k) s = fma(s, x * (1.0 / (k + 1)), f[k]);
+    F[NMAX] = s;
+    const double et = exp(-T), t2 = 2.0 * T;
+#pragma unroll
+    for (int n = NMAX - 1; n >= 0; --n) F[n] = fma(t2, F[n + 1], et) * (1.0 / (2 * n + 1));
     return;
   }
-  const double et = exp(-T);
-  if (T >= 33.0) {
-    const double st = sqrt(T);
-    F[0] = 0.5 * sqrt(M_PI) / st * erf(st);
+  const double rt = 1.0 / T;
+  F[0] = 0.886226925452758 * sqrt(rt);  // sqrt(pi) / 2
 #pragma unroll
-    for (int n = 0; n < NMAX; ++n) F[n + 1] = ((2 * n + 1) * F[n] - et) / (2.0 * T);
-    return;
-  }
-  double term = 1.0 / (2 * NMAX + 1), sum = term;
-  for (int k = 1; k < 200; ++k) {
-    term *= 2.0 * T / (2 * NMAX + 2 * k + 1);
-    sum += term;
-    if (term < 1e-17 * sum) break;
-  }
-  F[NMAX] = et * sum;
-#pragma unroll
-  for (int n = NMAX - 1; n >= 0; --n) F[n] = (2.0 * T * F[n + 1] + et) / (2 * n + 1);
+  for (int n = 0; n < NMAX; ++n) F[n + 1] = F[n] * ((n + 0.5) * rt);
 }
 
 // R^0_{tuv}(alpha, X, Y, Z), t + u + v <= L, into buf[0][tuv_index].  Ping-pong
@@ -377,6 +385,27 @@ void build_sph(double sph[kLmax + 1][2 * kLmax + 1][10]) {
     }
 }
 
+// F_n(T_i), T_i = i / kBoysPerUnit, by the series
+// F_N(T) = e^-T sum_k (2T)^k / ((2N+1)(2N+3)...(2N+2k+1)) for the highest
+// order (all terms positive) and downward recursion, in long double.
+void build_boys(double* tab) {
+  for (int i = 0; i < kBoysPoints; ++i) {
+    const long double T = (long double)i / kBoysPerUnit;
+    const int N = kBoysOrders - 1;
+    long double term = 1.0L / (2 * N + 1), sum = term;
+    for (int k = 1; k < 2000; ++k) {
+      term *= 2.0L * T / (2 * N + 2 * k + 1);
+      sum += term;
+      if (term < 1e-22L * sum) break;
+    }
+    const long double et = expl(-T);
+    long double f[kBoysOrders];
+    f[N] = et * sum;
+    for (int n = N - 1; n >= 0; --n) f[n] = (2.0L * T * f[n + 1] + et) / (2 * n + 1);
+    for (int n = 0; n < kBoysOrders; ++n) tab[(size_t)i * kBoysOrders + n] = (double)f[n];
+  }
+}
+
 double dfact(int n) {  // n!!, 1 for n <= 0
   double r = 1.0;
   for (int k = n; k > 1; k -= 2) r *= k;
@@ -593,6 +622,18 @@ extern "C" int corr_ri_integrals(corr_context* c, const corr_basis* obs, const c
     CORR_TRY(up(p[10], p3flat.data(), p3flat.size() * 8));
   }
   CORR_CUDA(cudaMemcpyToSymbolAsync(c_sph, sph, sizeof(sph), 0, cudaMemcpyHostToDevice, c->stream));
+  {
+    static std::vector<double> boys_tab;
+    static bool boys_done[64] = {};
+    if (boys_tab.empty()) {
+      boys_tab.resize((size_t)kBoysPoints * kBoysOrders);
+      build_boys(boys_tab.data());
+    }
+    if (c->device < 0 || c->device >= 64 || !boys_done[c->device]) {
+      CORR_CUDA(cudaMemcpyToSymbol(d_boys, boys_tab.data(), boys_tab.size() * 8));
+      if (c->device >= 0 && c->device < 64) boys_done[c->device] = true;
+    }
+  }
   {
     static int ce[kLmax + 1][10][3], tv[kTmax][kTmax][kTmax];  // constant tables
     for (int l = 0; l <= kLmax; ++l)
