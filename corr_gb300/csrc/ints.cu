@@ -183,6 +183,8 @@ struct Basis3 {
   int nalist;
   const ShellD* obs;   // ket shells
   const int2* plist;   // ket shell pairs (c, d) of this class; d < 0: exponent-0 s partner
+  const int2* prange;  // per ket pair: its primitive pairs pp[x .. y)
+  const ushort2* pp;   // (primitive of c, primitive of d) that pass the screening
   int nplist;
   const double* aexp;  // primitives of the bra basis (coefficients include the
   const double* acof;  // primitive normalisation)
@@ -217,8 +219,10 @@ __global__ void __launch_bounds__(128) eri3_kernel(Basis3 g) {
 #pragma unroll
     for (int k = 0; k < NP * NC * ND; ++k) cart[k] = 0.0;
     const double Xcd = sc.x - sd.x, Ycd = sc.y - sd.y, Zcd = sc.z - sd.z;
-    for (int ic = 0; ic < sc.nprim; ++ic)
-      for (int id = 0; id < npd; ++id) {
+    (void)npd;
+    const int2 rg = g.prange[ki];
+    for (int q = rg.x; q < rg.y; ++q) {
+        const int ic = g.pp[q].x, id = g.pp[q].y;
         const double a = g.oexp[sc.poff + ic];
         const double b = has_d ? g.oexp[sd.poff + id] : 0.0;
         const double ccd = g.ocof[sc.poff + ic] * (has_d ? g.ocof[sd.poff + id] : 1.0);
@@ -494,6 +498,47 @@ int make_basis(const corr_basis* b, const double sph[kLmax + 1][2 * kLmax + 1][1
   return CORR_OK;
 }
 
+// Primitive screening of the 3-index integrals.  For primitive Gaussians
+// (exponents a, b on centres A, B; coefficients with their normalisation)
+// the Schwarz inequality |(P|ab)| <= (P|P)^1/2 (ab|ab)^1/2 with, for s
+// functions, (ab|ab) = 2 pi^(5/2) / (p^2 sqrt(2p)) K_ab^2, p = a + b,
+// K_ab = exp(-ab/p |AB|^2); the factor (1 + |AB|)^(la+lb) (1 + 1/sqrt p)^(la+lb)
+// covers the polynomial parts of higher angular momenta.  A primitive pair
+// whose bound times the largest auxiliary factor stays below kScreen is
+// skipped (its contributions lie below 1e-15 of the unit-normalised
+// integrals); a shell pair left with none is zero.
+constexpr double kScreen = 1e-15;
+
+double aux_schwarz_max(const HostBasis& hb) {
+  double m = 0.0;
+  for (const ShellD& sh : hb.sh)
+    for (int k = 0; k < sh.nprim; ++k) {
+      const double q = hb.exps[sh.poff + k];
+      const double f = std::fabs(hb.cofs[sh.poff + k]) *
+                       std::sqrt(2.0 * std::pow(M_PI, 2.5) / (q * q * std::sqrt(2.0 * q))) *
+                       std::pow(1.0 + 1.0 / std::sqrt(q), sh.l);
+      m = std::max(m, f);
+    }
+  return m;
+}
+
+void screen_pairs(const HostBasis& hb, int x, int y, double saux, std::vector<ushort2>* pp) {
+  const ShellD& A = hb.sh[x];
+  const ShellD& B = hb.sh[y];
+  const double dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
+  const double r2 = dx * dx + dy * dy + dz * dz, r = std::sqrt(r2);
+  const int lsum = A.l + B.l;
+  for (int i = 0; i < A.nprim; ++i)
+    for (int j = 0; j < B.nprim; ++j) {
+      const double a = hb.exps[A.poff + i], b = hb.exps[B.poff + j], p = a + b;
+      const double kab = std::exp(-a * b / p * r2);
+      const double bound = std::fabs(hb.cofs[A.poff + i] * hb.cofs[B.poff + j]) * kab *
+                           std::sqrt(2.0 * std::pow(M_PI, 2.5) / (p * p * std::sqrt(2.0 * p))) *
+                           std::pow((1.0 + r) * (1.0 + 1.0 / std::sqrt(p)), lsum) * saux;
+      if (bound >= kScreen) pp->push_back(make_ushort2((unsigned short)i, (unsigned short)j));
+    }
+}
+
 using Kern = void (*)(Basis3);
 
 template <int LP, int LC, int LD>
@@ -548,14 +593,34 @@ extern "C" int corr_ri_integrals(corr_context* c, const corr_basis* obs, const c
   std::vector<std::vector<int>> alist(kLmax + 1);
   for (int s = 0; s < (int)ha.sh.size(); ++s) alist[ha.sh[s].l].push_back(s);
   std::vector<std::vector<int2>> plist3(9), plist2(kLmax + 1);  // 3c: lc*3 + ld ; 2c: lc
-  for (int s = 0; s < (int)ha.sh.size(); ++s) plist2[ha.sh[s].l].push_back(make_int2(s, -1));
-  if (pmn)
+  // primitive pairs of every ket pair: all of them for (P|Q); for (P|cd) the
+  // pairs whose Schwarz factor can reach kScreen (see screen_pairs)
+  std::vector<std::vector<int2>> prange3(9), prange2(kLmax + 1);
+  std::vector<ushort2> pp;
+  for (int s = 0; s < (int)ha.sh.size(); ++s) {
+    const int b = (int)pp.size();
+    for (int k = 0; k < ha.sh[s].nprim; ++k) pp.push_back(make_ushort2((unsigned short)k, 0));
+    plist2[ha.sh[s].l].push_back(make_int2(s, -1));
+    prange2[ha.sh[s].l].push_back(make_int2(b, (int)pp.size()));
+  }
+  long long pairs_kept = 0, pairs_all = 0;
+  if (pmn) {
+    const double saux = aux_schwarz_max(ha);
     for (int cs = 0; cs < (int)ho.sh.size(); ++cs)
       for (int ds = 0; ds <= cs; ++ds) {
         int x = cs, y = ds;
         if (ho.sh[x].l < ho.sh[y].l) std::swap(x, y);  // lc >= ld
+        const int b = (int)pp.size();
+        screen_pairs(ho, x, y, saux, &pp);
+        pairs_all += (long long)ho.sh[x].nprim * ho.sh[y].nprim;
+        pairs_kept += (long long)pp.size() - b;
+        if ((int)pp.size() == b) continue;  // every integral of the pair is below the threshold
         plist3[ho.sh[x].l * 3 + ho.sh[y].l].push_back(make_int2(x, y));
+        prange3[ho.sh[x].l * 3 + ho.sh[y].l].push_back(make_int2(b, (int)pp.size()));
       }
+  }
+  (void)pairs_all;
+  (void)pairs_kept;
   // device copies (workspace): shells, primitives, norms, lists, staged outputs
   auto bytes_of = [](size_t n, size_t e) { return n * e; };
   size_t nal = 0, np3 = 0, np2 = 0;
@@ -577,8 +642,11 @@ extern "C" int corr_ri_integrals(corr_context* c, const corr_basis* obs, const c
     p[10] = pmn ? w.take(bytes_of(np3, 8)) : nullptr;
     p[11] = (J && !jdev) ? w.take((size_t)X * X * 8) : nullptr;
     p[12] = (pmn && !pdev) ? w.take((size_t)X * N * N * 8) : nullptr;
+    p[13] = w.take(bytes_of(np2, 8));
+    p[14] = pmn ? w.take(bytes_of(np3, 8)) : nullptr;
+    p[15] = w.take(bytes_of(pp.size(), 4));
   };
-  void* p[13];
+  void* p[16];
   Carver cv{nullptr, 0};
   plan(cv, p);
   CORR_TRY(c->ws.reserve(cv.used));
@@ -592,16 +660,18 @@ extern "C" int corr_ri_integrals(corr_context* c, const corr_basis* obs, const c
     aflat.insert(aflat.end(), alist[l].begin(), alist[l].end());
   }
   aoff[kLmax + 1] = (int)aflat.size();
-  std::vector<int2> p2flat, p3flat;
+  std::vector<int2> p2flat, p3flat, r2flat, r3flat;
   std::vector<int> p2off(kLmax + 2, 0), p3off(10, 0);
   for (int l = 0; l <= kLmax; ++l) {
     p2off[l] = (int)p2flat.size();
     p2flat.insert(p2flat.end(), plist2[l].begin(), plist2[l].end());
+    r2flat.insert(r2flat.end(), prange2[l].begin(), prange2[l].end());
   }
   p2off[kLmax + 1] = (int)p2flat.size();
   for (int k = 0; k < 9; ++k) {
     p3off[k] = (int)p3flat.size();
     p3flat.insert(p3flat.end(), plist3[k].begin(), plist3[k].end());
+    r3flat.insert(r3flat.end(), prange3[k].begin(), prange3[k].end());
   }
   p3off[9] = (int)p3flat.size();
   auto up = [&](void* dst, const void* src, size_t n) -> int {
@@ -614,7 +684,10 @@ extern "C" int corr_ri_integrals(corr_context* c, const corr_basis* obs, const c
   CORR_TRY(up(p[3], ha.norm.data(), ha.norm.size() * 8));
   CORR_TRY(up(p[4], aflat.data(), aflat.size() * 4));
   CORR_TRY(up(p[5], p2flat.data(), p2flat.size() * 8));
+  CORR_TRY(up(p[13], r2flat.data(), r2flat.size() * 8));
+  CORR_TRY(up(p[15], pp.data(), pp.size() * 4));
   if (pmn) {
+    CORR_TRY(up(p[14], r3flat.data(), r3flat.size() * 8));
     CORR_TRY(up(p[6], ho.sh.data(), ho.sh.size() * sizeof(ShellD)));
     CORR_TRY(up(p[7], ho.exps.data(), ho.exps.size() * 8));
     CORR_TRY(up(p[8], ho.cofs.data(), ho.cofs.size() * 8));
@@ -695,6 +768,7 @@ extern "C" int corr_ri_integrals(corr_context* c, const corr_basis* obs, const c
   const ShellD* dA = static_cast<const ShellD*>(p[0]);
   double* Jout = J ? (jdev ? J : static_cast<double*>(p[11])) : nullptr;
   double* Pout = pmn ? (pdev ? pmn : static_cast<double*>(p[12])) : nullptr;
+  if (Pout) CORR_CUDA(cudaMemsetAsync(Pout, 0, (size_t)X * N * N * 8, c->stream));
   for (int lp = 0; lp <= kLmax; ++lp) {
     const int na = aoff[lp + 1] - aoff[lp];
     if (na == 0) continue;
@@ -710,6 +784,8 @@ extern "C" int corr_ri_integrals(corr_context* c, const corr_basis* obs, const c
         Basis3 h = g;
         h.obs = dA;
         h.plist = static_cast<const int2*>(p[5]) + p2off[lc];
+        h.prange = static_cast<const int2*>(p[13]) + p2off[lc];
+        h.pp = static_cast<const ushort2*>(p[15]);
         h.nplist = p2off[lc + 1] - p2off[lc];
         h.oexp = h.aexp;
         h.ocof = h.acof;
@@ -726,6 +802,8 @@ extern "C" int corr_ri_integrals(corr_context* c, const corr_basis* obs, const c
           Basis3 h = g;
           h.obs = static_cast<const ShellD*>(p[6]);
           h.plist = static_cast<const int2*>(p[10]) + p3off[lc * 3 + ld];
+          h.prange = static_cast<const int2*>(p[14]) + p3off[lc * 3 + ld];
+          h.pp = static_cast<const ushort2*>(p[15]);
           h.nplist = p3off[lc * 3 + ld + 1] - p3off[lc * 3 + ld];
           h.oexp = static_cast<const double*>(p[7]);
           h.ocof = static_cast<const double*>(p[8]);
