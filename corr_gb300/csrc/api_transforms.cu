@@ -307,12 +307,11 @@ namespace corr {
 size_t jacobi_workspace_bytes(int m);
 size_t chol_workspace_bytes(int m);
 int chol_norm_inf(corr_context* c, void* scratch, const double* J, int m, double* out);
-__global__ void set_diagonal_kernel(double* __restrict__ A, int m, double d) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x < m) A[(size_t)x * m + x] = d;
-}
 int chol_factor_device(corr_context* c, void* ws, const double* J, int m, double shift,
                        double** Lm_out, double** Linv_out, bool* ok);
+int chol_inverse_device(corr_context* c, const double* Lm, const double* Linv, int m, double* X,
+                        double* T);
+int chol_norm_one_inf(corr_context* c, void* scratch, const double* X, int m, double* out);
 int chol_solve_device(corr_context* c, const double* Lm, const double* Linv, int m, double* P,
                       long long ncols, double* out);
 int ri_inv_sqrt_device(corr_context* c, void* ws, const double* J, int m, double tol,
@@ -520,33 +519,48 @@ int corr_rimp2_energy_from_3index(corr_context* c, int nroe, int nroao, int naux
   double jnorm = 0.0;
   CORR_TRY(chol_norm_inf(c, jm, d_j, X, &jnorm));
   double *Lm = nullptr, *Linv = nullptr;
-  bool certified = false;
-  if (jnorm > 0.0) CORR_TRY(chol_factor_device(c, jws, d_j, X, 10.0 * tol * jnorm, &Lm, &Linv,
-                                               &certified));
+  double* W = nullptr;  // the explicit metric factor of the tensor-core product
   bool factored = false;
-  if (certified) CORR_TRY(chol_factor_device(c, jws, d_j, X, 0.0, &Lm, &Linv, &factored));
-  // W as an explicit matrix for the tensor-core product: L^-1 (lower
-  // triangular, by the blocked substitution on the identity) or J^-1/2
-  double* W = nullptr;
-  if (factored) {
-    if (ncut) *ncut = 0;
-    if (tc) {
+  if (tc) {
+    // One factorisation J = L L^T and W = L^-1 (recursive blocked inversion).
+    // Certificate from W itself: lambda_min(J) = 1 / ||L^-1||_2^2 >=
+    // 1 / (||L^-1||_1 ||L^-1||_inf); when that bound does not reach twice
+    // the threshold, J - t I is factored as below.
+    if (jnorm > 0.0) CORR_TRY(chol_factor_device(c, jws, d_j, X, 0.0, &Lm, &Linv, &factored));
+    if (factored) {
       Carver r2 = w;
       r2.take(dg_bytes - 2 * nj * 8 - 512);
-      double* eye = static_cast<double*>(r2.take(nj * 8));
+      double* T = static_cast<double*>(r2.take(nj * 8));
       W = static_cast<double*>(r2.take(nj * 8));
-      CORR_CUDA(cudaMemsetAsync(eye, 0, nj * 8, c->stream));
-      set_diagonal_kernel<<<(X + 255) / 256, 256, 0, c->stream>>>(eye, X, 1.0);
-      CORR_CUDA(cudaGetLastError());
-      CORR_TRY(chol_solve_device(c, Lm, Linv, X, eye, X, W));
-      c->launches += 1;
+      CORR_TRY(chol_inverse_device(c, Lm, Linv, X, W, T));
+      double n1inf = 0.0;
+      CORR_TRY(chol_norm_one_inf(c, jm, W, X, &n1inf));
+      bool certified = n1inf > 0.0 && 1.0 / n1inf > 2.0 * 10.0 * tol * jnorm;
+      if (!certified)
+        CORR_TRY(chol_factor_device(c, jws, d_j, X, 10.0 * tol * jnorm, &Lm, &Linv, &certified));
+      factored = certified;
+    }
+    if (factored) {
+      if (ncut) *ncut = 0;
     } else {
-      CORR_TRY(chol_solve_device(c, Lm, Linv, X, pia, (long long)o * v, bia));
+      CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, X, tol, jm, ncut));
+      W = jm;
     }
   } else {
-    CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, X, tol, jm, ncut));
-    W = jm;
-    if (!tc) {
+    // The metric.  The energy sees J only through J^-1 = W^T W: when the
+    // reference's cutoff (ri.cc:56-66, lambda/lambda_max < 1e-10) provably
+    // cuts nothing -- J - 10 tol ||J||_inf I is positive definite -- W = L^-1
+    // from a Cholesky factorisation (chol.cu); otherwise W = J^-1/2 with the
+    // cutoff (ri.cc:50-69), applied to the (P|ia) matrix (2 X^2 o v flops).
+    bool certified = false;
+    if (jnorm > 0.0) CORR_TRY(chol_factor_device(c, jws, d_j, X, 10.0 * tol * jnorm, &Lm, &Linv,
+                                                 &certified));
+    if (certified) CORR_TRY(chol_factor_device(c, jws, d_j, X, 0.0, &Lm, &Linv, &factored));
+    if (factored) {
+      CORR_TRY(chol_solve_device(c, Lm, Linv, X, pia, (long long)o * v, bia));
+      if (ncut) *ncut = 0;
+    } else {
+      CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, X, tol, jm, ncut));
       CORR_TRY(gemm_f64(gemm_args(jm, pia, bia, X, o * v, X, X, (long long)o * v,
                                   (long long)o * v, 0, 0),
                         &c->dres->status, c->stream));

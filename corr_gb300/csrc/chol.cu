@@ -24,6 +24,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <utility>
+#include <vector>
 
 #include "common.cuh"
 #include "gemm_fp64.h"
@@ -79,24 +81,28 @@ __global__ void __launch_bounds__(256) chol_diag(const double* __restrict__ A, i
     }
     __syncthreads();
   }
-  // Linv = L^-1 by columns: thread j owns column j (forward substitution,
-  // reading back only its own earlier stores); zero outside the nb x nb
-  // lower triangle.
-  if (t < NB) {
-    const int j = t;
-    for (int i = 0; i < NB; ++i) {
-      double xv = 0.0;
-      if (j < nb && i < nb && i >= j) {
-        if (i == j) {
-          xv = 1.0 / a[j][j];
-        } else {
-          double s = 0.0;
-          for (int q = j; q < i; ++q) s = fma(a[i][q], Linv[q * NB + j], s);
-          xv = -s / a[i][i];
-        }
-      }
-      Linv[i * NB + j] = xv;
-    }
+  // Linv = L^-1 row by row in shared memory: Linv[i][j] (j < i) is kept
+  // transposed in the strict upper triangle a[j][i], its diagonal in dinv.
+  // Row i: Linv[i][j] = -dinv[i] sum_{q=j}^{i-1} L[i][q] Linv[q][j], four
+  // threads per column j (partial sums over q, combined by shuffles).
+  __shared__ double dinv[NB];
+  if (t < NB) dinv[t] = t < nb ? 1.0 / a[t][t] : 0.0;
+  __syncthreads();
+  const int j = t >> 2, part = t & 3;
+  for (int i = 1; i < nb; ++i) {
+    double s = 0.0;
+    if (j < i)
+      for (int q = j + part; q < i; q += 4) s = fma(a[i][q], q == j ? dinv[j] : a[j][q], s);
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    if (j < i && part == 0) a[j][i] = -dinv[i] * s;
+    __syncthreads();
+  }
+  for (int e = t; e < NB * NB; e += 256) {
+    const int r = e / NB, cc = e % NB;
+    double xv = 0.0;
+    if (r < nb && cc < nb && cc <= r) xv = cc == r ? dinv[r] : a[cc][r];
+    Linv[e] = xv;
   }
   for (int e = t; e < nb * nb; e += 256) {
     const int r = e / nb, cc = e % nb;
@@ -117,6 +123,27 @@ __global__ void norm_inf_kernel(const double* __restrict__ J, int m,
     s = warp_sum(s);
     if (lane == 0) atomicMax(out, (unsigned long long)__double_as_longlong(s));
   }
+}
+
+// X[kb .. kb+nb)[kb .. kb+nb) = Linv block b, for every diagonal block (one
+// block of threads per diagonal block).
+__global__ void place_diag_inverses(const double* __restrict__ Linv, int m,
+                                    double* __restrict__ X) {
+  const int b = blockIdx.x, k = b * NB, nb = min(NB, m - k);
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int r = e / nb, cc = e % nb;
+    X[(size_t)(k + r) * m + k + cc] = Linv[(size_t)b * NB * NB + r * NB + cc];
+  }
+}
+
+// max_c sum_r |X[r][c]| (one thread per column, coalesced across columns).
+__global__ void norm_one_kernel(const double* __restrict__ X, int m,
+                                unsigned long long* __restrict__ out) {
+  const int cidx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cidx >= m) return;
+  double s = 0.0;
+  for (int r = 0; r < m; ++r) s += fabs(X[(size_t)r * m + cidx]);
+  atomicMax(out, (unsigned long long)__double_as_longlong(s));
 }
 
 }  // namespace
@@ -204,6 +231,72 @@ int chol_solve_device(corr_context* c, const double* Lm, const double* Linv, int
                       &c->dres->status, s));
     c->launches += (r0 > 0) ? 2 : 1;
   }
+  return CORR_OK;
+}
+
+// X = L^-1 (m x m, ld m) for the factor of chol_factor_device (Lm, and the
+// inverses of its 64 x 64 diagonal blocks in Linv), by recursive blocked
+// inversion on 64-aligned splits:
+//   [[L11, 0], [L21, L22]]^-1 = [[X11, 0], [-X22 L21 X11, X22]].
+// T: scratch of m * m doubles.  The strict upper triangle of X is zero.
+int chol_inverse_device(corr_context* c, const double* Lm, const double* Linv, int m, double* X,
+                        double* T) {
+  const int nblk = (m + NB - 1) / NB;
+  cudaStream_t s = c->stream;
+  CORR_CUDA(cudaMemsetAsync(X, 0, (size_t)m * m * 8, s));
+  place_diag_inverses<<<nblk, 256, 0, s>>>(Linv, m, X);
+  CORR_CUDA(cudaGetLastError());
+  c->launches += 1;
+  struct Node {
+    int r0, n;
+  };
+  // post-order over the split tree (children before their parent)
+  std::vector<Node> order;
+  std::vector<std::pair<Node, bool>> stack{{{0, m}, false}};
+  while (!stack.empty()) {
+    auto [nd, expanded] = stack.back();
+    stack.pop_back();
+    if (nd.n <= NB) continue;
+    if (expanded) {
+      order.push_back(nd);
+      continue;
+    }
+    const int n1 = NB * (((nd.n + NB - 1) / NB + 1) / 2);
+    stack.push_back({nd, true});
+    stack.push_back({{nd.r0 + n1, nd.n - n1}, false});
+    stack.push_back({{nd.r0, n1}, false});
+  }
+  for (const Node& nd : order) {
+    const int n1 = NB * (((nd.n + NB - 1) / NB + 1) / 2), n2 = nd.n - n1;
+    const int r0 = nd.r0, r1 = nd.r0 + n1;
+    // T = L21 X11   (n2 x n1)
+    GemmF64 g = gemm_args(Lm + (size_t)r1 * m + r0, X + (size_t)r0 * m + r0, T, n2, n1, n1, m, m,
+                          n1, 0, 0);
+    CORR_TRY(gemm_f64(g, &c->dres->status, s));
+    // X21 = -X22 T
+    GemmF64 h = gemm_args(X + (size_t)r1 * m + r1, T, X + (size_t)r1 * m + r0, n2, n1, n2, m, n1,
+                          m, 0, 0);
+    h.alpha = -1.0;
+    CORR_TRY(gemm_f64(h, &c->dres->status, s));
+    c->launches += 2;
+  }
+  return CORR_OK;
+}
+
+// ||X||_1 ||X||_inf of an m x m matrix (scratch: 16 bytes of device memory).
+int chol_norm_one_inf(corr_context* c, void* scratch, const double* X, int m, double* out) {
+  unsigned long long* d = static_cast<unsigned long long*>(scratch);
+  CORR_CUDA(cudaMemsetAsync(d, 0, 2 * sizeof(*d), c->stream));
+  norm_one_kernel<<<(m + 255) / 256, 256, 0, c->stream>>>(X, m, d);
+  norm_inf_kernel<<<(m + 7) / 8, 256, 0, c->stream>>>(X, m, d + 1);
+  CORR_CUDA(cudaGetLastError());
+  unsigned long long h[2] = {0, 0};
+  CORR_CUDA(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  CORR_CUDA(cudaStreamSynchronize(c->stream));
+  c->launches += 2;
+  double v[2];
+  memcpy(v, h, sizeof(v));
+  *out = v[0] * v[1];
   return CORR_OK;
 }
 

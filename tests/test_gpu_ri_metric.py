@@ -120,12 +120,15 @@ def _oracle_from_3index(J, P3, mos, eps, nocc):
     return O.rimp2_energy(B, eps, nocc, N - nocc), ncut
 
 
+@pytest.mark.parametrize("prec", ["fp64", "split_fp16"])
 @pytest.mark.parametrize("kind", ["certified", "rank_deficient", "near_cutoff"])
-def test_from_3index_metric_paths(ctx, kind):
+def test_from_3index_metric_paths(ctx, kind, prec):
     """Energy from (P|mn) and J: a certified metric takes the Cholesky path
-    (chol.cu), a metric with eigenvalues at or below 10 tol lambda_max takes
-    the eigendecomposition with the reference's cutoff.  Both must give the
-    reference energy."""
+    (chol.cu; for the precision forms W = L^-1 by blocked inversion and the
+    tensor-core product), a metric with eigenvalues at or below 10 tol
+    lambda_max takes the eigendecomposition with the reference's cutoff.  All
+    must give the reference energy (the precision form within its digit
+    rounding, 2e-7 relative)."""
     X, N, nocc = 96, 22, 5
     spec = None
     if kind == "rank_deficient":
@@ -136,20 +139,24 @@ def test_from_3index_metric_paths(ctx, kind):
         spec = np.concatenate([np.geomspace(1.0, 1e-4, 95), [5e-10]])
     J, P3, mos, eps = _from_3index_case(X, N, nocc, 71, spec)
     (ess, eos, et), ncut_ref = _oracle_from_3index(J, P3, mos, eps, nocc)
-    e, ncut = ctx.rimp2_energy_from_3index(2 * nocc, mos, eps, J, P3, "fp64")
+    e, ncut = ctx.rimp2_energy_from_3index(2 * nocc, mos, eps, J, P3, prec)
     assert ncut == ncut_ref
     if kind == "rank_deficient":
         assert ncut == 16
     tol = {"certified": 1e-10, "rank_deficient": 1e-8, "near_cutoff": 1e-6}[kind]
+    if prec != "fp64":
+        tol = max(tol, 2e-7)
     assert abs(e.e_total - et) <= tol * abs(et), (e, et)
     assert abs(e.e_os - eos) <= tol * abs(eos)
 
 
+@pytest.mark.parametrize("prec", ["fp64", "split_fp16"])
 @pytest.mark.parametrize("X,N,nocc", [(64, 16, 3), (200, 30, 7), (650, 40, 9)])
-def test_from_3index_cholesky_sizes(ctx, X, N, nocc):
-    """Certified metrics of sizes around the 64-row block edges."""
+def test_from_3index_cholesky_sizes(ctx, X, N, nocc, prec):
+    """Certified metrics of sizes around the 64-row block edges (for the
+    precision forms: the recursive inversion's splits)."""
     J, P3, mos, eps = _from_3index_case(X, N, nocc, X + N)
     (ess, eos, et), ncut_ref = _oracle_from_3index(J, P3, mos, eps, nocc)
-    e, ncut = ctx.rimp2_energy_from_3index(2 * nocc, mos, eps, J, P3, "fp64")
+    e, ncut = ctx.rimp2_energy_from_3index(2 * nocc, mos, eps, J, P3, prec)
     assert ncut == ncut_ref == 0
-    assert abs(e.e_total - et) <= 1e-10 * abs(et)
+    assert abs(e.e_total - et) <= (1e-10 if prec == "fp64" else 2e-7) * abs(et)
