@@ -40,17 +40,22 @@ def test_fp64_matches_oracle(ctx, o, v, X, seed):
 
 @pytest.mark.parametrize("o,v,X,seed", SHAPES)
 # split_fp16 carries two FP16 digits (about 21 bits of each row's scale), so
-# shapes with a handful of terms see up to ~1e-6 relative; split_bf16 carries
-# three BF16 digits (21-27 bits).
-@pytest.mark.parametrize("prec,rel", [("split_fp16", 1e-6), ("split_bf16", 2e-7)])
-def test_split_matches_oracle(ctx, o, v, X, seed, prec, rel):
+# shapes with a handful of terms see up to ~3e-7 relative; split_bf16 carries
+# three BF16 digits (21-27 bits), up to ~4e-9.  Bounds: about 3x the largest
+# deviation measured over these shapes (E, E_OS; E_SS relative to E).
+@pytest.mark.parametrize("prec,rel,rel_ss", [("split_fp16", 9e-7, 2e-7),
+                                             ("split_bf16", 1.3e-8, 8e-9)])
+def test_split_matches_oracle(ctx, o, v, X, seed, prec, rel, rel_ss):
     B, eps = O.synth_rimp2(o, v, X, seed)
     ref = O.rimp2_energy(B, eps, o, v)
     got = ctx.rimp2_energy(B, eps, o, v, X, prec)
+    print(f"REL split_matches {prec} o={o} v={v} X={X}: "
+          f"{abs(got.e_total - ref[2]) / abs(ref[2]):.3e} {abs(got.e_os - ref[1]) / abs(ref[1]):.3e} "
+          f"{abs(got.e_ss - ref[0]) / abs(ref[2]):.3e}")
     assert abs(got.e_total - ref[2]) <= rel * abs(ref[2]), (prec, got, ref)
     assert abs(got.e_os - ref[1]) <= rel * abs(ref[1]), (prec, got, ref)
     # E_SS is a difference; bound it relative to the total
-    assert abs(got.e_ss - ref[0]) <= rel * abs(ref[2]), (prec, got, ref)
+    assert abs(got.e_ss - ref[0]) <= rel_ss * abs(ref[2]), (prec, got, ref)
 
 
 @pytest.mark.parametrize("o,v,X,seed", [
@@ -62,6 +67,8 @@ def test_split_fp16_row_statistics_forms(ctx, o, v, X, seed):
     B, eps = O.synth_rimp2(o, v, X, seed)
     ref = O.rimp2_energy(B, eps, o, v)
     got = ctx.rimp2_energy(B, eps, o, v, X, "split_fp16")
+    print(f"REL rowstat o={o} v={v} X={X}: {abs(got.e_total - ref[2]) / abs(ref[2]):.3e} "
+          f"{abs(got.e_ss - ref[0]) / abs(ref[2]):.3e}")
     assert abs(got.e_total - ref[2]) <= 1e-6 * abs(ref[2]), (got, ref)
     assert abs(got.e_ss - ref[0]) <= 1e-6 * abs(ref[2]), (got, ref)
 
@@ -75,7 +82,8 @@ def test_config2_full_size(ctx):
     assert _close(f64.e_total, ref[2], FP64_ABS, FP64_REL), (f64, ref)
     assert _close(f64.e_ss, ref[0], FP64_ABS, FP64_REL), (f64, ref)
     h16 = ctx.rimp2_energy(B, eps, o, v, X, "split_fp16")
-    assert abs(h16.e_total - ref[2]) <= 2e-7 * abs(ref[2]), (h16, ref)
+    print(f"REL config2 {abs(h16.e_total - ref[2]) / abs(ref[2]):.3e}")
+    assert abs(h16.e_total - ref[2]) <= 1e-7 * abs(ref[2]), (h16, ref)  # measured 3.1e-8
 
 
 def test_device_resident_inputs(ctx):
@@ -131,8 +139,11 @@ def test_split_wide_dynamic_range(ctx, prec):
     eps = np.concatenate([np.sort(r.uniform(-1.5, -0.3, o)), np.sort(r.uniform(0.05, 3.0, v))])
     ref = O.rimp2_energy(B, eps, o, v)
     got = ctx.rimp2_energy(B, eps, o, v, X, prec)
-    assert abs(got.e_total - ref[2]) <= 2e-7 * abs(ref[2]), (prec, got, ref)
-    assert abs(got.e_os - ref[1]) <= 2e-7 * abs(ref[1]), (prec, got, ref)
+    print(f"REL wide {prec}: {abs(got.e_total - ref[2]) / abs(ref[2]):.3e} "
+          f"{abs(got.e_os - ref[1]) / abs(ref[1]):.3e}")
+    rel = {"split_fp16": 3e-9, "split_bf16": 6e-11}[prec]  # measured 8.4e-10, 1.7e-11
+    assert abs(got.e_total - ref[2]) <= rel * abs(ref[2]), (prec, got, ref)
+    assert abs(got.e_os - ref[1]) <= rel * abs(ref[1]), (prec, got, ref)
 
 
 @pytest.mark.parametrize("o,v,X", [(3, 64, 40), (5, 150, 70), (7, 300, 90), (4, 192, 50),
