@@ -50,7 +50,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-count", type=int, default=256,
                     help="instances of the batched workload (256 by default)")
-    ap.add_argument("--workload", default="rimp2", choices=["rimp2", "batch256", "ri_pipeline"],
+    ap.add_argument("--workload", default="rimp2",
+                    choices=["rimp2", "batch256", "ri_pipeline", "cluster", "dgemm_tc"],
                     help="batch256: 256 uneven RI-MP2 instances in one batched launch; "
                          "ri_pipeline: time-to-E_corr from the 3-index integrals")
     ap.add_argument("--nbf", type=int, default=480, help="ri_pipeline: basis functions")
@@ -692,8 +693,116 @@ def run_pipeline(args):
     print(json.dumps(line), flush=True)
 
 
+def run_cluster(args):
+    """Config-3 time-to-E_corr from the basis, as one process runs it: (P|Q) and
+    (P|mu nu) on the GPU (corr_ri_integrals) for the 20-water cluster's shells,
+    then corr_rimp2_energy_from_3index in the precision form, per step; the
+    orbitals are the cluster's RHF orbitals (tests/golden)."""
+    import numpy as np
+    import torch
+
+    import corr_gb300
+
+    torch.cuda.set_device(0)
+    gold = os.path.join(ROOT, "tests", "golden")
+    sysd = np.load(os.path.join(gold, "systems.npz"))
+    basis = [corr_gb300.Basis(*(sysd[f"c3_{k}_{n}"]
+                                for n in ("l", "nprim", "poff", "center", "exps", "coefs")))
+             for k in ("obs", "aux")]
+    fx = np.load(os.path.join(gold, "config3_cluster.npz"))
+    mos = torch.from_numpy(fx["mos"]).cuda()
+    eps = torch.from_numpy(fx["eps"]).cuda()
+    ctx = corr_gb300.Context(0)
+    prec = args.precision if args.precision != "fp64" else "split_fp16"
+
+    def step():
+        J, P = ctx.ri_integrals(*basis)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        e, ncut = ctx.rimp2_energy_from_3index(200, mos, eps, J, P, prec)
+        return e, ncut, t1
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    steps = max(3, min(args.steps, 20))
+    tot, ints = [], []
+    for _ in range(steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e, ncut, t1 = step()
+        t2 = time.perf_counter()
+        tot.append((t2 - t0) * 1e3)
+        ints.append((t1 - t0) * 1e3)
+    ms = statistics.median(tot)
+    line = {
+        "metric": "RI-MP2 time-to-E_corr from the basis (20-water cluster)",
+        "value": ms, "unit": "ms", "n_gpus": 1, "steps": steps, "warmup": max(3, args.warmup),
+        "ms_per_step": ms, "higher_is_better": False,
+        "dtype": "bf16" if prec == "split_bf16" else "f16", "data": "molecular",
+        "config": {"workload": "20 H2O, def2-SVP/def2-SVP-RI, N=480 nocc=100 naux=1520, shells of "
+                               "tests/golden/systems.npz, RHF orbitals of config3_cluster.npz",
+                   "precision": prec, "metric_path": "cholesky" if ncut == 0 else f"jacobi, {ncut} cut"},
+        "integrals_ms": statistics.median(ints),
+        "pipeline_ms": ms - statistics.median(ints),
+        "energy": e.e_total,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_dgemm(args):
+    """The FP64-accurate digit GEMM (corr_dgemm_tc) on the (P|ia) transform's
+    shape for 304 auxiliary functions (M = 304 x 100 rows, N = 384, K = 480),
+    device operands, against the FP64-pipe GEMM (corr_dgemm) of the same call;
+    value = FP64-equivalent TFLOP/s of the whole call (slicing included)."""
+    import numpy as np
+    import torch
+
+    import corr_gb300
+
+    torch.cuda.set_device(0)
+    M, N, K = 30400, 384, 480
+    r = np.random.default_rng(5)
+    A = torch.from_numpy(r.standard_normal((M, K))).cuda()
+    B = torch.from_numpy(r.standard_normal((N, K))).cuda()
+    ctx = corr_gb300.Context(0)
+
+    def timed(tc, n):
+        for _ in range(max(3, args.warmup)):
+            C = ctx.dgemm(A, B, transb=True, tensor_cores=tc)
+        torch.cuda.synchronize()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record()
+        for _ in range(n):
+            C = ctx.dgemm(A, B, transb=True, tensor_cores=tc)
+        s1.record()
+        torch.cuda.synchronize()
+        return s0.elapsed_time(s1) / n, C
+
+    steps = max(3, min(args.steps, 50))
+    ms, C = timed(True, steps)
+    ms64, C64 = timed(False, 3)
+    flop = 2.0 * M * N * K
+    line = {
+        "metric": "FP64-accurate GEMM on the tensor cores, FP64-equivalent TFLOP/s",
+        "value": flop / (ms * 1e-3) / 1e12, "unit": "TFLOP/s", "n_gpus": 1, "steps": steps,
+        "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True,
+        "dtype": "f64 (bf16 digits)", "data": "synthetic",
+        "config": {"workload": f"C[{M}][{N}] = A[{M}][{K}] B[{N}][{K}]^T, normal random, seed 5"},
+        "fp64_pipe_gemm": {"ms": ms64, "tflops": flop / (ms64 * 1e-3) / 1e12,
+                           "speedup": ms64 / ms},
+        "max_abs_diff_vs_fp64_gemm": float((C - C64).abs().max()),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "cluster":
+        run_cluster(args)
+        return
+    if args.workload == "dgemm_tc":
+        run_dgemm(args)
+        return
     if args.workload == "batch256":
         run_batch(args)
         return

@@ -315,7 +315,7 @@ int chol_norm_one_inf(corr_context* c, void* scratch, const double* X, int m, do
 int chol_solve_device(corr_context* c, const double* Lm, const double* Linv, int m, double* P,
                       long long ncols, double* out);
 int ri_inv_sqrt_device(corr_context* c, void* ws, const double* J, int m, double tol,
-                       double* out, int* ncut);
+                       double* out, int* ncut, bool try_ns);
 }  // namespace corr
 
 extern "C" {
@@ -342,7 +342,7 @@ int corr_ri_metric_inv_sqrt(corr_context* c, int naux, const double* J, double t
   const double* d_j = static_cast<const double*>(stage_in(c, J, nj * 8, s_j));
   CORR_CHECK_ARG(d_j, "host-to-device copy failed");
   mark(c, 1);
-  CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, naux, tol, out, ncut));
+  CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, naux, tol, out, ncut, true));
   mark(c, 2);
   CORR_TRY(stage_out(c, jm12, out, nj * 8));
   return finish_results(c, 0);
@@ -377,7 +377,7 @@ int corr_calculate_ri(corr_context* c, int naux, int nroao, const double* J, con
   CORR_CHECK_ARG(d_j && d_p, "host-to-device copy failed");
   mark(c, 1);
   // ri.cc:50-69: J^-1/2 with the 1e-10 relative eigenvalue cutoff
-  CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, naux, 1e-10, jm, nullptr));
+  CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, naux, 1e-10, jm, nullptr, true));
   // ri.cc:102-103: BPQ = J^-1/2 (Q|mn)
   CORR_TRY(gemm_f64(gemm_args(jm, d_p, out, naux, (int)N2, naux, naux, N2, N2, 0, 0),
                     &c->dres->status, c->stream));
@@ -543,7 +543,7 @@ int corr_rimp2_energy_from_3index(corr_context* c, int nroe, int nroao, int naux
     if (factored) {
       if (ncut) *ncut = 0;
     } else {
-      CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, X, tol, jm, ncut));
+      CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, X, tol, jm, ncut, false));
       W = jm;
     }
   } else {
@@ -560,7 +560,7 @@ int corr_rimp2_energy_from_3index(corr_context* c, int nroe, int nroao, int naux
       CORR_TRY(chol_solve_device(c, Lm, Linv, X, pia, (long long)o * v, bia));
       if (ncut) *ncut = 0;
     } else {
-      CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, X, tol, jm, ncut));
+      CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, X, tol, jm, ncut, false));
       CORR_TRY(gemm_f64(gemm_args(jm, pia, bia, X, o * v, X, X, (long long)o * v,
                                   (long long)o * v, 0, 0),
                         &c->dres->status, c->stream));

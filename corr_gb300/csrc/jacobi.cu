@@ -853,14 +853,30 @@ int sym_eig_device(corr_context* c, void* ws, const double* Ain, int m, double* 
 // Eigen-decomposition + reference cutoff + assembly.  J, out: device pointers
 // (m x m).  Workspace carved from c->ws (caller already reserved
 // jacobi_workspace_bytes(m)).
+size_t ns_workspace_bytes(int m);
+int ri_inv_sqrt_ns(corr_context* c, void* ws, const double* J, int m, double tol, double* out,
+                   bool* done);
+
 size_t jacobi_workspace_bytes(int m) {
   const int n = m + (m & 1);
-  return (size_t)4 * n * n * 8 + (n >= kMixedMin ? f32_floats(n) * 4 : 0) + (size_t)n * 16 +
-         (size_t)kFrobBlocks * 16 + (size_t)8 * 256;
+  return std::max((size_t)4 * n * n * 8 + (n >= kMixedMin ? f32_floats(n) * 4 : 0) +
+                      (size_t)n * 16 + (size_t)kFrobBlocks * 16 + (size_t)8 * 256,
+                  ns_workspace_bytes(m));
 }
 
+// J^-1/2 with the reference's cutoff.  try_ns: first the certificate and, if
+// nothing can be cut, the Newton-Schulz iteration (invsqrt.cu); otherwise
+// (or if it does not converge) the eigendecomposition below.
 int ri_inv_sqrt_device(corr_context* c, void* ws, const double* J, int m, double tol,
-                       double* out, int* ncut) {
+                       double* out, int* ncut, bool try_ns) {
+  if (try_ns && m >= kMixedMin) {
+    bool done = false;
+    CORR_TRY(ri_inv_sqrt_ns(c, ws, J, m, tol, out, &done));
+    if (done) {
+      if (ncut) *ncut = 0;
+      return CORR_OK;
+    }
+  }
   const int n = m + (m & 1);
   Carver cw{ws, 0};
   const EigWork e = carve_eig(cw, n);
