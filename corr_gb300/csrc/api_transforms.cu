@@ -362,14 +362,16 @@ int corr_calculate_ri(corr_context* c, int naux, int nroao, const double* J, con
   if (!pdev) cv.take(np * 8);
   if (!odev) cv.take(np * 8);
   cv.take(nj * 8);
-  cv.take(jacobi_workspace_bytes(naux));
+  const size_t jwb = std::max(jacobi_workspace_bytes(naux),
+                              dgemm_tc_workspace(naux, (int)N2, naux));
+  cv.take(jwb);
   CORR_TRY(c->ws.reserve(cv.used));
   Carver w{c->ws.ptr, 0};
   void* s_j = jdev ? nullptr : w.take(nj * 8);
   void* s_p = pdev ? nullptr : w.take(np * 8);
   double* out = odev ? bpq : static_cast<double*>(w.take(np * 8));
   double* jm = static_cast<double*>(w.take(nj * 8));
-  void* jws = w.take(jacobi_workspace_bytes(naux));
+  void* jws = w.take(jwb);
   CORR_CUDA(cudaMemsetAsync(c->dres, 0, sizeof(ResultBlock), c->stream));
   mark(c, 0);
   const double* d_j = static_cast<const double*>(stage_in(c, J, nj * 8, s_j));
@@ -378,10 +380,19 @@ int corr_calculate_ri(corr_context* c, int naux, int nroao, const double* J, con
   mark(c, 1);
   // ri.cc:50-69: J^-1/2 with the 1e-10 relative eigenvalue cutoff
   CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, naux, 1e-10, jm, nullptr, true));
-  // ri.cc:102-103: BPQ = J^-1/2 (Q|mn)
-  CORR_TRY(gemm_f64(gemm_args(jm, d_p, out, naux, (int)N2, naux, naux, N2, N2, 0, 0),
-                    &c->dres->status, c->stream));
-  c->launches += 1;
+  // ri.cc:102-103: BPQ = J^-1/2 (Q|mn), on the FP64-accurate digit GEMM
+  // (rows P of J^-1/2 against the columns mn of (Q|mn) read as rows over Q)
+  DgemmTc g;
+  g.A = mat_view(jm, naux, 1);
+  g.B = mat_view(d_p, 1, N2);
+  g.C = out_view(out, N2, 1);
+  g.M = naux;
+  g.N = (int)N2;
+  g.K = naux;
+  g.alpha = 1.0;
+  g.accumulate = false;
+  g.a_lower = false;
+  CORR_TRY(dgemm_tc(c, g, jws));
   mark(c, 2);
   CORR_TRY(stage_out(c, bpq, out, np * 8));
   return finish_results(c, 0);
