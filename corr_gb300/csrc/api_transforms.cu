@@ -308,9 +308,9 @@ size_t jacobi_workspace_bytes(int m);
 size_t chol_workspace_bytes(int m);
 int chol_norm_inf(corr_context* c, void* scratch, const double* J, int m, double* out);
 int chol_factor_device(corr_context* c, void* ws, const double* J, int m, double shift,
-                       double** Lm_out, double** Linv_out, bool* ok);
+                       double** Lm_out, double** Linv_out, bool* ok, void* tc_ws);
 int chol_inverse_device(corr_context* c, const double* Lm, const double* Linv, int m, double* X,
-                        double* T);
+                        double* T, void* tc_ws);
 int chol_norm_one_inf(corr_context* c, void* scratch, const double* X, int m, double* out);
 int chol_solve_device(corr_context* c, const double* Lm, const double* Linv, int m, double* P,
                       long long ncols, double* out);
@@ -537,18 +537,20 @@ int corr_rimp2_energy_from_3index(corr_context* c, int nroe, int nroao, int naux
     // Certificate from W itself: lambda_min(J) = 1 / ||L^-1||_2^2 >=
     // 1 / (||L^-1||_1 ||L^-1||_inf); when that bound does not reach twice
     // the threshold, J - t I is factored as below.
-    if (jnorm > 0.0) CORR_TRY(chol_factor_device(c, jws, d_j, X, 0.0, &Lm, &Linv, &factored));
+    Carver r2 = w;
+    void* tcw = r2.take(dg_bytes - 2 * nj * 8 - 512);  // digit-GEMM workspace of region 2
+    double* T = static_cast<double*>(r2.take(nj * 8));
+    if (jnorm > 0.0)
+      CORR_TRY(chol_factor_device(c, jws, d_j, X, 0.0, &Lm, &Linv, &factored, tcw));
     if (factored) {
-      Carver r2 = w;
-      r2.take(dg_bytes - 2 * nj * 8 - 512);
-      double* T = static_cast<double*>(r2.take(nj * 8));
       W = static_cast<double*>(r2.take(nj * 8));
-      CORR_TRY(chol_inverse_device(c, Lm, Linv, X, W, T));
+      CORR_TRY(chol_inverse_device(c, Lm, Linv, X, W, T, tcw));
       double n1inf = 0.0;
       CORR_TRY(chol_norm_one_inf(c, jm, W, X, &n1inf));
       bool certified = n1inf > 0.0 && 1.0 / n1inf > 2.0 * 10.0 * tol * jnorm;
       if (!certified)
-        CORR_TRY(chol_factor_device(c, jws, d_j, X, 10.0 * tol * jnorm, &Lm, &Linv, &certified));
+        CORR_TRY(chol_factor_device(c, jws, d_j, X, 10.0 * tol * jnorm, &Lm, &Linv, &certified,
+                                    tcw));
       factored = certified;
     }
     if (factored) {
@@ -565,8 +567,9 @@ int corr_rimp2_energy_from_3index(corr_context* c, int nroe, int nroao, int naux
     // cutoff (ri.cc:50-69), applied to the (P|ia) matrix (2 X^2 o v flops).
     bool certified = false;
     if (jnorm > 0.0) CORR_TRY(chol_factor_device(c, jws, d_j, X, 10.0 * tol * jnorm, &Lm, &Linv,
-                                                 &certified));
-    if (certified) CORR_TRY(chol_factor_device(c, jws, d_j, X, 0.0, &Lm, &Linv, &factored));
+                                                 &certified, nullptr));
+    if (certified)
+      CORR_TRY(chol_factor_device(c, jws, d_j, X, 0.0, &Lm, &Linv, &factored, nullptr));
     if (factored) {
       CORR_TRY(chol_solve_device(c, Lm, Linv, X, pia, (long long)o * v, bia));
       if (ncut) *ncut = 0;

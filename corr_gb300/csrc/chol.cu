@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "dgemm_tc.h"
 #include "gemm_fp64.h"
 #include "kernels.h"
 
@@ -168,8 +169,11 @@ int chol_norm_inf(corr_context* c, void* scratch, const double* J, int m, double
   return CORR_OK;
 }
 
+// tc_ws: when non-null, the panel and trailing products run on the
+// FP64-accurate digit GEMM (dgemm_tc.cu) with that workspace
+// (dgemm_tc_workspace(m, m, NB) bytes); else on the FP64 GEMM.
 int chol_factor_device(corr_context* c, void* ws, const double* J, int m, double shift,
-                       double** Lm_out, double** Linv_out, bool* ok) {
+                       double** Lm_out, double** Linv_out, bool* ok, void* tc_ws) {
   const int nblk = (m + NB - 1) / NB;
   Carver w{ws, 0};
   double* A = static_cast<double*>(w.take((size_t)m * m * 8));
@@ -189,17 +193,41 @@ int chol_factor_device(corr_context* c, void* ws, const double* J, int m, double
     CORR_CUDA(cudaGetLastError());
     c->launches += 1;
     if (rem == 0) break;
-    // L21 = A21 L11^-T
-    GemmF64 g = gemm_args(A + (size_t)(k + nb) * m + k, Li, Lm + (size_t)(k + nb) * m + k, rem,
-                          nb, nb, m, NB, m, 0, 1);
-    CORR_TRY(gemm_f64(g, &c->dres->status, s));
-    // A22 -= L21 L21^T
     const double* P = Lm + (size_t)(k + nb) * m + k;
-    GemmF64 u = gemm_args(P, P, A + (size_t)(k + nb) * m + k + nb, rem, rem, nb, m, m, m, 0, 1);
-    u.alpha = -1.0;
-    u.beta = 1.0;
-    CORR_TRY(gemm_f64(u, &c->dres->status, s));
-    c->launches += 2;
+    if (tc_ws) {
+      // L21 = A21 L11^-T: rows of A21 against the rows of L11^-1
+      DgemmTc g;
+      g.A = mat_view(A + (size_t)(k + nb) * m + k, m, 1);
+      g.B = mat_view(Li, NB, 1);
+      g.C = out_view(Lm + (size_t)(k + nb) * m + k, m, 1);
+      g.M = rem;
+      g.N = nb;
+      g.K = nb;
+      g.alpha = 1.0;
+      g.accumulate = false;
+      g.a_lower = false;
+      CORR_TRY(dgemm_tc(c, g, tc_ws));
+      // A22 -= L21 L21^T
+      DgemmTc u = g;
+      u.A = mat_view(P, m, 1);
+      u.B = mat_view(P, m, 1);
+      u.C = out_view(A + (size_t)(k + nb) * m + k + nb, m, 1);
+      u.N = rem;
+      u.alpha = -1.0;
+      u.accumulate = true;
+      CORR_TRY(dgemm_tc(c, u, tc_ws));
+    } else {
+      // L21 = A21 L11^-T
+      GemmF64 g = gemm_args(A + (size_t)(k + nb) * m + k, Li, Lm + (size_t)(k + nb) * m + k, rem,
+                            nb, nb, m, NB, m, 0, 1);
+      CORR_TRY(gemm_f64(g, &c->dres->status, s));
+      // A22 -= L21 L21^T
+      GemmF64 u = gemm_args(P, P, A + (size_t)(k + nb) * m + k + nb, rem, rem, nb, m, m, m, 0, 1);
+      u.alpha = -1.0;
+      u.beta = 1.0;
+      CORR_TRY(gemm_f64(u, &c->dres->status, s));
+      c->launches += 2;
+    }
   }
   int h = 0;
   CORR_CUDA(cudaMemcpyAsync(&h, fail, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -240,7 +268,7 @@ int chol_solve_device(corr_context* c, const double* Lm, const double* Linv, int
 //   [[L11, 0], [L21, L22]]^-1 = [[X11, 0], [-X22 L21 X11, X22]].
 // T: scratch of m * m doubles.  The strict upper triangle of X is zero.
 int chol_inverse_device(corr_context* c, const double* Lm, const double* Linv, int m, double* X,
-                        double* T) {
+                        double* T, void* tc_ws) {
   const int nblk = (m + NB - 1) / NB;
   cudaStream_t s = c->stream;
   CORR_CUDA(cudaMemsetAsync(X, 0, (size_t)m * m * 8, s));
@@ -269,16 +297,40 @@ int chol_inverse_device(corr_context* c, const double* Lm, const double* Linv, i
   for (const Node& nd : order) {
     const int n1 = NB * (((nd.n + NB - 1) / NB + 1) / 2), n2 = nd.n - n1;
     const int r0 = nd.r0, r1 = nd.r0 + n1;
-    // T = L21 X11   (n2 x n1)
-    GemmF64 g = gemm_args(Lm + (size_t)r1 * m + r0, X + (size_t)r0 * m + r0, T, n2, n1, n1, m, m,
-                          n1, 0, 0);
-    CORR_TRY(gemm_f64(g, &c->dres->status, s));
-    // X21 = -X22 T
-    GemmF64 h = gemm_args(X + (size_t)r1 * m + r1, T, X + (size_t)r1 * m + r0, n2, n1, n2, m, n1,
-                          m, 0, 0);
-    h.alpha = -1.0;
-    CORR_TRY(gemm_f64(h, &c->dres->status, s));
-    c->launches += 2;
+    if (tc_ws && n1 >= 4 * NB) {
+      // T = L21 X11: rows of L21 against the columns of X11 (read as rows over k)
+      DgemmTc g;
+      g.A = mat_view(Lm + (size_t)r1 * m + r0, m, 1);
+      g.B = mat_view(X + (size_t)r0 * m + r0, 1, m);
+      g.C = out_view(T, n1, 1);
+      g.M = n2;
+      g.N = n1;
+      g.K = n1;
+      g.alpha = 1.0;
+      g.accumulate = false;
+      g.a_lower = false;
+      CORR_TRY(dgemm_tc(c, g, tc_ws));
+      // X21 = -X22 T (X22 lower triangular)
+      DgemmTc h = g;
+      h.A = mat_view(X + (size_t)r1 * m + r1, m, 1);
+      h.B = mat_view(T, 1, n1);
+      h.C = out_view(X + (size_t)r1 * m + r0, m, 1);
+      h.K = n2;
+      h.alpha = -1.0;
+      h.a_lower = true;
+      CORR_TRY(dgemm_tc(c, h, tc_ws));
+    } else {
+      // T = L21 X11   (n2 x n1)
+      GemmF64 g = gemm_args(Lm + (size_t)r1 * m + r0, X + (size_t)r0 * m + r0, T, n2, n1, n1, m,
+                            m, n1, 0, 0);
+      CORR_TRY(gemm_f64(g, &c->dres->status, s));
+      // X21 = -X22 T
+      GemmF64 h = gemm_args(X + (size_t)r1 * m + r1, T, X + (size_t)r1 * m + r0, n2, n1, n2, m,
+                            n1, m, 0, 0);
+      h.alpha = -1.0;
+      CORR_TRY(gemm_f64(h, &c->dres->status, s));
+      c->launches += 2;
+    }
   }
   return CORR_OK;
 }

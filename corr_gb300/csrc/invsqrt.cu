@@ -32,7 +32,7 @@ namespace corr {
 
 int chol_norm_inf(corr_context* c, void* scratch, const double* J, int m, double* out);
 int chol_factor_device(corr_context* c, void* ws, const double* J, int m, double shift,
-                       double** Lm_out, double** Linv_out, bool* ok);
+                       double** Lm_out, double** Linv_out, bool* ok, void* tc_ws);
 size_t chol_workspace_bytes(int m);
 
 namespace {
@@ -124,7 +124,7 @@ int ri_inv_sqrt_ns(corr_context* c, void* ws, const double* J, int m, double tol
   double *Lm = nullptr, *Linv = nullptr;
   bool certified = false;
   const double t = 10.0 * tol * jinf;
-  CORR_TRY(chol_factor_device(c, front, J, m, t, &Lm, &Linv, &certified));
+  CORR_TRY(chol_factor_device(c, front, J, m, t, &Lm, &Linv, &certified, dws));
   if (!certified) return CORR_OK;
   sumsq_kernel<<<kSqBlocks, 256, 0, s>>>(J, (long long)mm, part);
   CORR_CUDA(cudaGetLastError());
