@@ -177,6 +177,45 @@ __device__ __forceinline__ void hermite_e(double a, double b, double Xab, double
 #undef EIDX
 }
 
+// As hermite_e, from the pair's precomputed quantities: e0 = exp(-ab/p X^2)
+// in this dimension, Xpa = P - A, Xpb = P - B, h = 1/(2p).
+template <int LA, int LB>
+__device__ __forceinline__ void hermite_e_pre(double e0, double Xpa, double Xpb, double h,
+                                              double* E) {
+  constexpr int NT = LA + LB + 1;
+#define EIDX(i, j, t) (((i) * (LB + 1) + (j)) * NT + (t))
+#pragma unroll
+  for (int k = 0; k < (LA + 1) * (LB + 1) * NT; ++k) E[k] = 0.0;
+  E[EIDX(0, 0, 0)] = e0;
+#pragma unroll
+  for (int i = 0; i <= LA; ++i)
+#pragma unroll
+    for (int j = 0; j <= LB; ++j) {
+      if (i == 0 && j == 0) continue;
+#pragma unroll
+      for (int t = 0; t <= i + j; ++t) {
+        double v;
+        if (i > 0) {
+          v = Xpa * E[EIDX(i - 1, j, t)];
+          if (t > 0) v += h * E[EIDX(i - 1, j, t - 1)];
+          if (t + 1 <= i - 1 + j) v += (t + 1) * E[EIDX(i - 1, j, t + 1)];
+        } else {
+          v = Xpb * E[EIDX(i, j - 1, t)];
+          if (t > 0) v += h * E[EIDX(i, j - 1, t - 1)];
+          if (t + 1 <= i + j - 1) v += (t + 1) * E[EIDX(i, j - 1, t + 1)];
+        }
+        E[EIDX(i, j, t)] = v;
+      }
+    }
+#undef EIDX
+}
+
+// Per orbital primitive pair (host-computed): p = a + b, the centre P, the
+// per-dimension Gaussian factors exp(-ab/p X_AB^2), c_a c_b / p and 1/(2p).
+struct PairData {
+  double p, px, py, pz, ex, ey, ez, cdp, h;
+};
+
 struct Basis3 {
   const ShellD* aux;   // bra shells (the auxiliary basis)
   const int* alist;    // bra shells of this class
@@ -185,6 +224,9 @@ struct Basis3 {
   const int2* plist;   // ket shell pairs (c, d) of this class; d < 0: exponent-0 s partner
   const int2* prange;  // per ket pair: its primitive pairs pp[x .. y)
   const ushort2* pp;   // (primitive of c, primitive of d) that pass the screening
+  const PairData* ppd; // their precomputed data (same index)
+  const double* arq;   // per auxiliary primitive: c / gamma
+  const double* ahq;   // per auxiliary primitive: 1 / (2 gamma)
   int nplist;
   const double* aexp;  // primitives of the bra basis (coefficients include the
   const double* acof;  // primitive normalisation)
@@ -222,27 +264,24 @@ __global__ void __launch_bounds__(128) eri3_kernel(Basis3 g) {
     (void)npd;
     const int2 rg = g.prange[ki];
     for (int q = rg.x; q < rg.y; ++q) {
-        const int ic = g.pp[q].x, id = g.pp[q].y;
-        const double a = g.oexp[sc.poff + ic];
-        const double b = has_d ? g.oexp[sd.poff + id] : 0.0;
-        const double ccd = g.ocof[sc.poff + ic] * (has_d ? g.ocof[sd.poff + id] : 1.0);
-        const double p = a + b;
-        const double Px = (a * sc.x + b * sd.x) / p, Py = (a * sc.y + b * sd.y) / p,
-                     Pz = (a * sc.z + b * sd.z) / p;
+        const PairData pd = g.ppd[q];
+        const double p = pd.p, Px = pd.px, Py = pd.py, Pz = pd.pz;
         double Ex[(LC + 1) * (LD + 1) * (LCD + 1)], Ey[(LC + 1) * (LD + 1) * (LCD + 1)],
             Ez[(LC + 1) * (LD + 1) * (LCD + 1)];
-        hermite_e<LC, LD>(a, b, Xcd, Ex);
-        hermite_e<LC, LD>(a, b, Ycd, Ey);
-        hermite_e<LC, LD>(a, b, Zcd, Ez);
+        hermite_e_pre<LC, LD>(pd.ex, Px - sc.x, Px - sd.x, pd.h, Ex);
+        hermite_e_pre<LC, LD>(pd.ey, Py - sc.y, Py - sd.y, pd.h, Ey);
+        hermite_e_pre<LC, LD>(pd.ez, Pz - sc.z, Pz - sd.z, pd.h, Ez);
+        (void)Xcd;
+        (void)Ycd;
+        (void)Zcd;
         for (int ip = 0; ip < sp.nprim; ++ip) {
           const double gq = g.aexp[sp.poff + ip];
-          const double cq = g.acof[sp.poff + ip];
           // bra Hermite coefficients of a single Gaussian: EP[k][tau], same in x, y, z
           double EP[(LP + 1) * (LP + 1)];
 #pragma unroll
           for (int k = 0; k < (LP + 1) * (LP + 1); ++k) EP[k] = 0.0;
           EP[0] = 1.0;
-          const double hq = 0.5 / gq;
+          const double hq = g.ahq[sp.poff + ip];
 #pragma unroll
           for (int k = 1; k <= LP; ++k)
 #pragma unroll
@@ -252,12 +291,13 @@ __global__ void __launch_bounds__(128) eri3_kernel(Basis3 g) {
               if (t + 1 <= k - 1) v += (t + 1) * EP[(k - 1) * (LP + 1) + t + 1];
               EP[k * (LP + 1) + t] = v;
             }
-          const double alpha = gq * p / (gq + p);
+          const double rs = rsqrt(gq + p);          // (gq + p)^-1/2
+          const double alpha = gq * p * (rs * rs);  // gq p / (gq + p)
           double Rbuf[2][tuv_count(L)];  // R^0_tuv ends in Rbuf[0]
           hermite_r<L>(alpha, sp.x - Px, sp.y - Py, sp.z - Pz, Rbuf);
           const double* R = Rbuf[0];
           // 2 pi^(5/2) / (p q sqrt(p + q)) times the contraction coefficients
-          const double pref = 34.986836655249725 / (gq * p * sqrt(gq + p)) * cq * ccd;
+          const double pref = 34.986836655249725 * g.arq[sp.poff + ip] * pd.cdp * rs;
           // ket Cartesian pair (kc, kd): G[tuv] = sum_{tau nu phi} (-1)^(tau+nu+phi)
           // E^cd_tau E^cd_nu E^cd_phi R_{t+tau, u+nu, v+phi} over the bra orders
           // t+u+v <= LP, then the bra Cartesian components.  Run-time loops
@@ -597,9 +637,15 @@ extern "C" int corr_ri_integrals(corr_context* c, const corr_basis* obs, const c
   // pairs whose Schwarz factor can reach kScreen (see screen_pairs)
   std::vector<std::vector<int2>> prange3(9), prange2(kLmax + 1);
   std::vector<ushort2> pp;
+  std::vector<PairData> ppd;
   for (int s = 0; s < (int)ha.sh.size(); ++s) {
     const int b = (int)pp.size();
-    for (int k = 0; k < ha.sh[s].nprim; ++k) pp.push_back(make_ushort2((unsigned short)k, 0));
+    for (int k = 0; k < ha.sh[s].nprim; ++k) {
+      pp.push_back(make_ushort2((unsigned short)k, 0));
+      const ShellD& A = ha.sh[s];
+      const double a = ha.exps[A.poff + k];
+      ppd.push_back(PairData{a, A.x, A.y, A.z, 1.0, 1.0, 1.0, ha.cofs[A.poff + k] / a, 0.5 / a});
+    }
     plist2[ha.sh[s].l].push_back(make_int2(s, -1));
     prange2[ha.sh[s].l].push_back(make_int2(b, (int)pp.size()));
   }
@@ -612,6 +658,18 @@ extern "C" int corr_ri_integrals(corr_context* c, const corr_basis* obs, const c
         if (ho.sh[x].l < ho.sh[y].l) std::swap(x, y);  // lc >= ld
         const int b = (int)pp.size();
         screen_pairs(ho, x, y, saux, &pp);
+        for (int q = b; q < (int)pp.size(); ++q) {
+          const ShellD& A = ho.sh[x];
+          const ShellD& B = ho.sh[y];
+          const double a = ho.exps[A.poff + pp[q].x], bb = ho.exps[B.poff + pp[q].y];
+          const double pe = a + bb, mu = a * bb / pe;
+          const double dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
+          ppd.push_back(PairData{pe, (a * A.x + bb * B.x) / pe, (a * A.y + bb * B.y) / pe,
+                                 (a * A.z + bb * B.z) / pe, std::exp(-mu * dx * dx),
+                                 std::exp(-mu * dy * dy), std::exp(-mu * dz * dz),
+                                 ho.cofs[A.poff + pp[q].x] * ho.cofs[B.poff + pp[q].y] / pe,
+                                 0.5 / pe});
+        }
         pairs_all += (long long)ho.sh[x].nprim * ho.sh[y].nprim;
         pairs_kept += (long long)pp.size() - b;
         if ((int)pp.size() == b) continue;  // every integral of the pair is below the threshold
@@ -645,8 +703,11 @@ extern "C" int corr_ri_integrals(corr_context* c, const corr_basis* obs, const c
     p[13] = w.take(bytes_of(np2, 8));
     p[14] = pmn ? w.take(bytes_of(np3, 8)) : nullptr;
     p[15] = w.take(bytes_of(pp.size(), 4));
+    p[16] = w.take(bytes_of(ppd.size(), sizeof(PairData)));
+    p[17] = w.take(bytes_of(ha.exps.size(), 8));
+    p[18] = w.take(bytes_of(ha.exps.size(), 8));
   };
-  void* p[16];
+  void* p[19];
   Carver cv{nullptr, 0};
   plan(cv, p);
   CORR_TRY(c->ws.reserve(cv.used));
@@ -686,6 +747,14 @@ extern "C" int corr_ri_integrals(corr_context* c, const corr_basis* obs, const c
   CORR_TRY(up(p[5], p2flat.data(), p2flat.size() * 8));
   CORR_TRY(up(p[13], r2flat.data(), r2flat.size() * 8));
   CORR_TRY(up(p[15], pp.data(), pp.size() * 4));
+  CORR_TRY(up(p[16], ppd.data(), ppd.size() * sizeof(PairData)));
+  std::vector<double> arq(ha.exps.size()), ahq(ha.exps.size());
+  for (size_t k = 0; k < ha.exps.size(); ++k) {
+    arq[k] = ha.cofs[k] / ha.exps[k];
+    ahq[k] = 0.5 / ha.exps[k];
+  }
+  CORR_TRY(up(p[17], arq.data(), arq.size() * 8));
+  CORR_TRY(up(p[18], ahq.data(), ahq.size() * 8));
   if (pmn) {
     CORR_TRY(up(p[14], r3flat.data(), r3flat.size() * 8));
     CORR_TRY(up(p[6], ho.sh.data(), ho.sh.size() * sizeof(ShellD)));
@@ -779,6 +848,9 @@ extern "C" int corr_ri_integrals(corr_context* c, const corr_basis* obs, const c
     g.aexp = static_cast<const double*>(p[1]);
     g.acof = static_cast<const double*>(p[2]);
     g.anorm = static_cast<const double*>(p[3]);
+    g.ppd = static_cast<const PairData*>(p[16]);
+    g.arq = static_cast<const double*>(p[17]);
+    g.ahq = static_cast<const double*>(p[18]);
     if (J) {  // (P|Q): the ket is the auxiliary basis with an exponent-0 s partner
       for (int lc = 0; lc <= kLmax; ++lc) {
         Basis3 h = g;
