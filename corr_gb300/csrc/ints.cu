@@ -812,11 +812,33 @@ extern "C" int corr_ri_integrals(corr_context* c, const corr_basis* obs, const c
     need = (need + 1023) / 1024 * 1024 + 1024;
     if (have < need) CORR_CUDA(cudaDeviceSetLimit(cudaLimitStackSize, need));
   }
+  // The classes write disjoint blocks of J and (P|mu nu): they run on four
+  // side streams forked from (and joined back into) the context stream, so
+  // the tails of the large classes overlap the small ones.
+  constexpr int kSide = 4;
+  struct Side {
+    cudaStream_t st[kSide] = {};
+    cudaEvent_t ev[kSide + 1] = {};
+    ~Side() {
+      for (cudaStream_t x : st)
+        if (x) cudaStreamDestroy(x);
+      for (cudaEvent_t x : ev)
+        if (x) cudaEventDestroy(x);
+    }
+  } side;
+  for (int k = 0; k < kSide; ++k) {
+    CORR_CUDA(cudaStreamCreateWithFlags(&side.st[k], cudaStreamNonBlocking));
+    CORR_CUDA(cudaEventCreateWithFlags(&side.ev[k], cudaEventDisableTiming));
+  }
+  CORR_CUDA(cudaEventCreateWithFlags(&side.ev[kSide], cudaEventDisableTiming));
+  CORR_CUDA(cudaEventRecord(side.ev[kSide], c->stream));
+  for (int k = 0; k < kSide; ++k) CORR_CUDA(cudaStreamWaitEvent(side.st[k], side.ev[kSide], 0));
+  int nlaunch = 0;
   auto launch = [&](Kern k, Basis3 g, int lp, int lc, int ld) -> int {
     const long long work = (long long)g.nalist * g.nplist;
     if (work <= 0) return CORR_OK;
     const int grid = (int)std::min<long long>((work + 127) / 128, (long long)c->sms * 32);
-    k<<<grid, 128, 0, c->stream>>>(g);
+    k<<<grid, 128, 0, side.st[nlaunch++ % kSide]>>>(g);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
       cudaFuncAttributes fa{};
@@ -886,6 +908,10 @@ extern "C" int corr_ri_integrals(corr_context* c, const corr_basis* obs, const c
           CORR_TRY(launch(class_kernel(lp, lc, ld), h, lp, lc, ld));
         }
     }
+  }
+  for (int k = 0; k < kSide; ++k) {
+    CORR_CUDA(cudaEventRecord(side.ev[k], side.st[k]));
+    CORR_CUDA(cudaStreamWaitEvent(c->stream, side.ev[k], 0));
   }
   mark(c, 2);
   if (J && !jdev) CORR_TRY(stage_out(c, J, Jout, (size_t)X * X * 8));
