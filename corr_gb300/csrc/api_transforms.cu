@@ -307,6 +307,36 @@ namespace corr {
 size_t jacobi_workspace_bytes(int m);
 size_t chol_workspace_bytes(int m);
 int chol_norm_inf(corr_context* c, void* scratch, const double* J, int m, double* out);
+// A side stream forked from and joined back into a stream (events), and a
+// scoped switch of the context's stream (restored on every exit path).
+struct SideStream {
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  int fork(cudaStream_t from) {
+    CORR_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : ev) CORR_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    CORR_CUDA(cudaEventRecord(ev[0], from));
+    CORR_CUDA(cudaStreamWaitEvent(st, ev[0], 0));
+    return CORR_OK;
+  }
+  int join(cudaStream_t into) {
+    CORR_CUDA(cudaEventRecord(ev[1], st));
+    CORR_CUDA(cudaStreamWaitEvent(into, ev[1], 0));
+    return CORR_OK;
+  }
+  ~SideStream() {
+    if (st) cudaStreamDestroy(st);
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+};
+struct StreamSwap {
+  corr_context* c;
+  cudaStream_t saved;
+  StreamSwap(corr_context* ctx, cudaStream_t s) : c(ctx), saved(ctx->stream) { c->stream = s; }
+  ~StreamSwap() { c->stream = saved; }
+};
+
 int chol_factor_device(corr_context* c, void* ws, const double* J, int m, double shift,
                        double** Lm_out, double** Linv_out, bool* ok, void* tc_ws);
 int chol_inverse_device(corr_context* c, const double* Lm, const double* Linv, int m, double* X,
@@ -473,10 +503,12 @@ int corr_rimp2_energy_from_3index(corr_context* c, int nroe, int nroao, int naux
   plan(cv, &sm, &se, &sj, &sp, &pia, &bia, &jm, &biq, &jws);
   // Region 2, reused: the digit planes of the tensor-core contractions (and
   // the identity that becomes L^-1), then the energy's scratch.
-  const size_t dg_bytes =
+  const size_t ws_main =
       tc ? std::max(std::max(dgemm_tc_workspace(X * N, o, N), dgemm_tc_workspace(X * o, v, N)),
-                    dgemm_tc_workspace(X, o * v, X)) + 2 * nj * 8 + 512
+                    dgemm_tc_workspace(X, o * v, X))
          : 0;
+  const size_t ws_metric = tc ? dgemm_tc_workspace(X, X, X) : 0;
+  const size_t dg_bytes = tc ? ws_main + ws_metric + 2 * nj * 8 + 1024 : 0;
   CORR_TRY(c->ws.reserve(cv.used + std::max(dg_bytes, energy_scratch_bytes(c, o, v, X, precision))));
   Carver w{c->ws.ptr, 0};
   plan(w, &sm, &se, &sj, &sp, &pia, &bia, &jm, &biq, &jws);
@@ -488,9 +520,21 @@ int corr_rimp2_energy_from_3index(corr_context* c, int nroe, int nroao, int naux
   const double* d_p = static_cast<const double*>(stage_in(c, pmn, np * 8, sp));
   CORR_CHECK_ARG(d_m && d_e && d_j && d_p, "host-to-device copy failed");
   // (P|ia) = C_occ (P|mu nu) C_vir^T  (the transform_ri contractions, ri.cc:147-172)
+  const double tol = 1e-10;
+  double jnorm = 0.0;
+  double *Lm = nullptr, *Linv = nullptr;
+  bool factored = false;
   if (tc) {
     Carver r2 = w;
-    void* dws = r2.take(dg_bytes);
+    void* dws = r2.take(ws_main);
+    void* mws = r2.take(ws_metric);
+    double* T = static_cast<double*>(r2.take(nj * 8));
+    double* W = static_cast<double*>(r2.take(nj * 8));
+    // The metric stage does not depend on the transform: it runs on a side
+    // stream (its own digit-GEMM workspace) while the transform's products
+    // run on the context stream, and is joined before B = W (P|ia).
+    SideStream side;
+    CORR_TRY(side.fork(c->stream));
     // (P|i nu): rows (P, nu) of (P|mu nu) (symmetric in mu nu) against the
     // occupied rows of C, written in the [P][i][nu] layout
     DgemmTc g1;
@@ -512,6 +556,47 @@ int corr_rimp2_energy_from_3index(corr_context* c, int nroe, int nroao, int naux
     g2.M = X * o;
     g2.N = v;
     CORR_TRY(dgemm_tc(c, g2, dws));
+    {
+      StreamSwap onside(c, side.st);
+      // The metric (ri.cc:50-69): one factorisation J = L L^T and W = L^-1
+      // (recursive blocked inversion).  Certificate from W itself:
+      // lambda_min(J) = 1 / ||L^-1||_2^2 >= 1 / (||L^-1||_1 ||L^-1||_inf);
+      // when that bound does not reach twice the threshold, J - t I is
+      // factored (chol.cu); without a certificate, J^-1/2 with the cutoff.
+      CORR_TRY(chol_norm_inf(c, jm, d_j, X, &jnorm));
+      if (jnorm > 0.0)
+        CORR_TRY(chol_factor_device(c, jws, d_j, X, 0.0, &Lm, &Linv, &factored, mws));
+      if (factored) {
+        CORR_TRY(chol_inverse_device(c, Lm, Linv, X, W, T, mws));
+        double n1inf = 0.0;
+        CORR_TRY(chol_norm_one_inf(c, jm, W, X, &n1inf));
+        bool certified = n1inf > 0.0 && 1.0 / n1inf > 2.0 * 10.0 * tol * jnorm;
+        if (!certified)
+          CORR_TRY(chol_factor_device(c, jws, d_j, X, 10.0 * tol * jnorm, &Lm, &Linv,
+                                      &certified, mws));
+        factored = certified;
+      }
+      if (factored) {
+        if (ncut) *ncut = 0;
+      } else {
+        CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, X, tol, jm, ncut, false));
+        W = jm;
+      }
+    }
+    CORR_TRY(side.join(c->stream));
+    // B[Q][ia] = sum_P W[Q][P] (P|ia): rows Q of W against the columns ia of
+    // (P|ia) read as rows over P
+    DgemmTc g3;
+    g3.A = mat_view(W, X, 1);
+    g3.B = mat_view(pia, 1, (long long)o * v);
+    g3.C = out_view(bia, (long long)o * v, 1);
+    g3.M = X;
+    g3.N = o * v;
+    g3.K = X;
+    g3.alpha = 1.0;
+    g3.accumulate = false;
+    g3.a_lower = factored;
+    CORR_TRY(dgemm_tc(c, g3, dws));
   } else {
     GemmF64 g1 = gemm_args(d_m, d_p, biq, o, N, N, N, N, N, 0, 0);
     g1.sb = (long long)N * N;
@@ -520,51 +605,12 @@ int corr_rimp2_energy_from_3index(corr_context* c, int nroe, int nroao, int naux
     CORR_TRY(gemm_f64(g1, &c->dres->status, c->stream));
     CORR_TRY(gemm_f64(gemm_args(biq, d_m + (size_t)o * N, pia, X * o, v, N, N, N, v, 0, 1),
                       &c->dres->status, c->stream));
-  }
-  // The metric.  The energy sees J only through J^-1 = W^T W: when the
-  // reference's cutoff (ri.cc:56-66, lambda/lambda_max < 1e-10) provably cuts
-  // nothing -- J - 10 tol ||J||_inf I is positive definite -- W = L^-1 from a
-  // Cholesky factorisation (chol.cu); otherwise W = J^-1/2 with the cutoff
-  // (ri.cc:50-69), applied to the (P|ia) matrix (2 X^2 o v flops).
-  const double tol = 1e-10;
-  double jnorm = 0.0;
-  CORR_TRY(chol_norm_inf(c, jm, d_j, X, &jnorm));
-  double *Lm = nullptr, *Linv = nullptr;
-  double* W = nullptr;  // the explicit metric factor of the tensor-core product
-  bool factored = false;
-  if (tc) {
-    // One factorisation J = L L^T and W = L^-1 (recursive blocked inversion).
-    // Certificate from W itself: lambda_min(J) = 1 / ||L^-1||_2^2 >=
-    // 1 / (||L^-1||_1 ||L^-1||_inf); when that bound does not reach twice
-    // the threshold, J - t I is factored as below.
-    Carver r2 = w;
-    void* tcw = r2.take(dg_bytes - 2 * nj * 8 - 512);  // digit-GEMM workspace of region 2
-    double* T = static_cast<double*>(r2.take(nj * 8));
-    if (jnorm > 0.0)
-      CORR_TRY(chol_factor_device(c, jws, d_j, X, 0.0, &Lm, &Linv, &factored, tcw));
-    if (factored) {
-      W = static_cast<double*>(r2.take(nj * 8));
-      CORR_TRY(chol_inverse_device(c, Lm, Linv, X, W, T, tcw));
-      double n1inf = 0.0;
-      CORR_TRY(chol_norm_one_inf(c, jm, W, X, &n1inf));
-      bool certified = n1inf > 0.0 && 1.0 / n1inf > 2.0 * 10.0 * tol * jnorm;
-      if (!certified)
-        CORR_TRY(chol_factor_device(c, jws, d_j, X, 10.0 * tol * jnorm, &Lm, &Linv, &certified,
-                                    tcw));
-      factored = certified;
-    }
-    if (factored) {
-      if (ncut) *ncut = 0;
-    } else {
-      CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, X, tol, jm, ncut, false));
-      W = jm;
-    }
-  } else {
     // The metric.  The energy sees J only through J^-1 = W^T W: when the
     // reference's cutoff (ri.cc:56-66, lambda/lambda_max < 1e-10) provably
     // cuts nothing -- J - 10 tol ||J||_inf I is positive definite -- W = L^-1
     // from a Cholesky factorisation (chol.cu); otherwise W = J^-1/2 with the
     // cutoff (ri.cc:50-69), applied to the (P|ia) matrix (2 X^2 o v flops).
+    CORR_TRY(chol_norm_inf(c, jm, d_j, X, &jnorm));
     bool certified = false;
     if (jnorm > 0.0) CORR_TRY(chol_factor_device(c, jws, d_j, X, 10.0 * tol * jnorm, &Lm, &Linv,
                                                  &certified, nullptr));
@@ -580,23 +626,6 @@ int corr_rimp2_energy_from_3index(corr_context* c, int nroe, int nroao, int naux
                         &c->dres->status, c->stream));
       c->launches += 1;
     }
-  }
-  if (tc) {
-    // B[Q][ia] = sum_P W[Q][P] (P|ia): rows Q of W against the columns ia of
-    // (P|ia) read as rows over P
-    Carver r2 = w;
-    void* dws = r2.take(dg_bytes - 2 * nj * 8 - 512);
-    DgemmTc g3;
-    g3.A = mat_view(W, X, 1);
-    g3.B = mat_view(pia, 1, (long long)o * v);
-    g3.C = out_view(bia, (long long)o * v, 1);
-    g3.M = X;
-    g3.N = o * v;
-    g3.K = X;
-    g3.alpha = 1.0;
-    g3.accumulate = false;
-    g3.a_lower = factored;
-    CORR_TRY(dgemm_tc(c, g3, dws));
   }
   c->launches += 2;
   // energy on the device-resident B; its scratch is carved after region 1
