@@ -140,13 +140,16 @@ class Context:
                                               _ptr(bia), _ptr(eps), _prec(precision),
                                               _ptr(out)))
 
-    def rimp2_gradient(self, bia, eps, nocc, nvir, naux, dbia=None, deps=None):
-        """(E, dE/dB, dE/deps) of the RI-MP2 energy, FP64."""
+    def rimp2_gradient(self, bia, eps, nocc, nvir, naux, dbia=None, deps=None,
+                       tensor_cores=False):
+        """(E, dE/dB, dE/deps) of the RI-MP2 energy: FP64 (DMMA panels and the
+        FP64 GEMM), or with tensor_cores the digit-GEMM form (FP64-accurate)."""
         dbia = self._out(bia, tuple(bia.shape), dbia)
         deps = self._out(eps, tuple(eps.shape), deps)
         e = MP2Energy()
-        check(self._L.corr_rimp2_gradient(self._h, int(nocc), int(nvir), int(naux), _ptr(bia),
-                                          _ptr(eps), _ptr(dbia), _ptr(deps), ctypes.byref(e)))
+        fn = self._L.corr_rimp2_gradient_tc if tensor_cores else self._L.corr_rimp2_gradient
+        check(fn(self._h, int(nocc), int(nvir), int(naux), _ptr(bia), _ptr(eps), _ptr(dbia),
+                 _ptr(deps), ctypes.byref(e)))
         return e.e_total, dbia, deps
 
     # -- batched RI-MP2 ---------------------------------------------------------

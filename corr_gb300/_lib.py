@@ -86,6 +86,7 @@ SIGNATURES = {
                                    ctypes.POINTER(_d)],
     "corr_sync": [_vp],
     "corr_rimp2_gradient": [_vp, _i, _i, _i, _vp, _vp, _vp, _vp, ctypes.POINTER(MP2Energy)],
+    "corr_rimp2_gradient_tc": [_vp, _i, _i, _i, _vp, _vp, _vp, _vp, ctypes.POINTER(MP2Energy)],
     "corr_rimp2_energy_noalloc": [_i, _vp, _i, _i, _i, _vp, _vp, _i, ctypes.POINTER(MP2Energy)],
     "corr_rimp2_energy_batched": [_vp, _i, ctypes.POINTER(RIMP2Instance), _i,
                                   ctypes.POINTER(MP2Energy)],

@@ -14,7 +14,10 @@
 // doubles, never the whole amplitude tensor) and folds W into dE/de with FP64
 // atomics; then dB[Q][i][a] (i in I) = 2 sum_{(j,b)} B[Q][(j,b)] P[(i,a)][(j,b)]
 // is one FP64 GEMM (gemm_fp64.cu).
+#include <algorithm>
+
 #include "common.cuh"
+#include "dgemm_tc.h"
 #include "gemm_fp64.h"
 #include "kernels.h"
 
@@ -174,6 +177,77 @@ __global__ void __launch_bounds__(128) adjoint_panel_kernel(PanelArgs g) {
   }
 }
 
+// Tensor-core form, step 2: the panel P[(il, a)][(j, b)] holds M^{ij}_ab for
+// the occupied block i = i0 + il; one CTA per (il, j) replaces every element
+// by G^{ij}_ab = -(4 M_ab - 2 M_ba) / D (in place: one thread owns the pair
+// (a, b), (b, a)), accumulates W = (2 M_ab - M_ba) M_ab / D^2 into dE/d eps
+// (per-CTA sums in shared memory, then atomics) and writes the pair block's
+// energy -sum (2 M_ab - M_ba) M_ab / D to its own partial.
+__global__ void __launch_bounds__(256) grad_panel_kernel(double* __restrict__ P,
+                                                         const double* __restrict__ eps, int o,
+                                                         int v, int i0, double* __restrict__ deps,
+                                                         double* __restrict__ part) {
+  extern __shared__ double wv[];  // [v]: W summed into dE/d eps_(o+c)
+  __shared__ double red[2][8];
+  const int il = blockIdx.x / o, j = blockIdx.x % o, i = i0 + il;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int c = threadIdx.x; c < v; c += blockDim.x) wv[c] = 0.0;
+  __syncthreads();
+  const long long ld = (long long)o * v;
+  double* Pi = P + (long long)il * v * ld + (long long)j * v;  // row a at Pi + a * ld
+  const double eij = eps[i] + eps[j];
+  double wsum = 0.0, esum = 0.0;
+  for (int a = warp; a < v; a += nw) {
+    const double ea = eps[o + a];
+    double wa = 0.0;
+    for (int b = a + lane; b < v; b += 32) {
+      const double r = 1.0 / ((ea + eps[o + b]) - eij);
+      double* pab = Pi + (long long)a * ld + b;
+      double* pba = Pi + (long long)b * ld + a;
+      const double mab = *pab, mba = *pba;
+      const double tab = 2.0 * mab - mba, tba = 2.0 * mba - mab;
+      double w, e;
+      if (a == b) {
+        w = 2.0 * tab * mab * r * r;  // (a == c) and (b == c)
+        e = tab * mab * r;
+        *pab = -2.0 * tab * r;
+      } else {
+        const double wab = (tab * mab + tba * mba) * r * r;
+        w = wab;
+        e = (tab * mab + tba * mba) * r;
+        *pab = -2.0 * tab * r;
+        *pba = -2.0 * tba * r;
+        atomicAdd(&wv[b], wab);
+      }
+      wa += w;
+      wsum += (a == b) ? 0.5 * w : w;
+      esum -= e;
+    }
+    for (int off = 16; off > 0; off >>= 1) wa += __shfl_xor_sync(0xffffffffu, wa, off);
+    if (lane == 0) atomicAdd(&wv[a], wa);
+  }
+  wsum = warp_sum(wsum);
+  esum = warp_sum(esum);
+  if (lane == 0) {
+    red[0][warp] = wsum;
+    red[1][warp] = esum;
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < v; c += blockDim.x)
+    if (wv[c] != 0.0) atomicAdd(&deps[o + c], wv[c]);
+  if (threadIdx.x == 0) {
+    double ws = 0.0, es = 0.0;
+    for (int k = 0; k < nw; ++k) {
+      ws += red[0][k];
+      es += red[1][k];
+    }
+    atomicAdd(&deps[i], -ws);
+    atomicAdd(&deps[j], -ws);
+    part[2 * blockIdx.x] = es;
+    part[2 * blockIdx.x + 1] = 0.0;
+  }
+}
+
 }  // namespace
 
 size_t rimp2_gradient_workspace(int o, int v, int sms, size_t panel_budget);
@@ -229,13 +303,73 @@ size_t rimp2_gradient_workspace(int o, int v, int sms, size_t panel_budget) {
   return per_i * bi + (size_t)sms * 2 * 16 * ((o + bi - 1) / bi) + 512;
 }
 
+// The adjoint on the tensor cores: per block of bi occupied orbitals the
+// panel M[(i, a)][(j, b)] = sum_Q B^Q_ia B^Q_jb (i in the block, all j) by the
+// FP64-accurate digit GEMM (dgemm_tc.cu), G, W and E by grad_panel_kernel,
+// then dB[Q][(i, a)] = 2 sum_(j,b) B[Q][(j, b)] G[(i, a)][(j, b)] by the digit
+// GEMM.  FP64 accuracy (bounds of the digit GEMM), tensor-core speed.
+size_t rimp2_gradient_tc_workspace(int o, int v, int X, size_t panel_budget, int* bi_out) {
+  const size_t per_i = (size_t)v * o * v * 8;
+  int bi = (int)(panel_budget / per_i);
+  bi = std::max(1, std::min(bi, o));
+  if (bi_out) *bi_out = bi;
+  const int ov = o * v;
+  const size_t ws = std::max(dgemm_tc_workspace(bi * v, ov, X), dgemm_tc_workspace(X, bi * v, ov));
+  return per_i * bi + ws + (size_t)o * o * 16 + 1024;
+}
+
+int rimp2_gradient_tc(corr_context* c, Carver& w, int o, int v, int X, const double* bia,
+                      const double* eps, double* dbia, double* deps, size_t panel_budget) {
+  CORR_CHECK_ARG(v <= 6144, "corr_rimp2_gradient_tc: nvir %d above 6144", v);
+  int bi = 1;
+  rimp2_gradient_tc_workspace(o, v, X, panel_budget, &bi);
+  const int ov = o * v;
+  double* panel = static_cast<double*>(w.take((size_t)v * o * v * 8 * bi));
+  void* dws = w.take(std::max(dgemm_tc_workspace(bi * v, ov, X),
+                              dgemm_tc_workspace(X, bi * v, ov)));
+  double* part = static_cast<double*>(w.take((size_t)o * o * 16));
+  CORR_CUDA(cudaMemsetAsync(deps, 0, (size_t)(o + v) * 8, c->stream));
+  for (int i0 = 0; i0 < o; i0 += bi) {
+    const int nb = std::min(bi, o - i0);
+    DgemmTc m;
+    m.A = mat_view(bia + (size_t)i0 * v, 1, ov);  // rows (i, a) of the block, over Q
+    m.B = mat_view(bia, 1, ov);                   // rows (j, b), over Q
+    m.C = out_view(panel, ov, 1);
+    m.M = nb * v;
+    m.N = ov;
+    m.K = X;
+    m.alpha = 1.0;
+    m.accumulate = false;
+    m.a_lower = false;
+    CORR_TRY(dgemm_tc(c, m, dws));
+    grad_panel_kernel<<<nb * o, 256, (size_t)v * 8, c->stream>>>(panel, eps, o, v, i0, deps,
+                                                                  part + (size_t)i0 * o * 2);
+    CORR_CUDA(cudaGetLastError());
+    DgemmTc d;
+    d.A = mat_view(bia, ov, 1);    // rows Q, over (j, b)
+    d.B = mat_view(panel, ov, 1);  // rows (i, a) of the block, over (j, b)
+    d.C = out_view(dbia + (size_t)i0 * v, ov, 1);
+    d.M = X;
+    d.N = nb * v;
+    d.K = ov;
+    d.alpha = 2.0;
+    d.accumulate = false;
+    d.a_lower = false;
+    CORR_TRY(dgemm_tc(c, d, dws));
+    c->launches += 1;
+  }
+  CORR_CUDA(launch_energy_reduce(part, o * o, nullptr, c->dres->e, c->stream));
+  c->launches += 1;
+  return CORR_OK;
+}
+
 }  // namespace corr
 
 using namespace corr;
 
-extern "C" int corr_rimp2_gradient(corr_context* c, int nocc, int nvir, int naux,
-                                   const double* bia, const double* eps, double* dbia,
-                                   double* deps, corr_mp2_energy* e_out) {
+static int rimp2_gradient_call(corr_context* c, int nocc, int nvir, int naux, const double* bia,
+                               const double* eps, double* dbia, double* deps,
+                               corr_mp2_energy* e_out, bool tc) {
   CORR_CHECK_ARG(c && bia && eps && dbia && deps, "corr_rimp2_gradient: null pointer argument");
   CORR_CHECK_ARG(nocc >= 1 && nvir >= 1 && naux >= 1, "corr_rimp2_gradient: bad sizes");
   CORR_CHECK_ARG((long long)nocc * nvir <= 0x7fffffffLL, "corr_rimp2_gradient: nocc*nvir too large");
@@ -254,7 +388,8 @@ extern "C" int corr_rimp2_gradient(corr_context* c, int nocc, int nvir, int naux
   double *db, *de;
   Carver cv{nullptr, 0};
   plan(cv, &sb, &se, &db, &de);
-  cv.take(rimp2_gradient_workspace(nocc, nvir, c->sms, budget));
+  cv.take(tc ? rimp2_gradient_tc_workspace(nocc, nvir, naux, budget, nullptr)
+             : rimp2_gradient_workspace(nocc, nvir, c->sms, budget));
   CORR_TRY(c->ws.reserve(cv.used));
   Carver w{c->ws.ptr, 0};
   plan(w, &sb, &se, &db, &de);
@@ -264,7 +399,10 @@ extern "C" int corr_rimp2_gradient(corr_context* c, int nocc, int nvir, int naux
   const double* d_e = static_cast<const double*>(stage_in(c, eps, ne * 8, se));
   CORR_CHECK_ARG(d_b && d_e, "host-to-device copy failed");
   mark(c, 1);
-  CORR_TRY(rimp2_gradient_fp64(c, w, nocc, nvir, naux, d_b, d_e, db, de, budget));
+  if (tc)
+    CORR_TRY(rimp2_gradient_tc(c, w, nocc, nvir, naux, d_b, d_e, db, de, budget));
+  else
+    CORR_TRY(rimp2_gradient_fp64(c, w, nocc, nvir, naux, d_b, d_e, db, de, budget));
   mark(c, 2);
   CORR_TRY(stage_out(c, dbia, db, nb * 8));
   CORR_TRY(stage_out(c, deps, de, ne * 8));
@@ -274,4 +412,16 @@ extern "C" int corr_rimp2_gradient(corr_context* c, int nocc, int nvir, int naux
     e_out->e_os = e_out->e_ss = e_out->e_scs = 0.0;  // the gradient call reports E only
   }
   return CORR_OK;
+}
+
+extern "C" int corr_rimp2_gradient(corr_context* c, int nocc, int nvir, int naux,
+                                   const double* bia, const double* eps, double* dbia,
+                                   double* deps, corr_mp2_energy* e_out) {
+  return rimp2_gradient_call(c, nocc, nvir, naux, bia, eps, dbia, deps, e_out, false);
+}
+
+extern "C" int corr_rimp2_gradient_tc(corr_context* c, int nocc, int nvir, int naux,
+                                      const double* bia, const double* eps, double* dbia,
+                                      double* deps, corr_mp2_energy* e_out) {
+  return rimp2_gradient_call(c, nocc, nvir, naux, bia, eps, dbia, deps, e_out, true);
 }

@@ -205,6 +205,15 @@ int corr_rimp2_batch_autotune(corr_context* ctx, int n, const corr_rimp2_instanc
 int corr_rimp2_gradient(corr_context* ctx, int nocc, int nvir, int naux, const double* bia,
                         const double* eps, double* dbia, double* deps, corr_mp2_energy* e_out);
 
+/* corr_rimp2_gradient on the tensor cores: per block of occupied orbitals the
+ * panel (ia|jb) by the FP64-accurate digit GEMM (corr_dgemm_tc), G, W and E
+ * in place, and dB = 2 B G^T by the digit GEMM; the same outputs to the digit
+ * GEMM's accuracy (~FP64), at tensor-core speed.  nvir <= 6144.  The adjoint
+ * of the precision forms (the autograd backward of a split-precision
+ * forward). */
+int corr_rimp2_gradient_tc(corr_context* ctx, int nocc, int nvir, int naux, const double* bia,
+                           const double* eps, double* dbia, double* deps, corr_mp2_energy* e_out);
+
 /* Allocation-free RI-MP2 energy (no counterpart in the reference).  For
  * callers that cannot call cudaMalloc -- a host program whose device memory is
  * all handed out by its own pool allocator, or a latency-critical loop where an

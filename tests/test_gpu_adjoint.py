@@ -20,6 +20,20 @@ def test_gradient_vs_fp64_restatement(ctx, o, v, X, seed):
     assert np.abs(deg - de).max() <= 1e-11 * max(1e-30, np.abs(de).max())
 
 
+@pytest.mark.parametrize("o,v,X,seed", [(1, 1, 1, 1), (3, 7, 9, 2), (5, 70, 33, 3), (4, 130, 65, 4),
+                                        (9, 200, 600, 5)])
+def test_gradient_tc_vs_fp64_restatement(ctx, o, v, X, seed):
+    """The tensor-core adjoint (digit GEMMs): the FP64 restatement's values to
+    the digit GEMM's accuracy (1e-10 of the largest component; X = 600 runs two
+    K passes)."""
+    B, eps = O.synth_rimp2(o, v, X, seed)
+    E, dB, de = O.rimp2_gradient(B, eps, o, v)
+    Eg, dBg, deg = ctx.rimp2_gradient(B, eps, o, v, X, tensor_cores=True)
+    assert abs(Eg - E) <= 1e-11 * max(1.0, abs(E))
+    assert np.abs(dBg - dB).max() <= 1e-10 * max(1e-30, np.abs(dB).max())
+    assert np.abs(deg - de).max() <= 1e-10 * max(1e-30, np.abs(de).max())
+
+
 def test_gradient_vs_central_differences_small(ctx):
     o, v, X = 4, 40, 30
     B, eps = O.synth_rimp2(o, v, X, 9)
@@ -42,14 +56,63 @@ def test_gradient_vs_central_differences_small(ctx):
         assert abs(fd - de[p]) <= 1e-6 * max(abs(fd), 1e-3 * np.abs(de).max())
 
 
-def test_gradient_config4_finite_differences(ctx):
-    """nocc=64, nvir=512, naux=2048 (config-2 distributions, FP32 storage):
-    central differences (h=1e-4) on 200 seeded entries of B, and sampled
-    rows of the FP64 restatement."""
+@pytest.fixture(scope="module")
+def config4():
     o, v, X = 64, 512, 2048
     B32, eps = O.synth_rimp2(o, v, X, 4004, dtype=np.float32)
-    B = B32.astype(np.float64)  # the stored values, exactly
-    E, dB, de = ctx.rimp2_gradient(B, eps, o, v, X)
+    return o, v, X, B32.astype(np.float64), eps  # the stored values, exactly
+
+
+@pytest.fixture(scope="module")
+def config4_fp64(ctx, config4):
+    import time
+
+    import torch
+
+    o, v, X, B, eps = config4
+    Bd, ed = torch.from_numpy(B).cuda(), torch.from_numpy(eps).cuda()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    E, dB, de = ctx.rimp2_gradient(Bd, ed, o, v, X)
+    torch.cuda.synchronize()
+    print(f"config-4 adjoint, FP64 form: {1e3 * (time.perf_counter() - t0):.1f} ms")
+    return E, dB.cpu().numpy(), de.cpu().numpy()
+
+
+def test_gradient_tc_config4_vs_fp64(ctx, config4, config4_fp64):
+    """Config 4 through the tensor-core adjoint (device arrays): the FP64 form's
+    gradient to 1e-10 of its largest component, and its time beside it."""
+    import time
+
+    import torch
+
+    o, v, X, B, eps = config4
+    Bd, ed = torch.from_numpy(B).cuda(), torch.from_numpy(eps).cuda()
+    ctx.rimp2_gradient(Bd, ed, o, v, X, tensor_cores=True)  # warm (workspace)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    E, dB, de = ctx.rimp2_gradient(Bd, ed, o, v, X, tensor_cores=True)
+    torch.cuda.synchronize()
+    print(f"config-4 adjoint, tensor-core form: {1e3 * (time.perf_counter() - t0):.1f} ms")
+    E64, dB64, de64 = config4_fp64
+    dB = dB.cpu().numpy()
+    de = de.cpu().numpy()
+    assert abs(E - E64) <= 1e-11 * abs(E64)
+    assert np.abs(dB - dB64).max() <= 1e-10 * np.abs(dB64).max()
+    assert np.abs(de - de64).max() <= 1e-10 * np.abs(de64).max()
+
+
+@pytest.mark.parametrize("tc", [False, True])
+def test_gradient_config4_finite_differences(ctx, config4, config4_fp64, tc):
+    """nocc=64, nvir=512, naux=2048 (config-2 distributions, FP32 storage):
+    central differences (h=1e-4) on 200 seeded entries of B, and sampled
+    rows of the FP64 restatement; both adjoint forms."""
+    o, v, X, B, eps = config4
+    B = B.copy()
+    if tc:
+        E, dB, de = ctx.rimp2_gradient(B, eps, o, v, X, tensor_cores=True)
+    else:
+        E, dB, de = config4_fp64
     r = O.rng(4005)
     h = 1e-4
     scale = np.abs(dB).max()
@@ -96,5 +159,8 @@ def test_autograd_function(ctx):
     E32 = rimp2_energy(B32, et.detach(), o, v, "split_bf16", ctx)
     (g,) = torch.autograd.grad(E32, B32)
     assert g.dtype == torch.float32
+    # the precision-form forward's backward is the tensor-core adjoint
+    _, dB32, _ = O.rimp2_gradient(B.astype(np.float32).astype(np.float64), eps, o, v)
+    assert np.abs(g.cpu().numpy() - dB32).max() <= 1e-6 * np.abs(dB32).max()
     assert abs(E32.item() - O.rimp2_energy(B.astype(np.float32).astype(np.float64), eps, o, v)[2]) \
         <= 2e-7 * abs(Eo)
