@@ -51,7 +51,8 @@ def parse():
     ap.add_argument("--batch-count", type=int, default=256,
                     help="instances of the batched workload (256 by default)")
     ap.add_argument("--workload", default="rimp2",
-                    choices=["rimp2", "batch256", "ri_pipeline", "cluster", "dgemm_tc"],
+                    choices=["rimp2", "batch256", "ri_pipeline", "cluster", "dgemm_tc",
+                             "adjoint"],
                     help="batch256: 256 uneven RI-MP2 instances in one batched launch; "
                          "ri_pipeline: time-to-E_corr from the 3-index integrals")
     ap.add_argument("--nbf", type=int, default=480, help="ri_pipeline: basis functions")
@@ -795,8 +796,57 @@ def run_dgemm(args):
     print(json.dumps(line), flush=True)
 
 
+def run_adjoint(args):
+    """The RI-MP2 adjoint (dE/dB, dE/deps) at nocc=64, nvir=512, naux=2048
+    (config-2 distributions, seeded), device arrays: the tensor-core form
+    (corr_rimp2_gradient_tc) per step, timed with CUDA events, and one call of
+    the FP64 form (corr_rimp2_gradient) beside it."""
+    import numpy as np
+    import torch
+
+    import corr_gb300
+    from corr_gb300 import workloads as W
+
+    torch.cuda.set_device(0)
+    o, v, X = 64, 512, 2048
+    B, eps = W.synth_rimp2(o, v, X, 4004)
+    Bd, ed = torch.from_numpy(B).cuda(), torch.from_numpy(eps).cuda()
+    ctx = corr_gb300.Context(0)
+
+    def timed(tc, n):
+        for _ in range(1 if not tc else max(1, args.warmup)):
+            r = ctx.rimp2_gradient(Bd, ed, o, v, X, tensor_cores=tc)
+        torch.cuda.synchronize()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record()
+        for _ in range(n):
+            r = ctx.rimp2_gradient(Bd, ed, o, v, X, tensor_cores=tc)
+        s1.record()
+        torch.cuda.synchronize()
+        return s0.elapsed_time(s1) / n, r
+
+    steps = max(1, min(args.steps, 10))
+    ms, (E, dB, de) = timed(True, steps)
+    line = {
+        "metric": "RI-MP2 adjoint (dE/dB, dE/deps) time", "value": ms, "unit": "ms",
+        "n_gpus": 1, "steps": steps, "warmup": max(1, args.warmup), "ms_per_step": ms,
+        "higher_is_better": False, "dtype": "f64 (bf16 digits)", "data": "synthetic",
+        "config": {"workload": f"nocc={o} nvir={v} naux={X}, B = G diag(s_Q), seed 4004"},
+        "energy": E,
+    }
+    if not args.no_cpu_baseline:
+        ms64, (E64, dB64, de64) = timed(False, 1)
+        line["fp64_form"] = {"ms": ms64, "speedup": ms64 / ms,
+                             "max_rel_dB": float((dB - dB64).abs().max() / dB64.abs().max()),
+                             "max_rel_deps": float((de - de64).abs().max() / de64.abs().max())}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "adjoint":
+        run_adjoint(args)
+        return
     if args.workload == "cluster":
         run_cluster(args)
         return
