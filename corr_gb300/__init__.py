@@ -182,6 +182,12 @@ class Context:
         status CORR_ERR_DEVICE_TIMEOUT; the context stays usable)."""
         check(self._L.corr_selftest_wait_timeout(self._h, int(limit_ms)))
 
+    def set_fp64_strict(self, strict=True):
+        """Plain-form metric calls (ri_metric_inv_sqrt, calculate_ri) on the
+        FP64 pipe only (True) or with the FP64-accurate digit GEMM (False,
+        the default)."""
+        check(self._L.corr_set_fp64_strict(self._h, 1 if strict else 0))
+
     def set_energy_tiles(self, tiles):
         """1 (default): a last virtual tile of at most 64 columns runs 64 wide;
         0: every tile 128 wide."""

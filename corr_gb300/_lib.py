@@ -93,6 +93,7 @@ SIGNATURES = {
     "corr_rimp2_energy_batched_async": [_vp, _i, ctypes.POINTER(RIMP2Instance), _i, _vp],
     "corr_set_batch_policy": [_vp, _i, _i, _i],
     "corr_set_energy_tiles": [_vp, _i],
+    "corr_set_fp64_strict": [_vp, _i],
     "corr_selftest_wait_timeout": [_vp, _i],
     "corr_rimp2_batch_autotune": [_vp, _i, ctypes.POINTER(RIMP2Instance), _i, ctypes.POINTER(_i),
                                   ctypes.POINTER(_i), ctypes.POINTER(_i),

@@ -264,6 +264,13 @@ int corr_sync(corr_context* c) {
   return CORR_OK;
 }
 
+int corr_set_fp64_strict(corr_context* c, int strict) {
+  CORR_CHECK_ARG(c != nullptr, "null context");
+  CORR_CHECK_ARG(strict == 0 || strict == 1, "corr_set_fp64_strict: strict must be 0 or 1");
+  c->fp64_strict = strict;
+  return CORR_OK;
+}
+
 int corr_set_energy_tiles(corr_context* c, int tiles) {
   CORR_CHECK_ARG(c != nullptr, "null context");
   CORR_CHECK_ARG(tiles == 0 || tiles == 1,

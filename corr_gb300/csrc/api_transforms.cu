@@ -372,7 +372,7 @@ int corr_ri_metric_inv_sqrt(corr_context* c, int naux, const double* J, double t
   const double* d_j = static_cast<const double*>(stage_in(c, J, nj * 8, s_j));
   CORR_CHECK_ARG(d_j, "host-to-device copy failed");
   mark(c, 1);
-  CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, naux, tol, out, ncut, true));
+  CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, naux, tol, out, ncut, !c->fp64_strict));
   mark(c, 2);
   CORR_TRY(stage_out(c, jm12, out, nj * 8));
   return finish_results(c, 0);
@@ -409,9 +409,18 @@ int corr_calculate_ri(corr_context* c, int naux, int nroao, const double* J, con
   CORR_CHECK_ARG(d_j && d_p, "host-to-device copy failed");
   mark(c, 1);
   // ri.cc:50-69: J^-1/2 with the 1e-10 relative eigenvalue cutoff
-  CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, naux, 1e-10, jm, nullptr, true));
+  CORR_TRY(ri_inv_sqrt_device(c, jws, d_j, naux, 1e-10, jm, nullptr, !c->fp64_strict));
   // ri.cc:102-103: BPQ = J^-1/2 (Q|mn), on the FP64-accurate digit GEMM
-  // (rows P of J^-1/2 against the columns mn of (Q|mn) read as rows over Q)
+  // (rows P of J^-1/2 against the columns mn of (Q|mn) read as rows over Q),
+  // or on the FP64 pipe when the context asks for strict FP64
+  if (c->fp64_strict) {
+    CORR_TRY(gemm_f64(gemm_args(jm, d_p, out, naux, (int)N2, naux, naux, N2, N2, 0, 0),
+                      &c->dres->status, c->stream));
+    c->launches += 1;
+    mark(c, 2);
+    CORR_TRY(stage_out(c, bpq, out, np * 8));
+    return finish_results(c, 0);
+  }
   DgemmTc g;
   g.A = mat_view(jm, naux, 1);
   g.B = mat_view(d_p, 1, N2);

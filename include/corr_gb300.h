@@ -183,6 +183,14 @@ int corr_selftest_wait_timeout(corr_context* ctx, int limit_ms);
  * 128 wide.  Both give the same energies up to FP64 summation order. */
 int corr_set_energy_tiles(corr_context* ctx, int tiles);
 
+/* FP64 arithmetic of the plain-form metric calls (no counterpart in the
+ * reference).  0 (the default): corr_ri_metric_inv_sqrt and corr_calculate_ri
+ * compute J^-1/2 of a certified metric by Newton-Schulz and BPQ = J^-1/2 (Q|mn)
+ * on the FP64-accurate digit GEMM (corr_dgemm_tc; 5e-11 from LAPACK's J^-1/2
+ * on the 20-water cluster).  1: every product on the FP64 pipe and J^-1/2 by
+ * the eigendecomposition -- IEEE FP64 end to end, several times slower. */
+int corr_set_fp64_strict(corr_context* ctx, int strict);
+
 /* Launch variant of the batched kernel: unit order (0 = input order,
  * 1 = costliest instance first), shared-memory pipeline depth in stages of
  * one 64-wide Q block (2 or 3; the three-digit form always runs 2) and tile

@@ -160,3 +160,25 @@ def test_from_3index_cholesky_sizes(ctx, X, N, nocc, prec):
     e, ncut = ctx.rimp2_energy_from_3index(2 * nocc, mos, eps, J, P3, prec)
     assert ncut == ncut_ref == 0
     assert abs(e.e_total - et) <= (1e-10 if prec == "fp64" else 2e-7) * abs(et)
+
+
+def test_fp64_strict_switch(ctx):
+    """corr_set_fp64_strict: the eigendecomposition and FP64-pipe products
+    give the same J^-1/2 and BPQ as the default (Newton-Schulz, digit GEMM)
+    to FP64 accuracy."""
+    r = O.rng(77)
+    X, N = 300, 12
+    L = r.standard_normal((X, X)) / np.sqrt(X)
+    J = L @ L.T + 0.3 * np.eye(X)
+    P3 = r.standard_normal((X, N, N))
+    P3 = P3 + P3.transpose(0, 2, 1)
+    jm_fast, _ = ctx.ri_metric_inv_sqrt(J)
+    b_fast = ctx.calculate_ri(J, P3)
+    ctx.set_fp64_strict(True)
+    try:
+        jm_strict, _ = ctx.ri_metric_inv_sqrt(J)
+        b_strict = ctx.calculate_ri(J, P3)
+    finally:
+        ctx.set_fp64_strict(False)
+    assert np.abs(jm_fast - jm_strict).max() <= 1e-12 * np.abs(jm_strict).max()
+    assert np.abs(b_fast - b_strict).max() <= 1e-12 * np.abs(b_strict).max()
