@@ -48,6 +48,9 @@ def parse():
     ap.add_argument("--precision", default="split_fp16",
                     choices=["split_fp16", "split_bf16", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cluster", action="store_true",
+                    help="leave the water-cluster time-to-E_corr block out of the line "
+                         "(profiling runs of the energy kernel)")
     ap.add_argument("--batch-count", type=int, default=256,
                     help="instances of the batched workload (256 by default)")
     ap.add_argument("--workload", default="rimp2",
@@ -425,7 +428,7 @@ def run_ours(args):
     f64 = statistics.median(f64_ms)
 
     # ---- the metric's time-to-E_corr leg at the water-cluster sizes
-    c3 = time_to_ecorr_c3(ctx)
+    c3 = None if args.no_cluster else time_to_ecorr_c3(ctx)
 
     # ---- end to end through the public API with host buffers
     Bh = torch.from_numpy(B).pin_memory()

@@ -812,10 +812,10 @@ extern "C" int corr_ri_integrals(corr_context* c, const corr_basis* obs, const c
     need = (need + 1023) / 1024 * 1024 + 1024;
     if (have < need) CORR_CUDA(cudaDeviceSetLimit(cudaLimitStackSize, need));
   }
-  // The classes write disjoint blocks of J and (P|mu nu): they run on four
+  // The classes write disjoint blocks of J and (P|mu nu): they run on eight
   // side streams forked from (and joined back into) the context stream, so
   // the tails of the large classes overlap the small ones.
-  constexpr int kSide = 4;
+  constexpr int kSide = 8;
   struct Side {
     cudaStream_t st[kSide] = {};
     cudaEvent_t ev[kSide + 1] = {};
@@ -833,12 +833,12 @@ extern "C" int corr_ri_integrals(corr_context* c, const corr_basis* obs, const c
   CORR_CUDA(cudaEventCreateWithFlags(&side.ev[kSide], cudaEventDisableTiming));
   CORR_CUDA(cudaEventRecord(side.ev[kSide], c->stream));
   for (int k = 0; k < kSide; ++k) CORR_CUDA(cudaStreamWaitEvent(side.st[k], side.ev[kSide], 0));
-  int nlaunch = 0;
+  int next_stream = 0;
   auto launch = [&](Kern k, Basis3 g, int lp, int lc, int ld) -> int {
     const long long work = (long long)g.nalist * g.nplist;
     if (work <= 0) return CORR_OK;
     const int grid = (int)std::min<long long>((work + 127) / 128, (long long)c->sms * 32);
-    k<<<grid, 128, 0, side.st[nlaunch++ % kSide]>>>(g);
+    k<<<grid, 128, 0, side.st[next_stream]>>>(g);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
       cudaFuncAttributes fa{};
@@ -860,9 +860,26 @@ extern "C" int corr_ri_integrals(corr_context* c, const corr_basis* obs, const c
   double* Jout = J ? (jdev ? J : static_cast<double*>(p[11])) : nullptr;
   double* Pout = pmn ? (pdev ? pmn : static_cast<double*>(p[12])) : nullptr;
   if (Pout) CORR_CUDA(cudaMemsetAsync(Pout, 0, (size_t)X * N * N * 8, c->stream));
+  // every class launch with a cost estimate (auxiliary primitives x orbital
+  // primitive pairs x Cartesian components); launched largest first, each on
+  // the side stream with the least estimated work so far
+  struct Job {
+    Kern k;
+    Basis3 g;
+    int lp, lc, ld;
+    double cost;
+  };
+  std::vector<Job> jobs;
+  auto pairs_of = [](const std::vector<int2>& r) {
+    double n = 0.0;
+    for (const int2& x : r) n += x.y - x.x;
+    return n;
+  };
   for (int lp = 0; lp <= kLmax; ++lp) {
     const int na = aoff[lp + 1] - aoff[lp];
     if (na == 0) continue;
+    double aprim = 0.0;
+    for (int sidx : alist[lp]) aprim += ha.sh[sidx].nprim;
     Basis3 g{};
     g.aux = dA;
     g.alist = static_cast<const int*>(p[4]) + aoff[lp];
@@ -887,7 +904,8 @@ extern "C" int corr_ri_integrals(corr_context* c, const corr_basis* obs, const c
         h.out = Jout;
         h.N = X;
         h.two_center = 1;
-        CORR_TRY(launch(class_kernel(lp, lc, 0), h, lp, lc, 0));
+        jobs.push_back({class_kernel(lp, lc, 0), h, lp, lc, 0,
+                        aprim * pairs_of(prange2[lc]) * ncart(lp) * ncart(lc)});
       }
     }
     if (pmn) {
@@ -905,9 +923,22 @@ extern "C" int corr_ri_integrals(corr_context* c, const corr_basis* obs, const c
           h.out = Pout;
           h.N = N;
           h.two_center = 0;
-          CORR_TRY(launch(class_kernel(lp, lc, ld), h, lp, lc, ld));
+          jobs.push_back({class_kernel(lp, lc, ld), h, lp, lc, ld,
+                          aprim * pairs_of(prange3[lc * 3 + ld]) * ncart(lp) * ncart(lc) *
+                              ncart(ld)});
         }
     }
+  }
+  std::stable_sort(jobs.begin(), jobs.end(),
+                   [](const Job& a, const Job& b) { return a.cost > b.cost; });
+  double load[kSide] = {};
+  for (const Job& jb : jobs) {
+    int k = 0;
+    for (int q = 1; q < kSide; ++q)
+      if (load[q] < load[k]) k = q;
+    load[k] += jb.cost;
+    next_stream = k;
+    CORR_TRY(launch(jb.k, jb.g, jb.lp, jb.lc, jb.ld));
   }
   for (int k = 0; k < kSide; ++k) {
     CORR_CUDA(cudaEventRecord(side.ev[k], side.st[k]));
