@@ -401,14 +401,15 @@ class Context:
         else:
             mos = mos.clone() if on_dev else np.array(mos, dtype=np.float64, copy=True)
         fmat = self._out(smat, (N, N), None)
+        pmat = self._out(smat, (N, N), None)
         moens = self._out(smat, (N,), None)
         e = np.zeros(3)
         it = ctypes.c_int(0)
         check(self._L.corr_run_scf(self._h, int(nroe), N, float(ion_rep), _ptr(smat), _ptr(hmat),
                                    int(intval.shape[0]), _ptr(sortcount), _ptr(intval),
                                    _ptr(intnums), int(maxiter), _ptr(mos), _ptr(fmat),
-                                   _ptr(moens), _ptr(e), ctypes.byref(it)))
-        return {"mos": mos, "fmat": fmat, "moens": moens, "energy": float(e[0]),
+                                   _ptr(moens), _ptr(e), ctypes.byref(it), _ptr(pmat)))
+        return {"mos": mos, "fmat": fmat, "pmat": pmat, "moens": moens, "energy": float(e[0]),
                 "one": float(e[1]), "two": float(e[2]), "iterations": it.value}
 
     # -- hand-off files (src/IO/ops_io.cc) -----------------------------------

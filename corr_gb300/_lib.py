@@ -117,7 +117,8 @@ SIGNATURES = {
     "corr_cc_fock": [_vp, _i, _i, _vp, _vp, _vp, _vp, _vp],
     "corr_dgemm_tc": [_vp, _i, _i, _i, _i, _i, _d, _vp, _i, _vp, _i, _d, _vp, _i],
     "corr_build_fmat": [_vp, _i, _vp, _vp, _ll, _vp, _vp, _vp, _vp],
-    "corr_run_scf": [_vp, _i, _i, _d, _vp, _vp, _ll, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp],
+    "corr_run_scf": [_vp, _i, _i, _d, _vp, _vp, _ll, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp,
+                     _vp],
     "corr_read_system": [ctypes.c_char_p, ctypes.POINTER(SystemInfo), _vp, _vp, _vp, _vp],
     "corr_read_oei": [_vp, ctypes.c_char_p, _i, _vp, _vp, _vp, _vp],
     "corr_read_tei": [_vp, ctypes.c_char_p, _ll, _vp, _vp, _vp],

@@ -256,7 +256,7 @@ int corr_build_fmat(corr_context* c, int nroao, const double* pmat, const double
 int corr_run_scf(corr_context* c, int nroe, int nroao, double ion_rep, const double* smat,
                  const double* hmat, long long nrofint, const long long* sortcount,
                  const double* intval, const unsigned short* intnums, int maxiter, double* mos,
-                 double* fmat, double* moens, double* energies, int* iterations) {
+                 double* fmat, double* moens, double* energies, int* iterations, double* pmat) {
   CORR_CHECK_ARG(c && smat && hmat && sortcount && mos && fmat && moens && energies &&
                      (nrofint == 0 || (intval && intnums)),
                  "corr_run_scf: null argument");
@@ -434,6 +434,7 @@ int corr_run_scf(corr_context* c, int nroe, int nroao, double ion_rep, const dou
   if (iterations) *iterations = iter;
   CORR_CUDA(cudaMemcpyAsync(mos, C, n2 * 8, cudaMemcpyDefault, c->stream));
   CORR_CUDA(cudaMemcpyAsync(fmat, F, n2 * 8, cudaMemcpyDefault, c->stream));
+  if (pmat) CORR_CUDA(cudaMemcpyAsync(pmat, P, n2 * 8, cudaMemcpyDefault, c->stream));
   if (diagonalised)  // else moens keeps what the caller passed (no orbital energies exist)
     CORR_CUDA(cudaMemcpyAsync(moens, w, (size_t)N * 8, cudaMemcpyDefault, c->stream));
   CORR_CUDA(cudaStreamSynchronize(c->stream));

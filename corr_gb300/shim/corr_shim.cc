@@ -230,6 +230,33 @@ void pmv(double* mat, double* vi, double* vo, int nroao) {
   check(corr_dgemm(ctx(), 0, 0, nroao, 1, nroao, 1.0, mat, nroao, vi, 1, 0.0, vo, 1), "pmv");
 }
 
+// ---- RHF (src/SCF) -----------------------------------------------------------
+
+void build_Fmat(int nroao, double* Fmat, double* Pmat, double* Hmat, double* intval,
+                unsigned short* intnums, long long int* sortcount, long long int nrofint) {
+  check(corr_build_fmat(ctx(), nroao, Pmat, Hmat, nrofint, sortcount, intval, intnums, Fmat),
+        "build_Fmat");
+}
+
+#ifdef CORR_SHIM_USE_REFERENCE_HEADERS
+void run_scf(systeminfo* sysinfo, OEints* onemats, TEints* twomats) {
+  std::cout << "\nSCF:\n----" << '\n';
+  double e[3];
+  int iters = 0;
+  check(corr_run_scf(ctx(), sysinfo->nroe, sysinfo->nroao, sysinfo->ion_rep, onemats->Smat,
+                     onemats->Hmat, sysinfo->nrofint, twomats->sortcount, twomats->intval,
+                     twomats->intnums, sysinfo->scfiter, onemats->MOs, onemats->Fmat,
+                     onemats->MOens, e, &iters, onemats->Pmat),
+        "run_scf");
+  std::cout << "iterations: " << iters << '\n';
+  std::cout << "\nHF-Results:\n";
+  std::cout << "-----------\n";
+  std::cout << std::setw(PWIDTH_L) << "  ONE E:" << std::setw(PWIDTH_R) << e[1] << '\n';
+  std::cout << std::setw(PWIDTH_L) << "  TWO E:" << std::setw(PWIDTH_R) << e[2] << '\n';
+  std::cout << std::setw(PWIDTH_L) << "TOTAL E:" << std::setw(PWIDTH_R) << e[0] << '\n';
+}
+#endif
+
 // ---- hand-off files (src/IO/ops_io.cc) --------------------------------------
 
 void write_wav_HF(std::string wavfile, int nroao, double* MOens, double* MOs) {

@@ -87,6 +87,18 @@ void read_tei(systeminfo* sysinfo, TEints* twomats);      // ops_io.h:39, caller
 void read_wav_HF(systeminfo* sysinfo, OEints* onemats);   // ops_io.h:34, caller-allocated arrays
 #endif
 
+// RHF (src/SCF).  ops_rhf.h:22 -- F = H + sum P ((mn|ls) - 1/2 (ml|ns)) from the
+// packed unique integrals, host arrays.
+void build_Fmat(int nroao, double* Fmat, double* Pmat, double* Hmat, double* intval,
+                unsigned short* intnums, long long int* sortcount, long long int nrofint);
+#ifdef CORR_SHIM_USE_REFERENCE_HEADERS
+// scf.h:5 -- the whole iteration on the GPU (needs systeminfo::ion_rep and
+// ::scfiter, members the standalone layout does not declare); S^-1/2 is formed
+// on the device, onemats->Som12 is not read; MOs, MOens, Pmat and Fmat are
+// written as the reference leaves them, and the HF-Results block is printed.
+void run_scf(systeminfo* sysinfo, OEints* onemats, TEints* twomats);
+#endif
+
 // Dense FP64 helpers of src/MATH/ops_mat.h, row-major np x np, on the GPU.
 void diag_mat(int nroao, double* mat, double* vals, double* vecs);          // ops_mat.h:3
 void symmortho_mat(int nroao, double* mat, double* tmat, double* dummat);   // ops_mat.h:4

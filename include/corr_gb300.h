@@ -372,9 +372,10 @@ int corr_build_fmat(corr_context* ctx, int nroao, const double* pmat, const doub
  * rows) is the guess on entry; when |sum_i mos[i][i]| < 0.1 the core guess
  * (diagonalised hmat, check_initial_guess, ops_rhf.cc:15-36) replaces it.  On
  * return: mos, fmat (rebuilt from the final density, scf.cc:289-290), moens
- * (the last diagonalisation's orbital energies; unchanged when none ran) and
+ * (the last diagonalisation's orbital energies; unchanged when none ran),
  * energies[3] = {TOTAL E, ONE E, TWO E} as run_scf prints them
- * (scf.cc:305-314).  *iterations optional.  The overlap must be positive
+ * (scf.cc:305-314) and, if pmat is non-null, that final density (onemats->Pmat
+ * of the reference).  *iterations optional.  The overlap must be positive
  * definite (CORR_ERR_BAD_ARG otherwise; the reference would divide by the
  * square root of a non-positive eigenvalue).  Runs all on the device; host or
  * device arrays; nroao <= 2048; its own device allocation of nroao^4 +
@@ -382,7 +383,7 @@ int corr_build_fmat(corr_context* ctx, int nroao, const double* pmat, const doub
 int corr_run_scf(corr_context* ctx, int nroe, int nroao, double ion_rep, const double* smat,
                  const double* hmat, long long nrofint, const long long* sortcount,
                  const double* intval, const unsigned short* intnums, int maxiter, double* mos,
-                 double* fmat, double* moens, double* energies, int* iterations);
+                 double* fmat, double* moens, double* energies, int* iterations, double* pmat);
 
 /* ---- dense FP64 helpers (src/MATH/ops_mat.cc) ---------------------------- */
 

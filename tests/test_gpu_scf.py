@@ -97,6 +97,8 @@ def test_run_scf_h2o_core_guess(ctx, h2o):
     assert np.abs(Pg - Pr).max() <= 1e-6
     # orthonormal in the metric S
     assert np.abs(C @ I.S @ C.T - np.eye(I.N)).max() <= 1e-10
+    # the final density (DIIS ran, so no damping is left): 2 C_occ^T C_occ
+    assert np.abs(r["pmat"] - Pg).max() <= 1e-12
 
 
 def test_run_scf_from_converged_orbitals(ctx, h2o):
@@ -127,3 +129,26 @@ def test_run_scf_zero_iterations_and_bad_overlap(ctx, h2o):
     bad[0, 0] = -1.0
     with pytest.raises(corr_gb300.CorrError):
         ctx.run_scf(10, bad, H, pk.sortcount, pk.intval, pk.intnums, ion_rep=I.enuc)
+
+
+def test_shim_build_fmat(h2o):
+    """The drop-in shim's build_Fmat (the reference's signature, ops_rhf.h:22)
+    through its mangled symbol, on host arrays."""
+    import ctypes
+
+    from corr_gb300 import build
+
+    build.build_shim()
+    lib = ctypes.CDLL(os.path.join(os.path.dirname(HERE), "corr_gb300", "libcorr_shim.so"))
+    fn = getattr(lib, "_Z10build_FmatiPdS_S_S_PtPxx")
+    I, pk, fx = h2o
+    H = np.ascontiguousarray(I.T + I.V)
+    Co = fx["mos"][:5]
+    P = np.ascontiguousarray(2.0 * Co.T @ Co)
+    F = np.zeros_like(P)
+    dp = ctypes.POINTER(ctypes.c_double)
+    fn(ctypes.c_int(I.N), F.ctypes.data_as(dp), P.ctypes.data_as(dp), H.ctypes.data_as(dp),
+       pk.intval.ctypes.data_as(dp), pk.intnums.ctypes.data_as(ctypes.POINTER(ctypes.c_ushort)),
+       pk.sortcount.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
+       ctypes.c_longlong(pk.nrofint))
+    assert np.abs(F - fx["fmat"]).max() <= 1e-12

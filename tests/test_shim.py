@@ -21,6 +21,7 @@ REFERENCE_SYMBOLS = [
     "_Z9mat_mat_TiPdS_S_", "_Z9mat_mat_TxPdS_S_",         # ops_mat.h:6, :9
     "_Z9mat_T_matiPdS_S_", "_Z9mat_T_matxPdS_S_",         # ops_mat.h:7, :10
     "_Z3pmvPdS_S_i",                                      # ops_mat.h:13
+    "_Z10build_FmatiPdS_S_S_PtPxx",                       # ops_rhf.h:22
 ]
 # declared in ops_mat.h:5, 8, 11-12 but defined nowhere in the reference (the
 # definitions in ops_mat.cc:155-190 are commented out); the shim provides them
