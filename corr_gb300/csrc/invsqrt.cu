@@ -19,6 +19,8 @@
 // from l_0 = (t / c)^1/2.  Then unscaled steps until max|Z Y - I| stops
 // falling below 1e-14 (quadratic convergence).  Products of symmetric
 // iterates are symmetric up to rounding; the result is symmetrised.
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -27,6 +29,7 @@
 #include "abi_internal.h"
 #include "common.cuh"
 #include "dgemm_tc.h"
+#include "gemm_fp64.h"
 
 namespace corr {
 
@@ -96,6 +99,144 @@ __global__ void sumsq_kernel(const double* __restrict__ J, long long n, double* 
 
 constexpr int kSqBlocks = 256;
 
+// The whole computation for small orders (m < 256) in one cooperative launch:
+// ||J||_inf and ||J||_F (c = min of the two >= lambda_max, t = 10 tol
+// ||J||_inf), then the same iteration as the host loop below (scaled steps
+// following the bound l from l0 = (t / c)^1/2, then unscaled steps until
+// max|a^2 Z Y - I| stops falling below 1e-14), each product a grid-wide pass
+// of FP64 dot products over L2-resident matrices, grid.sync() between passes;
+// finally the certificate from Z itself: Z ~ (J/c)^-1/2 is symmetric, so
+// lambda_min(J) = c / ||Z||_2^2 >= c / r^2 with r its largest absolute row
+// sum (||Z||_2 <= (||Z||_1 ||Z||_inf)^1/2 = r); nothing is cut when that bound
+// exceeds 2t.  The control flow is computed identically by every thread
+// (reductions are read back from global slots after the syncs), so every
+// thread reaches every grid.sync().  done[0] = 1 when converged and
+// certified; out = (Z + Z^T) / (2 c^1/2).
+__global__ void __launch_bounds__(256) ns_small_kernel(const double* __restrict__ J, int m,
+                                                       double tol, double* Y, double* Z,
+                                                       double* T, double* Y2, double* Z2,
+                                                       double* __restrict__ out,
+                                                       unsigned long long* slots, double* fsum,
+                                                       int* done) {
+  namespace cg = cooperative_groups;
+  cg::grid_group grid = cg::this_grid();
+  const long long mm = (long long)m * m;
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long nth = (long long)gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  auto warp_max = [&](double v) {
+    for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
+    return v;
+  };
+  for (long long x = tid; x < 64; x += nth) slots[x] = 0ull;
+  if (tid == 0) fsum[0] = 0.0;
+  grid.sync();
+  // norms of J: slot 62 = max absolute row sum, fsum = sum of squares
+  double rmax = 0.0, sq = 0.0;
+  for (long long r = tid; r < m; r += nth) {
+    double rs = 0.0;
+    for (int k = 0; k < m; ++k) {
+      const double v = J[r * m + k];
+      rs += fabs(v);
+      sq += v * v;
+    }
+    rmax = fmax(rmax, rs);
+  }
+  rmax = warp_max(rmax);
+  for (int off = 16; off > 0; off >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, off);
+  if (lane == 0) {
+    atomicMax(&slots[62], (unsigned long long)__double_as_longlong(rmax));
+    if (sq != 0.0) atomicAdd(fsum, sq);
+  }
+  grid.sync();
+  const double jinf = __longlong_as_double((long long)slots[62]);
+  const double cnorm = fmin(jinf, sqrt(fsum[0])), t = 10.0 * tol * jinf;
+  if (!(cnorm > 0.0) || !isfinite(cnorm)) {
+    if (tid == 0) done[0] = 0;
+    return;  // uniform: every thread read the same slots
+  }
+  const double rc = 1.0 / cnorm;
+  for (long long x = tid; x < mm; x += nth) {
+    Y[x] = J[x] * rc;
+    Z[x] = (x / m) == (x % m) ? 1.0 : 0.0;
+  }
+  grid.sync();
+  double l = sqrt(fmin(1.0, t * rc)), prev = 1e300;
+  bool conv = false;
+  for (int it = 0; it < 60; ++it) {
+    const bool scaled = l < 0.999;
+    const double a2 = scaled ? 3.0 / (1.0 + l + l * l) : 1.0, a = sqrt(a2);
+    double e = 0.0;
+    for (long long x = tid; x < mm; x += nth) {
+      const int i = (int)(x / m), j = (int)(x % m);
+      double acc = 0.0;
+      for (int k = 0; k < m; ++k) acc = fma(Z[(long long)i * m + k], Y[(long long)k * m + j], acc);
+      const double q = a2 * acc;
+      e = fmax(e, fabs(q - (i == j ? 1.0 : 0.0)));
+      T[x] = (i == j ? 1.5 : 0.0) - 0.5 * q;
+    }
+    e = warp_max(e);
+    if (lane == 0) atomicMax(&slots[it], (unsigned long long)__double_as_longlong(e));
+    grid.sync();
+    if (!scaled) {
+      const double err = __longlong_as_double((long long)slots[it]);
+      if (!isfinite(err)) break;
+      if (err < 1e-14 || (err >= 0.5 * prev && err < 1e-12)) {
+        conv = true;
+        break;
+      }
+      prev = err;
+    }
+    // Y2 = a Y T, Z2 = a T Z
+    for (long long x = tid; x < 2 * mm; x += nth) {
+      const bool zpart = x >= mm;
+      const long long y = zpart ? x - mm : x;
+      const int i = (int)(y / m), j = (int)(y % m);
+      double acc = 0.0;
+      if (!zpart)
+        for (int k = 0; k < m; ++k) acc = fma(Y[(long long)i * m + k], T[(long long)k * m + j], acc);
+      else
+        for (int k = 0; k < m; ++k) acc = fma(T[(long long)i * m + k], Z[(long long)k * m + j], acc);
+      (zpart ? Z2 : Y2)[y] = a * acc;
+    }
+    grid.sync();
+    double* tmp = Y;
+    Y = Y2;
+    Y2 = tmp;
+    tmp = Z;
+    Z = Z2;
+    Z2 = tmp;
+    if (scaled) {
+      const double xx = a * l;
+      l = fmin(1.0, 0.5 * xx * (3.0 - xx * xx));
+    }
+  }
+  if (!conv) {
+    if (tid == 0) done[0] = 0;
+    return;
+  }
+  // certificate: slot 63 = largest absolute row sum of Z
+  double zr = 0.0;
+  for (long long r = tid; r < m; r += nth) {
+    double rs = 0.0;
+    for (int k = 0; k < m; ++k) rs += fabs(Z[r * m + k]);
+    zr = fmax(zr, rs);
+  }
+  zr = warp_max(zr);
+  if (lane == 0) atomicMax(&slots[63], (unsigned long long)__double_as_longlong(zr));
+  grid.sync();
+  const double rz = __longlong_as_double((long long)slots[63]);
+  const bool certified = rz > 0.0 && cnorm / (rz * rz) > 2.0 * t;
+  if (certified) {
+    const double osc = 0.5 * sqrt(rc);
+    for (long long x = tid; x < mm; x += nth) {
+      const long long i = x / m, j = x % m;
+      out[x] = osc * (Z[x] + Z[j * m + i]);
+    }
+  }
+  if (tid == 0) done[0] = certified ? 1 : 0;
+}
+
 }  // namespace
 
 size_t ns_workspace_bytes(int m) {
@@ -117,6 +258,26 @@ int ri_inv_sqrt_ns(corr_context* c, void* ws, const double* J, int m, double tol
   void* dws = w.take(dgemm_tc_workspace(m, m, m));
   double* part = static_cast<double*>(w.take(kSqBlocks * 8));
   unsigned long long* derr = reinterpret_cast<unsigned long long*>(part);
+  if (m < 256) {
+    // small orders: norms, iteration and certificate in one cooperative launch
+    double* Y = static_cast<double*>(front);
+    double* Z = Y + mm;
+    double* T = Z + mm;
+    double* Y2 = static_cast<double*>(dws);
+    double* Z2 = Y2 + mm;
+    double* fsum = part + 64;
+    int* dflag = reinterpret_cast<int*>(part + 65);
+    void* args[] = {(void*)&J,  (void*)&m,  (void*)&tol, (void*)&Y,    (void*)&Z,    (void*)&T,
+                    (void*)&Y2, (void*)&Z2, (void*)&out, (void*)&derr, (void*)&fsum, (void*)&dflag};
+    CORR_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(ns_small_kernel),
+                                          dim3(c->sms), dim3(256), args, 0, s));
+    int hd = 0;
+    CORR_CUDA(cudaMemcpyAsync(&hd, dflag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CORR_CUDA(cudaStreamSynchronize(s));
+    c->launches += 1;
+    *done = hd == 1;
+    return CORR_OK;
+  }
   // norms and the certificate
   double jinf = 0.0;
   CORR_TRY(chol_norm_inf(c, part, J, m, &jinf));
@@ -166,13 +327,15 @@ int ri_inv_sqrt_ns(corr_context* c, void* ws, const double* J, int m, double tol
     CORR_CUDA(cudaMemsetAsync(derr, 0, 8, s));
     ns_step_kernel<<<grid, 256, 0, s>>>(P, m, a2, T, derr);
     CORR_CUDA(cudaGetLastError());
-    unsigned long long he = 0;
-    CORR_CUDA(cudaMemcpyAsync(&he, derr, 8, cudaMemcpyDeviceToHost, s));
-    CORR_CUDA(cudaStreamSynchronize(s));
-    double err;
-    std::memcpy(&err, &he, 8);
     c->launches += 1;
-    if (!std::isfinite(err)) return CORR_OK;
+    double err = 0.0;
+    if (!scaled) {  // the scaled steps follow the bound l; only the tail reads the error
+      unsigned long long he = 0;
+      CORR_CUDA(cudaMemcpyAsync(&he, derr, 8, cudaMemcpyDeviceToHost, s));
+      CORR_CUDA(cudaStreamSynchronize(s));
+      std::memcpy(&err, &he, 8);
+      if (!std::isfinite(err)) return CORR_OK;
+    }
     if (!scaled && (err < 1e-14 || (err >= 0.5 * prev && err < 1e-12))) {
       conv = true;  // converged: a further step only re-rounds
       break;
