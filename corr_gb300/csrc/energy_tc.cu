@@ -506,8 +506,20 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                              os, ss);
         }
       } else if (!dead && !same) {
+        // The terms of (a, b) and (b, a) are equal on a diagonal tile pair (the
+        // denominator is symmetric, x and y swap), so the block pairs {q, q-k}
+        // of round k (k = 1: four adjacent pairs; k = 2: pairs {0,2}, {1,3},
+        // taken by quarters 0 and 1) count twice and round 3 repeats round 1.
+        static_assert(EG == 1, "the round plan below assumes one group of four quarters");
+        double w1_os = 0.0, w1_ss = 0.0;
 #pragma unroll 1
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < 3; ++k) {
+          if (k == 1) {  // the diagonal blocks (weight 1) are in; the rest weigh 2
+            w1_os = os.d;
+            w1_ss = ss.d;
+            os.d = 0.0;
+            ss.d = 0.0;
+          }
           if (q % EG == g) {  // publisher
             float x[32];
             const int cw = 32 * ((q + k) & 3);
@@ -524,12 +536,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           }
           named_bar(2 + g, 128);
           const int wr = (q - k) & 3, cb = 32 * wr;
-          if (wr % EG == g && cb < ncol)  // reader
+          if (wr % EG == g && cb < ncol && (k < 2 || q < 2))  // reader
             chunk_pair_terms(tq + COL_STASH + (uint32_t)cb,
                              [&](int e) { return ctl->tbuf[g][wr / EG][e][lane]; }, da, ctl->db,
                              cb, os, ss);
           named_bar(2 + g, 128);  // tbuf is rewritten in the next round
         }
+        os.d = w1_os + 2.0 * os.d;
+        ss.d = w1_ss + 2.0 * ss.d;
       }
       // unit partial (weighted), reduced over the epilogue threads in a fixed
       // order; the host-side reduction sums the units in unit order
