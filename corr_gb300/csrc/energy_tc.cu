@@ -166,7 +166,7 @@ __device__ __forceinline__ float pick_chunk(const float* a, int s, int e) {
 // FP64 at the end.
 template <class Y>
 __device__ __forceinline__ void chunk_pair_terms(uint32_t xs, Y y, float2 da, const float2* db,
-                                                 int cb, FFSum& os, FFSum& ss) {
+                                                 int cb, FFSum2& os, FFSum2& ss) {
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     float x[16];
@@ -174,10 +174,12 @@ __device__ __forceinline__ void chunk_pair_terms(uint32_t xs, Y y, float2 da, co
     tc_wait_ld();
     ld_ready<16>(x);
 #pragma unroll
-    for (int e = 0; e < 16; ++e) {
-      float rh, rl;
-      recip_ff(da, db[cb + 16 * h + e], &rh, &rl);
-      pair_terms(x[e], y(16 * h + e), rh, rl, os, ss);
+    for (int e = 0; e < 16; e += 2) {
+      const float2 b0 = db[cb + 16 * h + e], b1 = db[cb + 16 * h + e + 1];
+      float2 rh, rl;
+      recip_ff2(da, make_float2(b0.x, b1.x), make_float2(b0.y, b1.y), &rh, &rl);
+      pair_terms2(make_float2(x[e], x[e + 1]), make_float2(y(16 * h + e), y(16 * h + e + 1)), rh,
+                  rl, os, ss);
     }
   }
   os.flush();
@@ -396,7 +398,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const float sca1 = alive ? in.sc[(size_t)i * v + a] : 0.0f;
       const float sca2 = alive ? in.sc[(size_t)j * v + a] : 0.0f;
       const bool diag_tile = same && (A == B);
-      FFSum os, ss;  // flushed to FP64 after every 32 columns
+      FFSum2 os, ss;  // flushed to FP64 after every 32 columns
       float d2a[32 * NCH];  // this group's chunks of D2 of a two-phase unit, this row
 
       // ---- phase 1: D1
@@ -442,11 +444,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               tc_wait_ld();
               ld_ready<32>(d1);
 #pragma unroll
-              for (int k = 0; k < 32; ++k) {
-                const float x = (diag_tile && c + k == arow) ? dga.x : d1[k];
-                float rh, rl;
-                recip_ff(da, ctl->db[c + k], &rh, &rl);
-                same_pair_term(x, rh, rl, os);
+              for (int k = 0; k < 32; k += 2) {
+                const float x0 = (diag_tile && c + k == arow) ? dga.x : d1[k];
+                const float x1 = (diag_tile && c + k + 1 == arow) ? dga.x : d1[k + 1];
+                const float2 b0 = ctl->db[c + k], b1 = ctl->db[c + k + 1];
+                float2 rh, rl;
+                recip_ff2(da, make_float2(b0.x, b1.x), make_float2(b0.y, b1.y), &rh, &rl);
+                same_pair_term2(make_float2(x0, x1), rh, rl, os);
               }
               os.flush();
             }
@@ -455,7 +459,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           if (diag_tile && alive && (q % EG) == g) {
             float rh, rl;
             recip_ff(da, ctl->db[arow], &rh, &rl);
-            os.add(4.0f * dga.x * dga.y * rh, 0.0f);
+            os.add(make_float2(4.0f * dga.x * dga.y * rh, 0.0f), make_float2(0.0f, 0.0f));
             os.flush();
           }
         }

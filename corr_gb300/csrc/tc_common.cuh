@@ -210,6 +210,79 @@ __device__ __forceinline__ void same_pair_term(float x, float rh, float rl, FFSu
   os.add(2.0f * th, 2.0f * tl);
 }
 
+// ---- the same arithmetic on two columns at once --------------------------
+// Blackwell's packed FP32 instructions (FADD2/FMUL2/FFMA2: two IEEE
+// round-to-nearest operations per instruction, each lane exactly as its scalar
+// counterpart), so every error-free transformation above holds per lane and
+// the epilogue issues half the instructions.
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
+
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2* s, float2* e) {
+  const float2 t = __fadd2_rn(a, b);
+  const float2 bb = __fadd2_rn(t, neg2(a));
+  *e = __fadd2_rn(__fadd2_rn(a, neg2(__fadd2_rn(t, neg2(bb)))), __fadd2_rn(b, neg2(bb)));
+  *s = t;
+}
+
+// 1/(da + db) for one row value da and two column values (bh + bl per lane).
+__device__ __forceinline__ void recip_ff2(float2 da, float2 bh, float2 bl, float2* rh,
+                                          float2* rl) {
+  float2 dh, dl;
+  two_sum2(dup2(da.x), bh, &dh, &dl);
+  dl = __fadd2_rn(dl, __fadd2_rn(dup2(da.y), bl));
+  float2 r0;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0.x) : "f"(dh.x));
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0.y) : "f"(dh.y));
+  float2 e = __ffma2_rn(neg2(dh), r0, dup2(1.0f));
+  e = __ffma2_rn(neg2(dl), r0, e);
+  *rh = r0;
+  *rl = __fmul2_rn(r0, e);
+}
+
+// FFSum with two independent lanes (each a float-float running sum).
+struct FFSum2 {
+  float2 h = make_float2(0.0f, 0.0f), l = make_float2(0.0f, 0.0f);
+  double d = 0.0;
+  __device__ __forceinline__ void add(float2 hi, float2 lo) {
+    float2 t, e;
+    two_sum2(h, hi, &t, &e);
+    h = t;
+    l = __fadd2_rn(l, __fadd2_rn(e, lo));
+  }
+  __device__ __forceinline__ void flush() {
+    d += ((double)h.x + (double)h.y) + ((double)l.x + (double)l.y);
+    h = make_float2(0.0f, 0.0f);
+    l = make_float2(0.0f, 0.0f);
+  }
+};
+
+// pair_terms on two columns.
+__device__ __forceinline__ void pair_terms2(float2 x, float2 y, float2 rh, float2 rl, FFSum2& os,
+                                            FFSum2& ss) {
+  const float2 px = __fmul2_rn(x, x), ex = __ffma2_rn(x, x, neg2(px));
+  const float2 py = __fmul2_rn(y, y), ey = __ffma2_rn(y, y, neg2(py));
+  float2 nh, nl;
+  two_sum2(px, py, &nh, &nl);
+  nl = __fadd2_rn(nl, __fadd2_rn(ex, ey));
+  float2 dh, dl;
+  two_sum2(x, neg2(y), &dh, &dl);
+  const float2 mh = __fmul2_rn(dh, dh);
+  const float2 ml = __ffma2_rn(__fmul2_rn(dup2(2.0f), dh), dl, __ffma2_rn(dh, dh, neg2(mh)));
+  const float2 th = __fmul2_rn(nh, rh);
+  os.add(th, __fadd2_rn(__ffma2_rn(nh, rh, neg2(th)), __ffma2_rn(nh, rl, __fmul2_rn(nl, rh))));
+  const float2 uh = __fmul2_rn(mh, rh);
+  ss.add(uh, __fadd2_rn(__ffma2_rn(mh, rh, neg2(uh)), __ffma2_rn(mh, rl, __fmul2_rn(ml, rh))));
+}
+
+// same_pair_term on two columns.
+__device__ __forceinline__ void same_pair_term2(float2 x, float2 rh, float2 rl, FFSum2& os) {
+  const float2 px = __fmul2_rn(x, x), ex = __ffma2_rn(x, x, neg2(px));
+  const float2 th = __fmul2_rn(px, rh);
+  const float2 tl = __fadd2_rn(__ffma2_rn(px, rh, neg2(th)), __ffma2_rn(px, rl, __fmul2_rn(ex, rh)));
+  os.add(__fmul2_rn(dup2(2.0f), th), __fmul2_rn(dup2(2.0f), tl));
+}
+
 // The MMAs of one K=16 step: r[l], q[l] are the row/column descriptors of
 // digit plane l; c0..c2 the three accumulators.  MMAs sharing a row operand
 // run back to back and keep it in the tensor core's A collector buffer (one
