@@ -114,10 +114,18 @@ __device__ __forceinline__ void load_level_sum16(uint32_t tb, int c, float inv_l
   ld_ready<16>(a0);
   ld_ready<16>(a1);
   ld_ready<16>(a2);
+  // two columns per packed instruction (each lane as the scalar expression
+  // fmaf(a2, inv_l2, fmaf(a1, inv_l, a0)) * (sca * scb))
 #pragma unroll
-  for (int k = 0; k < 16; ++k) {
-    const float t = fmaf(a2[k], inv_l2, fmaf(a1[k], inv_l, a0[k]));
-    d[k] = t * (sca * scb[c + k]);
+  for (int k = 0; k < 16; k += 2) {
+    const float2 t = __ffma2_rn(make_float2(a2[k], a2[k + 1]), make_float2(inv_l2, inv_l2),
+                                __ffma2_rn(make_float2(a1[k], a1[k + 1]),
+                                           make_float2(inv_l, inv_l),
+                                           make_float2(a0[k], a0[k + 1])));
+    const float2 sc = __fmul2_rn(make_float2(sca, sca), make_float2(scb[c + k], scb[c + k + 1]));
+    const float2 r = __fmul2_rn(t, sc);
+    d[k] = r.x;
+    d[k + 1] = r.y;
   }
 }
 
