@@ -80,29 +80,10 @@ __device__ __forceinline__ int unit_decode_cost(long long k, int o, int nt, int 
   return 1;
 }
 
-// 32 columns [c, c+32) of one phase's result in scaled FP32 units, from the
+// 16 columns [c, c+16) of one phase's result in scaled FP32 units, from the
 // three exact integer accumulators at columns tb, tb+128, tb+256 (levels 0, 1,
 // 2 of either scheme): d = acc0 + acc1/L + acc2/L^2.  Every step rounds to
 // nearest (CUDA cores), so no bias enters here.
-template <int SCHEME>
-__device__ __forceinline__ void load_level_sum(uint32_t tb, int c, float inv_l, float inv_l2,
-                                               float sca, const float* scb, float* d) {
-  float a0[32], a1[32], a2[32];
-  tmem_ld32(tb + 0u + (uint32_t)c, a0);
-  tmem_ld32(tb + 128u + (uint32_t)c, a1);
-  tmem_ld32(tb + 256u + (uint32_t)c, a2);
-  tc_wait_ld();
-  ld_ready<32>(a0);
-  ld_ready<32>(a1);
-  ld_ready<32>(a2);
-#pragma unroll
-  for (int k = 0; k < 32; ++k) {
-    const float t = fmaf(a2[k], inv_l2, fmaf(a1[k], inv_l, a0[k]));
-    d[k] = t * (sca * scb[c + k]);
-  }
-}
-
-// As load_level_sum for 16 columns [c, c+16) (fewer live registers).
 template <int SCHEME>
 __device__ __forceinline__ void load_level_sum16(uint32_t tb, int c, float inv_l, float inv_l2,
                                                  float sca, const float* scb, float* d) {
@@ -166,63 +147,12 @@ __device__ __forceinline__ void recip_ff(float2 da, float2 db, float* rh, float*
   *rl = r0 * e;
 }
 
-// Running sum of float-float terms: h + l, with h updated by TwoSum (exact)
-// and l collecting the TwoSum errors and the terms' low parts in FP32.
-// flush() adds h + l to the FP64 total d and restarts: over m terms the FP32
-// roundings of l stay below m^2 2^-48 of the sum, so callers flush every 32
-// terms (a compensated sum in the sense of Kahan's, but carried to
-// float-float accuracy: plain Kahan summation in FP32 only reaches ~2^-23).
-struct FFSum {
-  float h = 0.0f, l = 0.0f;
-  double d = 0.0;
-  __device__ __forceinline__ void add(float hi, float lo) {
-    float t, e;
-    two_sum(h, hi, &t, &e);
-    h = t;
-    l += e + lo;
-  }
-  __device__ __forceinline__ void flush() {
-    d += (double)h + (double)l;
-    h = 0.0f;
-    l = 0.0f;
-  }
-};
-
-// Terms of one element (a, b) of a pair i != j with x = (ia|jb), y = (ib|ja)
-// (scaled FP32 values) and 1/D = rh + rl:
-//   E_OS += (x^2 + y^2)/D,  E_SS += (x - y)^2/D,
-// the squares and the difference error-free, the products with 1/D to
-// float-float accuracy.
-__device__ __forceinline__ void pair_terms(float x, float y, float rh, float rl, FFSum& os,
-                                           FFSum& ss) {
-  const float px = x * x, ex = fmaf(x, x, -px);
-  const float py = y * y, ey = fmaf(y, y, -py);
-  float nh, nl;
-  two_sum(px, py, &nh, &nl);
-  nl += ex + ey;
-  float dh, dl;
-  two_sum(x, -y, &dh, &dl);
-  const float mh = dh * dh;
-  const float ml = fmaf(dh, dh, -mh) + 2.0f * dh * dl;
-  const float th = nh * rh;
-  os.add(th, fmaf(nh, rh, -th) + fmaf(nh, rl, nl * rh));
-  const float uh = mh * rh;
-  ss.add(uh, fmaf(mh, rh, -uh) + fmaf(mh, rl, ml * rh));
-}
-
-// The term of one element of a pair i == j (D2 == D1 == x): E_OS += 2 x^2/D.
-__device__ __forceinline__ void same_pair_term(float x, float rh, float rl, FFSum& os) {
-  const float px = x * x, ex = fmaf(x, x, -px);
-  const float th = px * rh;
-  const float tl = fmaf(px, rh, -th) + fmaf(px, rl, ex * rh);
-  os.add(2.0f * th, 2.0f * tl);
-}
-
-// ---- the same arithmetic on two columns at once --------------------------
-// Blackwell's packed FP32 instructions (FADD2/FMUL2/FFMA2: two IEEE
-// round-to-nearest operations per instruction, each lane exactly as its scalar
-// counterpart), so every error-free transformation above holds per lane and
-// the epilogue issues half the instructions.
+// ---- two columns at once ---------------------------------------------------
+// The per-element arithmetic runs on Blackwell's packed FP32 instructions
+// (FADD2/FMUL2/FFMA2: two IEEE round-to-nearest operations per instruction,
+// each lane exactly as the scalar operation), so the error-free
+// transformations above hold per lane and the epilogue issues half the
+// instructions.
 __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
 __device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
 
@@ -248,7 +178,13 @@ __device__ __forceinline__ void recip_ff2(float2 da, float2 bh, float2 bl, float
   *rl = __fmul2_rn(r0, e);
 }
 
-// FFSum with two independent lanes (each a float-float running sum).
+// Running sum of float-float terms, two independent lanes: per lane h + l,
+// with h updated by TwoSum (exact) and l collecting the TwoSum errors and the
+// terms' low parts in FP32.  flush() adds both lanes to the FP64 total d and
+// restarts: over m terms per lane the FP32 roundings of l stay below
+// m^2 2^-48 of the sum, so callers flush every 32 columns (16 terms per lane)
+// -- a compensated sum in the sense of Kahan's, carried to float-float
+// accuracy (plain Kahan summation in FP32 only reaches ~2^-23).
 struct FFSum2 {
   float2 h = make_float2(0.0f, 0.0f), l = make_float2(0.0f, 0.0f);
   double d = 0.0;
@@ -265,7 +201,11 @@ struct FFSum2 {
   }
 };
 
-// pair_terms on two columns.
+// Terms of two elements (a, b) of a pair i != j with x = (ia|jb), y = (ib|ja)
+// (scaled FP32 values) and 1/D = rh + rl, per lane:
+//   E_OS += (x^2 + y^2)/D,  E_SS += (x - y)^2/D,
+// the squares and the difference error-free (FMA residuals, TwoSum), the
+// products with 1/D to float-float accuracy.
 __device__ __forceinline__ void pair_terms2(float2 x, float2 y, float2 rh, float2 rl, FFSum2& os,
                                             FFSum2& ss) {
   const float2 px = __fmul2_rn(x, x), ex = __ffma2_rn(x, x, neg2(px));
@@ -283,7 +223,8 @@ __device__ __forceinline__ void pair_terms2(float2 x, float2 y, float2 rh, float
   ss.add(uh, __fadd2_rn(__ffma2_rn(mh, rh, neg2(uh)), __ffma2_rn(mh, rl, __fmul2_rn(ml, rh))));
 }
 
-// same_pair_term on two columns.
+// The terms of two elements of a pair i == j (D2 == D1 == x), per lane:
+// E_OS += 2 x^2/D.
 __device__ __forceinline__ void same_pair_term2(float2 x, float2 rh, float2 rl, FFSum2& os) {
   const float2 px = __fmul2_rn(x, x), ex = __ffma2_rn(x, x, neg2(px));
   const float2 th = __fmul2_rn(px, rh);
