@@ -28,13 +28,13 @@
 // run at N = 64 (half the MMA work and half the column-operand bytes; the
 // rows stay 128, the padded rows being zeros in the digit layout).
 //
-// Energy arithmetic (tc_common.cuh, energy_terms): the denominators
+// Energy arithmetic (tc_common.cuh, pair_terms2): the denominators
 // D = (e_a - e_i) + (e_b - e_j) come from the FP64 orbital energies as
 // float-float pairs, 1/D is taken to ~2^-44 relative (one float-float
 // Newton-Raphson step), the squares and products are error-free (FMA
 // residuals), and the terms are summed in float-float over 32 columns, then
 // in FP64: the only rounding of FP32 size left in the energy is that of the
-// (ia|jb) values themselves.
+// (ia|jb) values themselves.  Two columns per packed FP32 instruction.
 //
 // CTA = 6 warps, persistent, one CTA per SM, units from a device work queue:
 //   warp 0     bulk-copy producer (lane 0 takes units and paces the stages;
