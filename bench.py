@@ -596,7 +596,7 @@ def run_batch(args):
         "config": {"workload": f"{len(items)} instances, nocc~U{{5..60}}, nvir=nocc*U{{4..8}}, "
                                "naux=round(3.5 nvir), seed 5005/5006",
                    "precision": prec, "policy": {"order": order, "stages": stages,
-                                                 "tiles": "narrow last tile" if tiles else "128",
+                                                 "tiles": "128",
                                                  "autotune_ms": tune_ms},
                    "b_bytes": int(sum(B.numel() * 8 for B, _, _, _ in items))},
         "tflops_algorithmic": flops / (ms * 1e-3) / 1e12,

@@ -189,16 +189,15 @@ class Context:
         check(self._L.corr_set_fp64_strict(self._h, 1 if strict else 0))
 
     def set_energy_tiles(self, tiles):
-        """1 (default): a last virtual tile of at most 64 columns runs 64 wide;
-        0: every tile 128 wide."""
+        """Accepts 0 or 1; no effect (every tile runs 128 wide)."""
         check(self._L.corr_set_energy_tiles(self._h, int(tiles)))
 
     def set_batch_policy(self, order, stages, tiles=1):
         check(self._L.corr_set_batch_policy(self._h, int(order), int(stages), int(tiles)))
 
     def batch_autotune(self, items, precision="split_bf16", cache=None):
-        """Pick the batched launch variant (unit order, pipeline stages, tile
-        shape) by timing them on this batch.  With a cache path, results are
+        """Pick the batched launch variant (unit order, pipeline stages) by
+        timing them on this batch.  With a cache path, results are
         stored per batch signature (sorted shape list) and reused without
         timing.  Returns (order, stages, tiles, ms)."""
         import hashlib

@@ -271,11 +271,12 @@ int corr_set_fp64_strict(corr_context* c, int strict) {
   return CORR_OK;
 }
 
+// Kept for callers of the earlier tile policy: both values now run every tile
+// 128 wide (energy_tc.cu says why).
 int corr_set_energy_tiles(corr_context* c, int tiles) {
   CORR_CHECK_ARG(c != nullptr, "null context");
   CORR_CHECK_ARG(tiles == 0 || tiles == 1,
                  "corr_set_energy_tiles: tiles must be 0 (128 wide) or 1 (narrow last tile)");
-  c->energy_tiles = tiles;
   return CORR_OK;
 }
 
@@ -511,7 +512,7 @@ int rimp2_energy_core(corr_context* c, Carver& w, int nocc, int nvir, int naux, 
     CORR_CUDA(prepare_energy_tc());
     c->attrs_set = true;
   }
-  const TcInst inst = make_tc_inst(sw, d_e, sh, Qp, c->energy_tiles == 1, 0);
+  const TcInst inst = make_tc_inst(sw, d_e, sh, Qp, 0);
   mark(c, 1);
   CORR_CUDA(launch_energy_tc(inst, fmt, scheme, 3, grid, partials, &c->dres->status, queue,
                              c->stream));

@@ -48,7 +48,6 @@ struct corr_context {
   float t_prepass = 0.f, t_kernel = 0.f, t_total = 0.f;
   long long launches = 0;
   bool attrs_set = false;  // one-time kernel attributes (kept out of graph capture)
-  int energy_tiles = 1;    // 1: a last virtual tile of <= 64 columns runs at N = 64
   int fp64_strict = 0;     // 1: the plain-form metric calls use FP64 GEMMs and Jacobi only
   // batched driver
   int batch_order = 1;   // 0 input order, 1 cost-descending

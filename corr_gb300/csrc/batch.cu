@@ -84,7 +84,7 @@ int grow_pinned(corr_context* c, size_t bytes) {
 
 // Enqueue one batched evaluation; energies (4 per caller instance) to `out`.
 int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int precision,
-                  double* out, int order_policy, int stages, int tiles) {
+                  double* out, int order_policy, int stages) {
   const bool tc = precision != CORR_PREC_FP64;
   // ---- plan: order and per-instance shapes
   std::vector<int> order(n);
@@ -192,7 +192,7 @@ int batch_enqueue(corr_context* c, int n, const corr_rimp2_instance* in, int pre
     const Shape& s = shp[k];
     CORR_CUDA(launch_slices(x.bia, x.naux, x.nocc, x.nvir, s.Qp, scheme, fmt, s.p, sws[k],
                             c->pre_stream[k % nside]));
-    htab[k] = make_tc_inst(sws[k], x.eps, s.sh, s.Qp, tiles == 1, ub);
+    htab[k] = make_tc_inst(sws[k], x.eps, s.sh, s.Qp, ub);
     horder[k] = order[k];
     ub += s.sh.nunits;
   }
@@ -262,8 +262,7 @@ int corr_rimp2_energy_batched_async(corr_context* c, int n, const corr_rimp2_ins
   CORR_TRY(check_batch(c, n, inst, precision));
   CORR_CHECK_ARG(is_device_ptr(energies_dev), "energies_dev must be a device pointer");
   CORR_CUDA(cudaSetDevice(c->device));
-  return batch_enqueue(c, n, inst, precision, energies_dev, c->batch_order, c->batch_stages,
-                       c->batch_tiles);
+  return batch_enqueue(c, n, inst, precision, energies_dev, c->batch_order, c->batch_stages);
 }
 
 int corr_rimp2_energy_batched(corr_context* c, int n, const corr_rimp2_instance* inst,
@@ -275,8 +274,7 @@ int corr_rimp2_energy_batched(corr_context* c, int n, const corr_rimp2_instance*
   double* dout = static_cast<double*>(c->batch_out.ptr);
   CORR_CUDA(cudaMemsetAsync(c->dres, 0, sizeof(ResultBlock), c->stream));
   mark(c, 0);
-  CORR_TRY(batch_enqueue(c, n, inst, precision, dout, c->batch_order, c->batch_stages,
-                         c->batch_tiles));
+  CORR_TRY(batch_enqueue(c, n, inst, precision, dout, c->batch_order, c->batch_stages));
   std::vector<double> h((size_t)n * 4);
   CORR_CUDA(cudaMemcpyAsync(h.data(), dout, (size_t)n * 32, cudaMemcpyDeviceToHost, c->stream));
   CORR_TRY(finish_results(c, 0));
@@ -304,35 +302,34 @@ int corr_rimp2_batch_autotune(corr_context* c, int n, const corr_rimp2_instance*
   CORR_CUDA(cudaEventCreate(&e0));
   CORR_CUDA(cudaEventCreate(&e1));
   float best = 1e30f;
-  int bo = c->batch_order, bs = c->batch_stages, bt = c->batch_tiles;
+  int bo = c->batch_order, bs = c->batch_stages;
+  const int bt = c->batch_tiles;  // no effect on the launch: reported back as set
   // the three-digit form always runs 2 stages: one stage value to try
-  const int orders[2] = {0, 1}, stages[2] = {3, 2}, tiles[2] = {1, 0};
+  const int orders[2] = {0, 1}, stages[2] = {3, 2};
   const int nst = precision == CORR_PREC_SPLIT_FP16 ? 2 : 1;
   int st = CORR_OK;
   for (int oi = 0; oi < 2 && st == CORR_OK; ++oi)
-    for (int si = 0; si < nst && st == CORR_OK; ++si)
-      for (int ti = 0; ti < 2 && st == CORR_OK; ++ti) {
-        const int so = orders[oi], ss = nst == 2 ? stages[si] : 2, stl = tiles[ti];
-        // one untimed warm-up, then the median of three timed runs
-        st = batch_enqueue(c, n, inst, precision, dout, so, ss, stl);
-        float t[3] = {0.f, 0.f, 0.f};
-        for (int r = 0; r < 3 && st == CORR_OK; ++r) {
-          if (cudaEventRecord(e0, c->stream) != cudaSuccess) st = CORR_ERR_CUDA;
-          if (st == CORR_OK) st = batch_enqueue(c, n, inst, precision, dout, so, ss, stl);
-          if (st == CORR_OK && (cudaEventRecord(e1, c->stream) != cudaSuccess ||
-                                cudaEventSynchronize(e1) != cudaSuccess ||
-                                cudaEventElapsedTime(&t[r], e0, e1) != cudaSuccess))
-            st = CORR_ERR_CUDA;
-        }
-        if (st != CORR_OK) break;
-        std::sort(t, t + 3);
-        if (t[1] < best) {
-          best = t[1];
-          bo = so;
-          bs = ss;
-          bt = stl;
-        }
+    for (int si = 0; si < nst && st == CORR_OK; ++si) {
+      const int so = orders[oi], ss = nst == 2 ? stages[si] : 2;
+      // one untimed warm-up, then the median of three timed runs
+      st = batch_enqueue(c, n, inst, precision, dout, so, ss);
+      float t[3] = {0.f, 0.f, 0.f};
+      for (int r = 0; r < 3 && st == CORR_OK; ++r) {
+        if (cudaEventRecord(e0, c->stream) != cudaSuccess) st = CORR_ERR_CUDA;
+        if (st == CORR_OK) st = batch_enqueue(c, n, inst, precision, dout, so, ss);
+        if (st == CORR_OK && (cudaEventRecord(e1, c->stream) != cudaSuccess ||
+                              cudaEventSynchronize(e1) != cudaSuccess ||
+                              cudaEventElapsedTime(&t[r], e0, e1) != cudaSuccess))
+          st = CORR_ERR_CUDA;
       }
+      if (st != CORR_OK) break;
+      std::sort(t, t + 3);
+      if (t[1] < best) {
+        best = t[1];
+        bo = so;
+        bs = ss;
+      }
+    }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (st == CORR_ERR_CUDA) {
@@ -343,7 +340,6 @@ int corr_rimp2_batch_autotune(corr_context* c, int n, const corr_rimp2_instance*
   CORR_TRY(corr_sync(c));  // a device-side timeout in any variant
   c->batch_order = bo;
   c->batch_stages = bs;
-  c->batch_tiles = bt;
   if (order_out) *order_out = bo;
   if (stages_out) *stages_out = bs;
   if (tiles_out) *tiles_out = bt;

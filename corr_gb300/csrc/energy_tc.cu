@@ -23,10 +23,13 @@
 // memory instead of a second pass.  On the (i==j, A==B) diagonal the element
 // (ia|ia) is replaced by its FP64 value.
 //
-// Narrow last tile: when an instance's last virtual tile holds at most 64
-// columns and the instance asks for it, units whose column tile is that tile
-// run at N = 64 (half the MMA work and half the column-operand bytes; the
-// rows stay 128, the padded rows being zeros in the digit layout).
+// Every tile runs 128 wide: the padded columns of the last virtual tile are
+// zeros in the digit layout and get column scale 0.  (A narrower last tile
+// needs a second MMA instruction descriptor, and on the issue path, which
+// runs in step with the tensor pipe, any descriptor that is not a kernel
+// parameter, a second copy of the issue loop, or predicated descriptor pairs
+// each cost more than the padded columns: 0.663 / 0.728 / 0.99 ms against
+// 0.613 ms for nocc=40, nvir=360, naux=1200.)
 //
 // Energy arithmetic (tc_common.cuh, pair_terms2): the denominators
 // D = (e_a - e_i) + (e_b - e_j) come from the FP64 orbital energies as
@@ -56,7 +59,6 @@ namespace corr {
 namespace {
 
 constexpr int TILE = kTcTile;                 // 128
-constexpr int NARROW = 64;                    // columns of a narrow last tile
 constexpr int KB = kSliceQ;                   // Q per stage (128-byte tile rows)
 constexpr int TILE_BYTES = TILE * KB * 2;     // 16 KB
 // Epilogue groups: EG groups of four warps (one per TMEM lane quarter); group
@@ -107,7 +109,6 @@ static_assert(smem_bytes<0, 2>() <= 227 * 1024, "shared memory");
 struct Work {
   int i, j, A, B;  // occupied pair and tile pair of the instance
   int nph;         // MMA phases: 1 (D2 from D1) or 2
-  int ncol;        // columns of the column tile (TILE, or NARROW)
 };
 
 // Table index of the instance that owns global unit u (the last instance
@@ -130,7 +131,6 @@ __device__ __forceinline__ Work work_at(long long u, const TcInst& one,
   Work w;
   w.nph = unit_decode_cost(u - in->unit_begin, in->o, in->ntiles, in->ntpairs, &w.i, &w.j, &w.A,
                            &w.B);
-  w.ncol = (in->narrow && w.B == in->ntiles - 1) ? NARROW : TILE;
   return w;
 }
 
@@ -186,10 +186,66 @@ __device__ __forceinline__ void chunk_pair_terms(uint32_t xs, Y y, float2 da, co
   ss.flush();
 }
 
+// Position in the operand ring: stage index and its mbarrier parity.
+struct StagePos {
+  int st;
+  uint32_t ph;
+};
+
+// One MMA phase: every Q block of the unit from the operand ring into the
+// level accumulators at TMEM columns tmem + {0, 128, 256}, each stage
+// released to the producer once its MMAs finish.  False when a wait failed.
+template <int SCHEME, int STAGES>
+__device__ __forceinline__ bool mma_phase(Ctl<STAGES>* ctl, uint64_t dbase, uint32_t tmem, int nkb,
+                                          uint32_t idesc, StagePos* pos, volatile int* abort,
+                                          int* status) {
+  using G = Geo<SCHEME, STAGES>;
+  constexpr int NPL = G::NPL, STAGE_BYTES = G::STAGE_BYTES;
+  const uint32_t c0 = tmem, c1 = tmem + 128u, c2 = tmem + 256u;
+  int st = pos->st;
+  uint32_t ph = pos->ph;
+  bool ok = true;
+  bool ready = false;  // the next stage's barrier, probed ahead of time
+  for (int kb = 0; kb < nkb; ++kb) {
+    if (!ready && !mbar_wait(&ctl->full[st], ph, abort, status)) {
+      ok = false;
+      break;
+    }
+    // (no tcgen05 fence: the bulk copies' mbarrier completion orders the
+    // shared-memory operands)
+    const uint64_t ds = dbase + (uint64_t)(((uint32_t)st * STAGE_BYTES) >> 4);
+    const int nst = st + 1 == STAGES ? 0 : st + 1;
+    const uint32_t nph = st + 1 == STAGES ? ph ^ 1 : ph;
+    ready = false;
+#pragma unroll
+    for (int kk = 0; kk < KB / 16; ++kk) {
+      uint64_t r[NPL], q[NPL];
+#pragma unroll
+      for (int p = 0; p < NPL; ++p) {
+        r[p] = ds + (uint64_t)((p * TILE_BYTES + kk * 32) >> 4);
+        q[p] = ds + (uint64_t)(((NPL + p) * TILE_BYTES + kk * 32) >> 4);
+      }
+      // while the MMAs queued so far run, probe the next stage (non-blocking),
+      // so the stage boundary costs no barrier latency
+      if (kk == KB / 16 - 1 && kb + 1 < nkb) ready = mbar_test_wait(&ctl->full[nst], nph);
+      const uint32_t acc = (kb | kk) ? 1u : 0u;
+      issue_digit_mmas<SCHEME>(c0, c1, c2, r, q, idesc, acc);
+    }
+    tc_commit(&ctl->empty[st]);  // stage reusable once these MMAs finish
+    if (++st == STAGES) {
+      st = 0;
+      ph ^= 1;
+    }
+  }
+  pos->st = st;
+  pos->ph = ph;
+  return ok;
+}
+
 template <int SCHEME, int STAGES, bool BATCH>
 __global__ void __launch_bounds__(NTHREADS, 1)
     energy_tc_kernel(TcInst one, const TcInst* __restrict__ tab, int ninst, long long total,
-                     uint32_t idesc_full, uint32_t idesc_narrow, double* __restrict__ partials,
+                     uint32_t idesc, double* __restrict__ partials,
                      int* status, unsigned long long* __restrict__ queue) {
   using G = Geo<SCHEME, STAGES>;
   constexpr int NPL = G::NPL, STAGE_BYTES = G::STAGE_BYTES;
@@ -250,12 +306,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       if (u < 0) break;
       TcInst in;
       const Work w = work_at<BATCH>(u, one, tab, ninst, &in);
-      const uint32_t colbytes = (uint32_t)w.ncol * KB * 2;
       for (int phs = 0; phs < w.nph && ok; ++phs) {
         const int x = phs == 0 ? w.i : w.j;  // row operand slab
         const int y = phs == 0 ? w.j : w.i;  // column operand slab
         const int slab = colop ? y : x, tile = colop ? w.B : w.A;
-        const uint32_t bytes = colop ? colbytes : (uint32_t)TILE_BYTES;
         for (int kb = 0; kb < in.nkb; ++kb) {
           bool got = true;
           if (lane == 0) got = mbar_wait(&ctl->empty[st], ph ^ 1, abort, status);
@@ -264,11 +318,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             break;
           }
           uint64_t* bar = &ctl->full[st];
-          if (lane == 0) mbar_expect_tx(bar, (uint32_t)NPL * (TILE_BYTES + colbytes));
+          if (lane == 0) mbar_expect_tx(bar, (uint32_t)(2 * NPL * TILE_BYTES));
           __syncwarp();
           if (lane < 2 * NPL)
             bulk_load(tiles + (size_t)st * STAGE_BYTES + (NPL * (colop ? 1 : 0) + l) * TILE_BYTES,
-                      in.S + slice_tile_offset(l, slab, kb, tile, in.nkb, in.ntiles, NPL), bytes,
+                      in.S + slice_tile_offset(l, slab, kb, tile, in.nkb, in.ntiles, NPL), TILE_BYTES,
                       bar);
           has[st] = true;
           last_ph[st] = ph;
@@ -289,8 +343,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      int st = 0;
-      uint32_t ph = 0;
+      StagePos ring{0, 0u};
       uint32_t nuse = 0;
       bool ok = true;
       // shared-memory descriptor of tile 0 of stage 0 (every tile address is
@@ -305,7 +358,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         if (u < 0) break;
         TcInst in;
         const Work w = work_at<BATCH>(u, one, tab, ninst, &in);
-        const uint32_t idesc = w.ncol == TILE ? idesc_full : idesc_narrow;
         const int nkb = in.nkb;
         for (int phs = 0; phs < w.nph && ok; ++phs) {
           if (!mbar_wait(&ctl->aempty, (nuse & 1) ^ 1, abort, status)) {
@@ -313,39 +365,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             break;
           }
           tc_fence_after();
-          const uint32_t c0 = tmem, c1 = tmem + 128u, c2 = tmem + 256u;
-          bool ready = false;  // the next stage's barrier, probed ahead of time
-          for (int kb = 0; kb < nkb; ++kb) {
-            if (!ready && !mbar_wait(&ctl->full[st], ph, abort, status)) {
-              ok = false;
-              break;
-            }
-            // (no tcgen05 fence: the bulk copies' mbarrier completion orders
-            // the shared-memory operands)
-            const uint64_t ds = dbase + (uint64_t)(((uint32_t)st * STAGE_BYTES) >> 4);
-            const int nst = st + 1 == STAGES ? 0 : st + 1;
-            const uint32_t nph = st + 1 == STAGES ? ph ^ 1 : ph;
-            ready = false;
-#pragma unroll
-            for (int kk = 0; kk < KB / 16; ++kk) {
-              uint64_t r[NPL], q[NPL];
-#pragma unroll
-              for (int p = 0; p < NPL; ++p) {
-                r[p] = ds + (uint64_t)((p * TILE_BYTES + kk * 32) >> 4);
-                q[p] = ds + (uint64_t)(((NPL + p) * TILE_BYTES + kk * 32) >> 4);
-              }
-              // while the MMAs queued so far run, probe the next stage
-              // (non-blocking), so the stage boundary costs no barrier latency
-              if (kk == KB / 16 - 1 && kb + 1 < nkb) ready = mbar_test_wait(&ctl->full[nst], nph);
-              const uint32_t acc = (kb | kk) ? 1u : 0u;
-              issue_digit_mmas<SCHEME>(c0, c1, c2, r, q, idesc, acc);
-            }
-            tc_commit(&ctl->empty[st]);  // stage reusable once these MMAs finish
-            if (++st == STAGES) {
-              st = 0;
-              ph ^= 1;
-            }
-          }
+          // the instruction descriptor stays a kernel parameter (see the header)
+          const bool pok =
+              mma_phase<SCHEME, STAGES>(ctl, dbase, tmem, nkb, idesc, &ring, abort, status);
+          if (!pok) ok = false;
           if (ok) tc_commit(&ctl->afull);
           ++nuse;
         }
@@ -378,7 +401,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       if (!all || u < 0) break;  // uniform: every thread read the same slot
       TcInst in;
       const Work w = work_at<BATCH>(u, one, tab, ninst, &in);
-      const int o = in.o, v = in.v, i = w.i, j = w.j, A = w.A, B = w.B, ncol = w.ncol;
+      const int o = in.o, v = in.v, i = w.i, j = w.j, A = w.A, B = w.B;
       const bool two = w.nph == 2, same = i == j;
       const float inv_l = (float)in.scale[1];
       const float inv_l2 = inv_l * inv_l;
@@ -387,7 +410,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         // phase-1 columns come from slab j; padded columns get scale 0 and a
         // finite denominator
         const int b = B0 + et;
-        const bool live = et < ncol && b < v;
+        const bool live = b < v;
         ctl->db[et] = live ? ff_split(in.eps[o + b] - in.eps[j]) : make_float2(1.0f, 0.0f);
         ctl->scb[et] = live ? in.sc[(size_t)j * v + b] : 0.0f;
       }
@@ -413,12 +436,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll 1
         for (int s = 0; s < NCH; ++s) {
           const int c = 32 * (g + EG * s);
-          if (c < ncol) {
-            float d1[32];
-            load_level_sum16<SCHEME>(tq, c, inv_l, inv_l2, sca1, ctl->scb, d1);
-            load_level_sum16<SCHEME>(tq, c + 16, inv_l, inv_l2, sca1, ctl->scb, d1 + 16);
-            tmem_st32(tq + COL_STASH + (uint32_t)c, d1);
-          }
+          float d1[32];
+          load_level_sum16<SCHEME>(tq, c, inv_l, inv_l2, sca1, ctl->scb, d1);
+          load_level_sum16<SCHEME>(tq, c + 16, inv_l, inv_l2, sca1, ctl->scb, d1 + 16);
+          tmem_st32(tq + COL_STASH + (uint32_t)c, d1);
         }
         tc_wait_st();
         tc_fence_before();
@@ -438,7 +459,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll 1
           for (int s = 0; s < NCH; ++s) {
             const int c = 32 * (g + EG * s);
-            if (c < ncol) {
+            {
               float d1[32];
               tmem_ld32(tq + COL_STASH + (uint32_t)c, d1);
               tc_wait_ld();
@@ -469,7 +490,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       // ---- phase 2: D2 (two-phase units): rows from slab j, columns from slab i
       if (two) {
         named_bar(1, NEPI);  // everyone is done with the phase-1 column scales
-        if (et < ncol && B0 + et < v) ctl->scb[et] = in.sc[(size_t)i * v + B0 + et];
+        if (B0 + et < v) ctl->scb[et] = in.sc[(size_t)i * v + B0 + et];
         named_bar(1, NEPI);
         got = !dead && mbar_wait(&ctl->afull, nuse & 1, abort, status);
         got = epi_agree(ctl, ctl->wok, (int)(nuse & 1), ew, lane, got);
@@ -481,11 +502,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll
           for (int s = 0; s < NCH; ++s) {
             const int c = 32 * (g + EG * s);
-            if (c < ncol) {
-              load_level_sum16<SCHEME>(tq, c, inv_l, inv_l2, sca2, ctl->scb, d2a + 32 * s);
-              load_level_sum16<SCHEME>(tq, c + 16, inv_l, inv_l2, sca2, ctl->scb,
-                                       d2a + 32 * s + 16);
-            }
+            load_level_sum16<SCHEME>(tq, c, inv_l, inv_l2, sca2, ctl->scb, d2a + 32 * s);
+            load_level_sum16<SCHEME>(tq, c + 16, inv_l, inv_l2, sca2, ctl->scb, d2a + 32 * s + 16);
           }
           tc_fence_before();
           __syncwarp();
@@ -499,15 +517,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       // A == B).  For D1^T, in round k every warp of the group whose lane
       // quarter c is one of the group's chunks publishes its D1 block of column
       // chunk (c+k)%4, and the warp of quarter q = (c+k)%4 takes it: the D1^T
-      // block of its column chunk c.  Chunks beyond a narrow tile are zeros.
+      // block of its column chunk c.
       if (!dead && !same && two) {
 #pragma unroll 1
         for (int s = 0; s < NCH; ++s) {
           const int cb = 32 * (g + EG * s);
-          if (cb < ncol)  // D2 from registers: a compile-time register choice per column
-            chunk_pair_terms(tq + COL_STASH + (uint32_t)cb,
-                             [&](int e) { return pick_chunk<NCH>(d2a, s, e); }, da, ctl->db, cb,
-                             os, ss);
+          // D2 from registers: a compile-time register choice per column
+          chunk_pair_terms(tq + COL_STASH + (uint32_t)cb,
+                           [&](int e) { return pick_chunk<NCH>(d2a, s, e); }, da, ctl->db, cb, os,
+                           ss);
         }
       } else if (!dead && !same) {
         // The terms of (a, b) and (b, a) are equal on a diagonal tile pair (the
@@ -527,20 +545,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           if (q % EG == g) {  // publisher
             float x[32];
             const int cw = 32 * ((q + k) & 3);
-            if (cw < ncol) {
-              tmem_ld32(tq + COL_STASH + (uint32_t)cw, x);
-              tc_wait_ld();
-              ld_ready<32>(x);
-            } else {
-#pragma unroll
-              for (int e = 0; e < 32; ++e) x[e] = 0.0f;
-            }
+            tmem_ld32(tq + COL_STASH + (uint32_t)cw, x);
+            tc_wait_ld();
+            ld_ready<32>(x);
 #pragma unroll
             for (int e = 0; e < 32; ++e) ctl->tbuf[g][q / EG][lane][e] = x[e];
           }
           named_bar(2 + g, 128);
           const int wr = (q - k) & 3, cb = 32 * wr;
-          if (wr % EG == g && cb < ncol && (k < 2 || q < 2))  // reader
+          if (wr % EG == g && (k < 2 || q < 2))  // reader
             chunk_pair_terms(tq + COL_STASH + (uint32_t)cb,
                              [&](int e) { return ctl->tbuf[g][wr / EG][e][lane]; }, da, ctl->db,
                              cb, os, ss);
@@ -591,9 +604,8 @@ cudaError_t launch_variant(const TcInst& one, const TcInst* tab, int n, long lon
                            int grid, double* partials, int* status, unsigned long long* queue,
                            cudaStream_t s) {
   const uint32_t idf = idesc_f16((uint32_t)fmt, TILE, TILE);
-  const uint32_t idn = idesc_f16((uint32_t)fmt, TILE, NARROW);
   energy_tc_kernel<SCHEME, STAGES, BATCH>
-      <<<grid, NTHREADS, smem_bytes<SCHEME, STAGES>(), s>>>(one, tab, n, total, idf, idn, partials,
+      <<<grid, NTHREADS, smem_bytes<SCHEME, STAGES>(), s>>>(one, tab, n, total, idf, partials,
                                                             status, queue);
   return cudaGetLastError();
 }
@@ -615,7 +627,7 @@ cudaError_t dispatch(const TcInst& one, const TcInst* tab, int n, long long tota
 }  // namespace
 
 TcInst make_tc_inst(const SliceWork& sw, const double* eps, const EnergyShape& sh, int Qp,
-                    bool narrow, long long unit_begin) {
+                    long long unit_begin) {
   TcInst t;
   t.S = sw.S;
   t.eps = eps;
@@ -629,8 +641,6 @@ TcInst make_tc_inst(const SliceWork& sw, const double* eps, const EnergyShape& s
   t.ntiles = sh.ntiles;
   t.ntpairs = sh.ntpairs;
   t.nkb = Qp / kSliceQ;
-  const int tail = sh.nvir % kTcTile;
-  t.narrow = (narrow && tail != 0 && tail <= NARROW) ? 1 : 0;
   return t;
 }
 

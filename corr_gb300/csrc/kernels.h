@@ -110,12 +110,9 @@ struct TcInst {
   long long unit_begin;  // first global unit of this instance
   long long nunits;
   int o, v, ntiles, ntpairs, nkb;
-  int narrow;            // 1: the last virtual tile (<= 64 columns) runs at N = 64
 };
-// narrow: the caller's tile policy; it takes effect only when nvir % 128 is
-// in 1..64.
 TcInst make_tc_inst(const SliceWork& sw, const double* eps, const EnergyShape& sh, int Qp,
-                    bool narrow, long long unit_begin);
+                    long long unit_begin);
 // Shared-memory attributes of every kernel variant (once per device, outside
 // stream capture).
 cudaError_t prepare_energy_tc();

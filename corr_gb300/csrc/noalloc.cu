@@ -168,7 +168,7 @@ extern "C" int corr_rimp2_energy_noalloc(int device, void* stream, int nocc, int
     const int fmt = format_for_scheme(scheme);
     const int p = slice_bits_for(Qp);
     CORR_CUDA(launch_slices(bia, naux, nocc, nvir, Qp, scheme, fmt, p, sw, s));
-    const TcInst inst = make_tc_inst(sw, eps, sh, Qp, true, 0);
+    const TcInst inst = make_tc_inst(sw, eps, sh, Qp, 0);
     CORR_CUDA(launch_energy_tc(inst, fmt, scheme, 3, grid, partials, &hdr->status, queue, s));
     if (launch_unit_reduce(partials, (int)sh.nunits, sw.scale, hdr->e, red_scratch,
                            reinterpret_cast<unsigned*>(queue + 1), s) < 0) {

@@ -175,12 +175,11 @@ int corr_rimp2_energy_batched_async(corr_context* ctx, int n, const corr_rimp2_i
  * the context remains usable. */
 int corr_selftest_wait_timeout(corr_context* ctx, int limit_ms);
 
-/* Tile shape of the tcgen05 energy kernel used by corr_rimp2_energy(_async),
- * corr_rimp2_energy_estimate and corr_rimp2_energy_from_3index (no
- * counterpart in the reference): 1 (the default) = when nvir % 128 is in
- * 1..64, the units whose column tile is the last virtual tile run 64 columns
- * wide (half the tensor-core work of a padded 128-wide tile); 0 = every tile
- * 128 wide.  Both give the same energies up to FP64 summation order. */
+/* Tile shape of the tcgen05 energy kernel (no counterpart in the reference).
+ * Accepts 0 or 1 and has no effect: every tile runs 128 wide, the padded
+ * columns of the last virtual tile being zeros.  (A narrower last tile needs
+ * a second MMA descriptor, which costs more on the issue path than the padded
+ * columns save.) */
 int corr_set_energy_tiles(corr_context* ctx, int tiles);
 
 /* FP64 arithmetic of the plain-form metric calls (no counterpart in the
@@ -192,14 +191,14 @@ int corr_set_energy_tiles(corr_context* ctx, int tiles);
 int corr_set_fp64_strict(corr_context* ctx, int strict);
 
 /* Launch variant of the batched kernel: unit order (0 = input order,
- * 1 = costliest instance first), shared-memory pipeline depth in stages of
- * one 64-wide Q block (2 or 3; the three-digit form always runs 2) and tile
- * shape (tiles as in corr_set_energy_tiles, per instance). */
+ * 1 = costliest instance first) and shared-memory pipeline depth in stages of
+ * one 64-wide Q block (2 or 3; the three-digit form always runs 2).  tiles (0
+ * or 1) is accepted and has no effect, as in corr_set_energy_tiles. */
 int corr_set_batch_policy(corr_context* ctx, int order, int stages, int tiles);
 
-/* Time every launch variant on this batch (order x stages x tiles; median of
- * three runs after a warm-up), keep the fastest in the context and report it
- * (any output pointer may be NULL). */
+/* Time every launch variant on this batch (order x stages; median of three
+ * runs after a warm-up), keep the fastest in the context and report it (any
+ * output pointer may be NULL; *tiles reports the value last set). */
 int corr_rimp2_batch_autotune(corr_context* ctx, int n, const corr_rimp2_instance* inst,
                               int precision, int* order, int* stages, int* tiles, float* ms);
 

@@ -42,10 +42,10 @@ def test_batched_policies_agree_and_autotune(ctx, tmp_path):
     sizes = O.synth_batch_sizes(24, 55)
     sizes = [(o, v, X) for (o, v, X) in sizes if o <= 25]  # keep the test quick
     items = _gpu_instances(sizes, 8)
-    assert any(0 < v % 128 <= 64 for (_, v, _) in sizes)  # the tile-shape choice matters
+    assert any(v % 128 != 0 for (_, v, _) in sizes)  # padded last tiles
     for prec in ("split_fp16", "split_bf16"):
-        for tiles in (1, 0):
-            base = None
+        base = None
+        for tiles in (1, 0):  # accepted, no effect
             for order in (0, 1):
                 for stages in (2, 3):
                     ctx.set_batch_policy(order, stages, tiles)
@@ -53,11 +53,6 @@ def test_batched_policies_agree_and_autotune(ctx, tmp_path):
                     if base is None:
                         base = got
                     assert got == base  # per-unit partials are reduced in a fixed order
-            if tiles == 1:
-                narrow = base
-        # narrow last tiles only drop padded zero terms
-        for a, b in zip(narrow, base):
-            assert abs(a - b) <= 1e-13 * abs(b), (prec, a, b)
     ctx.set_batch_policy(1, 3, 1)
     cache = str(tmp_path / "autotune.json")
     o1, s1, t1, ms1 = ctx.batch_autotune(items, "split_fp16", cache=cache)

@@ -149,22 +149,20 @@ def test_split_wide_dynamic_range(ctx, prec):
 @pytest.mark.parametrize("o,v,X", [(3, 64, 40), (5, 150, 70), (7, 300, 90), (4, 192, 50),
                                    (9, 257, 100)])
 @pytest.mark.parametrize("prec", ["split_fp16", "split_bf16"])
-def test_narrow_last_tile_matches_full_tiles(ctx, o, v, X, prec):
-    """nvir % 128 in 1..64: the units of the last virtual tile run 64 columns
-    wide (tiles = 1, the default) or padded to 128 (tiles = 0).  The digit
-    products are the same; only padded zero terms differ.  (257 leaves one
-    column in the last tile.)"""
+def test_padded_last_tile(ctx, o, v, X, prec):
+    """Last virtual tiles of 64, 22, 44, 64 and 1 columns padded to 128 (the
+    padded columns are zeros with column scale 0) against the oracle; the
+    tile setting is accepted and changes nothing."""
     B, eps = O.synth_rimp2(o, v, X, 61 + v)
-    narrow = ctx.rimp2_energy(B, eps, o, v, X, prec)
+    e1 = ctx.rimp2_energy(B, eps, o, v, X, prec)
     ctx.set_energy_tiles(0)
     try:
-        full = ctx.rimp2_energy(B, eps, o, v, X, prec)
+        e0 = ctx.rimp2_energy(B, eps, o, v, X, prec)
     finally:
         ctx.set_energy_tiles(1)
-    for a, b in zip(narrow.as_tuple(), full.as_tuple()):
-        assert abs(a - b) <= 1e-13 * abs(full.e_total), (prec, narrow, full)
+    assert e1.as_tuple() == e0.as_tuple()
     ref = O.rimp2_energy(B, eps, o, v)
-    assert abs(narrow.e_total - ref[2]) <= 2e-7 * abs(ref[2]), (prec, narrow, ref)
+    assert abs(e1.e_total - ref[2]) <= 2e-7 * abs(ref[2]), (prec, e1, ref)
 
 
 def _exact_digit_inputs(o, v, X, seed):
