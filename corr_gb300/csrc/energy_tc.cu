@@ -459,22 +459,20 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll 1
           for (int s = 0; s < NCH; ++s) {
             const int c = 32 * (g + EG * s);
-            {
-              float d1[32];
-              tmem_ld32(tq + COL_STASH + (uint32_t)c, d1);
-              tc_wait_ld();
-              ld_ready<32>(d1);
+            float d1[32];
+            tmem_ld32(tq + COL_STASH + (uint32_t)c, d1);
+            tc_wait_ld();
+            ld_ready<32>(d1);
 #pragma unroll
-              for (int k = 0; k < 32; k += 2) {
-                const float x0 = (diag_tile && c + k == arow) ? dga.x : d1[k];
-                const float x1 = (diag_tile && c + k + 1 == arow) ? dga.x : d1[k + 1];
-                const float2 b0 = ctl->db[c + k], b1 = ctl->db[c + k + 1];
-                float2 rh, rl;
-                recip_ff2(da, make_float2(b0.x, b1.x), make_float2(b0.y, b1.y), &rh, &rl);
-                same_pair_term2(make_float2(x0, x1), rh, rl, os);
-              }
-              os.flush();
+            for (int k = 0; k < 32; k += 2) {
+              const float x0 = (diag_tile && c + k == arow) ? dga.x : d1[k];
+              const float x1 = (diag_tile && c + k + 1 == arow) ? dga.x : d1[k + 1];
+              const float2 b0 = ctl->db[c + k], b1 = ctl->db[c + k + 1];
+              float2 rh, rl;
+              recip_ff2(da, make_float2(b0.x, b1.x), make_float2(b0.y, b1.y), &rh, &rl);
+              same_pair_term2(make_float2(x0, x1), rh, rl, os);
             }
+            os.flush();
           }
           // 2 (xh + xl)^2 - 2 xh^2 = 4 xh xl + O(xl^2), by the group owning column arow
           if (diag_tile && alive && (q % EG) == g) {
