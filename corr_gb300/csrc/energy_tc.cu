@@ -86,6 +86,8 @@ struct Ctl {
   uint64_t ufull[RING];   // unit ring: producer -> MMA thread and epilogue
   uint64_t uempty[RING];
   long long uring[RING];
+  int unph[RING];         // the unit's MMA phases and Q blocks, for the MMA role
+  int unkb[RING];
   uint64_t afull;
   uint64_t aempty;
   uint64_t fin;
@@ -298,7 +300,17 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       if (lane == 0 && mbar_wait(&ctl->uempty[slot], (use & 1) ^ 1, abort, status)) {
         u = (long long)atomicAdd(queue, 1ull);
         if (u >= total) u = -1;
+        // the MMA role needs only the phase and Q-block counts: decoded here,
+        // off its issue path (which runs in step with the tensor pipe)
+        int nph = 0, nkb = 0;
+        if (u >= 0) {
+          TcInst in0;
+          nph = work_at<BATCH>(u, one, tab, ninst, &in0).nph;
+          nkb = in0.nkb;
+        }
         ctl->uring[slot] = u;
+        ctl->unph[slot] = nph;
+        ctl->unkb[slot] = nkb;
         mbar_arrive(&ctl->ufull[slot]);
       }
       u = __shfl_sync(0xffffffffu, u, 0);
@@ -354,12 +366,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const uint32_t use = (uint32_t)(t / RING);
         if (!mbar_wait(&ctl->ufull[slot], use & 1, abort, status)) break;
         const long long u = ctl->uring[slot];
+        const int nph = ctl->unph[slot], nkb = ctl->unkb[slot];
         mbar_arrive(&ctl->uempty[slot]);
         if (u < 0) break;
-        TcInst in;
-        const Work w = work_at<BATCH>(u, one, tab, ninst, &in);
-        const int nkb = in.nkb;
-        for (int phs = 0; phs < w.nph && ok; ++phs) {
+        for (int phs = 0; phs < nph && ok; ++phs) {
           if (!mbar_wait(&ctl->aempty, (nuse & 1) ^ 1, abort, status)) {
             ok = false;
             break;
